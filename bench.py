@@ -1,0 +1,319 @@
+"""Benchmark: frames/s and Gsamples/s of the GB300 raycaster on the CT-like
+shaded DVR workload (512^3 uint16, spacing 0.7/0.7/1.0, 4096-entry TF,
+Phong, 1920x1080, 2 samples/voxel), with the CPU path timed beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one frame. `value` is frames/s with the volume, TF and entry/exit
+images resident in HBM (device-timed with CUDA events on the library's
+stream); `e2e` is the same metric through the C ABI with host entry/exit
+images and a host RGBA8 frame (copies inside the timed region).
+`--impl reference` times the CPU path (the FP32 restatement of
+CPURaycaster in oracle/, all host threads) on a bounded sample of rows per
+step. One process per GPU; N > 1 runs N independent replicas (the path does
+not shard across GPUs).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "frames/s & Gsamples/s, 512³ u16 @1080p; learned vs plain fps at PSNR≥40 dB"
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def _barrier_max(value: float, ws: int):
+    if ws <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9 and f[1].replace(".", "").isdigit():
+                    rows.append(f)
+        except OSError:
+            pass
+        finally:
+            if self.path and os.path.exists(self.path):
+                os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": float(rows[0][2]), "reasons": reasons,
+                "samples": len(rows), "power_w_max": max(float(r[3]) for r in rows if r[3].replace('.', '').isdigit())}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def load_traffic():
+    """Per-launch DRAM bytes of the march kernel from the committed ncu
+    summary (profiles/), scaled per frame; None if absent."""
+    p = os.path.join(ROOT, "profiles", "march_dvr_phong_512cube_u16_1080p.json")
+    if os.path.exists(p):
+        try:
+            return json.load(open(p)).get("dram_bytes_per_launch")
+        except (OSError, ValueError):
+            return None
+    return None
+
+
+def build_workload(small: bool):
+    from voreen_gb300 import synth
+    if small:
+        return synth.config2(size=(256, 256, 256), image=(960, 540))
+    return synth.config2()
+
+
+def run_cpu(w, entry, exit_pts, target_s: float):
+    import oracle
+    import numpy as np
+    p = w.params()
+    op = oracle.make_params(sampling_rate=p.sampling_rate, compositing=p.compositing, shading=p.shading,
+                            iso_value=p.iso_value, ert=p.ert_threshold, light_pos=list(p.light_position)[:3],
+                            camera_pos=list(p.camera.position))
+    import voreen_gb300 as v
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    ov = oracle.make_volume(w.voxels, w.spacing)
+    H = w.height
+    threads = os.cpu_count() or 1
+    # calibrate on 2 centre rows, then size the band to ~target_s
+    r0 = H // 2 - 1
+    t0 = time.perf_counter()
+    _, s, _ = oracle.render(ov, tf, w.domain, op, entry, exit_pts, 32, rows=(r0, r0 + 2), nthreads=threads)
+    dt = max(time.perf_counter() - t0, 1e-3)
+    rows = int(max(2, min(H, 2 * target_s / dt)))
+    lo = max(0, H // 2 - rows // 2)
+    t0 = time.perf_counter()
+    _, s, _ = oracle.render(ov, tf, w.domain, op, entry, exit_pts, 32, rows=(lo, lo + rows), nthreads=threads)
+    dt = time.perf_counter() - t0
+    return dt, rows, int(s.sum()), threads, lo
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    args = ap.parse_args()
+    warmup = max(3, args.warmup)
+    ws, rank, local = _dist()
+    if args.impl == "reference" and rank != 0:
+        return  # the CPU reference runs on rank 0 only
+    if ws > 1 and args.impl == "ours":
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    import numpy as np
+
+    import voreen_gb300 as v
+
+    w = build_workload(args.small)
+    p = w.params()
+    npix = w.width * w.height
+    config = {"workload": w.name, "volume": list(w.dims), "dtype_volume": "uint16", "spacing": list(w.spacing),
+              "image": [w.width, w.height], "sampling_rate": w.sampling_rate, "tf_width": w.tf_width,
+              "shading": "phong", "compositing": "dvr", "ert": 0.95, "camera": "orbit 1.25 x box diagonal",
+              "l2": "inputs larger than L2 (bricked volume > 129 MB)", "replicas": ws}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        from voreen_gb300 import build as vbuild
+        vbuild.build()  # host-only entry points (camera matrices, TF bake); no GPU is used on this arm
+        import oracle
+        desc = v.make_desc(v.U16, w.dims, w.spacing)
+        _, _, inv = v.camera_matrices(p.camera, desc, w.width, w.height)
+        e, x = oracle.entry_exit(inv, w.width, w.height)
+        per_step = max(1.0, min(args.cpu_seconds, 150.0 / (warmup + args.steps)))
+        times, rates = [], []
+        for i in range(warmup + args.steps):
+            dt, rows, samples, threads, lo = run_cpu(w, e, x, per_step / 2 if i < warmup else per_step)
+            if i >= warmup:
+                times.append(dt * w.height / rows)  # seconds per full frame, extrapolated from the band
+                rates.append(samples / dt / 1e9)
+        t_frame = statistics.median(times)
+        fps = 1.0 / t_frame
+        line = {"impl": "reference", "metric": METRIC, "value": fps, "unit": "frames/s", "n_gpus": ws,
+                "steps": args.steps, "warmup": warmup, "ms_per_step": t_frame * 1e3, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": config,
+                "gsamples_per_s": statistics.median(rates),
+                "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                                 "sample": f"{rows} centre rows of the {w.width}x{w.height} frame per step, extrapolated "
+                                           f"to a full frame; FP32 CPURaycaster restatement, OpenMP over x per row"},
+                "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+    from voreen_gb300 import build as vbuild
+    vbuild.build()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = v.Context(dev)
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    # device-resident inputs: entry/exit images in HBM, RGBA8 frame in HBM
+    e_host, x_host = v.entry_exit(ctx, vol, p)
+    e_dev = torch.from_numpy(e_host).to(f"cuda:{dev}")
+    x_dev = torch.from_numpy(x_host).to(f"cuda:{dev}")
+    out_dev = torch.empty((w.height, w.width, 4), dtype=torch.uint8, device=f"cuda:{dev}")
+    torch.cuda.synchronize()
+
+    # per-frame stats (sample counts, kernel time) from untimed frames
+    _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
+    samples, shaded = st.samples, st.samples_shaded
+    kernel_ms = []
+    for _ in range(3):
+        _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
+        kernel_ms.append(st.kernel_ms)
+
+    for _ in range(warmup):
+        v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    _barrier(ws)
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        with torch.cuda.stream(stream):
+            start.record(stream)
+            for _ in range(args.steps):
+                v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
+            end.record(stream)
+        end.synchronize()
+        ctx.synchronize()
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    ms = start.elapsed_time(end) / args.steps
+    ms = _barrier_max(ms, ws)
+    fps_local = 1000.0 / ms
+    value = fps_local * ws
+
+    # e2e: host entry/exit in, host RGBA8 frame out, through the C ABI
+    e_pin = torch.from_numpy(e_host).pin_memory().numpy()
+    x_pin = torch.from_numpy(x_host).pin_memory().numpy()
+    o_pin = torch.empty((w.height, w.width, 4), dtype=torch.uint8).pin_memory().numpy()
+    for _ in range(2):
+        v.render(ctx, vol, tf, p, e_pin, x_pin, v.OUT_RGBA8, o_pin)
+    _barrier(ws)
+    t0 = time.perf_counter()
+    k_e2e = max(3, args.steps // 2)
+    for _ in range(k_e2e):
+        v.render(ctx, vol, tf, p, e_pin, x_pin, v.OUT_RGBA8, o_pin)
+    e2e_ms = (time.perf_counter() - t0) * 1e3 / k_e2e
+    e2e_ms = _barrier_max(e2e_ms, ws)
+
+    bpv = 2
+    b_alg = samples * 8 * bpv + shaded * 24 * bpv + npix * 4
+    k_ms = statistics.median(kernel_ms)
+    peak, peak_kind = measured_peaks()
+    achieved = b_alg / (k_ms * 1e-3) / 1e9
+    traffic = load_traffic()
+
+    line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded procedural 512^3 u16 CT-like shells)", "config": config,
+            "gsamples_per_s": samples / (ms * 1e-3) / 1e9 * ws,
+            "samples_per_frame": samples, "shaded_samples_per_frame": shaded,
+            "samples_fetched_per_frame": st.samples_fetched,
+            "kernel_ms": k_ms,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": b_alg,
+                         "note": "algorithmic bytes = 16 B/sample + 48 B/shaded sample + 4 B/pixel"},
+            "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "frames/s", "h2d_bytes_per_step": 2 * npix * 16,
+                    "d2h_bytes_per_step": npix * 4},
+            "gpu_launches": 2 * args.steps,
+            "clocks": clocks,
+            "volume_upload_bytes": int(w.voxels.nbytes), "volume_device_bytes": vol.device_bytes}
+
+    if rank == 0 and ws == 1:
+        dt, rows, s_cpu, threads, lo = run_cpu(w, e_host, x_host, args.cpu_seconds)
+        cpu_fps = 1.0 / (dt * w.height / rows)
+        line["cpu_baseline"] = {"value": cpu_fps, "unit": "frames/s", "cores": threads, "kind": "port",
+                                "sample": f"{rows} centre rows ({s_cpu} samples) of the same frame, extrapolated "
+                                          f"to {w.width}x{w.height}; FP32 CPURaycaster restatement",
+                                "gsamples_per_s": s_cpu / dt / 1e9}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

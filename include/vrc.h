@@ -1,0 +1,190 @@
+/*
+ * vrc -- GB300-native single-volume raycaster, C ABI.
+ *
+ * This is the drop-in boundary for Voreen's CPURaycaster / SingleVolumeRaycaster
+ * path. Every entry point takes plain pointers and sizes, returns a vrc_status
+ * and never throws. Handles own device memory; the caller owns host buffers.
+ * A context owns one CUDA stream; all work of a context is ordered on it.
+ *
+ * Reference interfaces each entry point replaces (paths in the Voreen tree):
+ *   vrc_volume_upload   VolumeGL upload of a VolumeRAM representation
+ *                       src/core/datastructures/volume/volumegl.cpp:126-168
+ *                       (+ brick min/max, optimizedproxygeometry.cpp:894-987)
+ *   vrc_volume_minmax   VolumeMinMax derived data used for TF domain fitting
+ *                       src/core/properties/transfunc/1d/1dkeys/transfunc1dkeysproperty.cpp:104-140
+ *   vrc_tf_bake_keys    TransFunc1D::createTextureData + TransFunc1DKeys::getMappingForValueUByte
+ *                       src/core/datastructures/transfunc/1d/transfunc1d.cpp:85-116,
+ *                       src/core/datastructures/transfunc/1d/1dkeys/transfunc1dkeys.cpp:119-154
+ *   vrc_tf_table_width  TransFuncPropertyBase::setVolume width rule + 4096 cap
+ *                       src/core/properties/transfunc/transfuncpropertybase.cpp:134-174,
+ *                       transfunc1dkeysproperty.cpp:94-97
+ *   vrc_tf_create       TransFuncBase::getTexture (RGBA8 table, NEAREST lookup)
+ *                       src/core/datastructures/transfunc/transfuncbase.cpp:99-161
+ *   vrc_render          CPURaycaster::process / directRendering
+ *                       modules/base/processors/render/cpuraycaster.cpp:90-331, and
+ *                       SingleVolumeRaycaster::process + rc_singlevolume.frag
+ *                       modules/base/processors/render/singlevolumeraycaster.cpp:246-425,
+ *                       modules/base/glsl/rc_singlevolume.frag:116-340
+ *   vrc_entry_exit      MeshEntryExitPoints::process on OptimizedProxyGeometry::processCube
+ *                       modules/base/processors/entryexitpoints/meshentryexitpoints.cpp:188-273,
+ *                       modules/base/processors/proxygeometry/optimizedproxygeometry.cpp:420-448
+ *   vrc_camera_matrices tgt::Camera::getViewMatrix / getProjectionMatrix
+ *                       ext/tgt/camera.cpp:133-216, ext/tgt/matrix.h:1196-1248
+ *
+ * Conventions: images are row-major with row 0 at the bottom (OpenGL window
+ * coordinates); entry/exit points are texture-space float4 (w = 1 on hit, the
+ * whole pixel 0 for background), as CPURaycaster downloads them.
+ */
+#ifndef VRC_H
+#define VRC_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VRC_ABI_VERSION 1
+
+typedef enum {
+    VRC_OK = 0,
+    VRC_ERR_INVALID_ARG = 1,   /* bad pointer, size, enum or dimension */
+    VRC_ERR_CUDA = 2,          /* a CUDA runtime call failed (see vrc_last_error) */
+    VRC_ERR_OUT_OF_MEMORY = 3, /* a device or host allocation was refused */
+    VRC_ERR_UNSUPPORTED = 4,   /* valid request the library does not implement */
+    VRC_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
+    VRC_ERR_NOT_READY = 6,     /* missing input (isReady() == false in the reference) */
+    VRC_ERR_DEVICE = 7         /* a kernel reported an internal error status */
+} vrc_status;
+
+typedef enum { VRC_U8 = 0, VRC_U16 = 1, VRC_F32 = 2 } vrc_dtype;
+typedef enum { VRC_DVR = 0, VRC_MIP = 1, VRC_ISO = 2 } vrc_compositing;
+typedef enum { VRC_SHADE_NONE = 0, VRC_SHADE_PHONG = 1 } vrc_shading;
+typedef enum { VRC_OUT_RGBA8 = 0, VRC_OUT_RGBA32F = 1, VRC_OUT_RGBA16 = 2 } vrc_out_format;
+typedef enum { VRC_EE_BUFFERS = 0, VRC_EE_ANALYTIC = 1 } vrc_entry_exit_mode;
+
+typedef struct vrc_context vrc_context;
+typedef struct vrc_volume vrc_volume;
+typedef struct vrc_tf vrc_tf;
+
+/* ---- context ---------------------------------------------------------- */
+vrc_status vrc_context_create(int device, vrc_context** out);
+vrc_status vrc_context_destroy(vrc_context* ctx);
+vrc_status vrc_context_synchronize(vrc_context* ctx);
+/* The context's cudaStream_t, for callers that order their own work with it. */
+void* vrc_context_stream(vrc_context* ctx);
+const char* vrc_status_string(vrc_status s);
+/* Human-readable detail of the last failing call on this context. */
+const char* vrc_last_error(const vrc_context* ctx);
+int vrc_abi_version(void);
+
+/* ---- volume ----------------------------------------------------------- */
+typedef struct {
+    int dtype;            /* vrc_dtype */
+    int dims[3];          /* voxels, x fastest (VolumeAtomic::calcPos) */
+    float spacing[3];     /* voxel size in physical units */
+    float offset[3];      /* physical position of voxel (0,0,0)'s lower corner + 0.5 spacing */
+    float rwm_scale;      /* RealWorldMapping: rw = normalized * scale + offset */
+    float rwm_offset;
+} vrc_volume_desc;
+
+/* Upload a linear x-fastest volume into the bricked device layout and build
+ * the per-brick min/max table. `voxels_on_device` != 0 means `voxels` is a
+ * device pointer. brick_size: 0 = default (32); otherwise 8, 16, 32 or 64. */
+vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels,
+                             int voxels_on_device, int brick_size, vrc_volume** out);
+vrc_status vrc_volume_destroy(vrc_volume* vol);
+/* Min/max of the normalised intensity (getVoxelNormalized) over the volume. */
+vrc_status vrc_volume_minmax(vrc_volume* vol, float* min_norm, float* max_norm);
+/* Brick grid and per-brick min/max of normalised intensity (core voxels plus
+ * one voxel on the high side, the trilinear support). out_* may be NULL to
+ * query nbricks only. */
+vrc_status vrc_volume_brick_minmax(vrc_volume* vol, int nbricks_out[3], float* out_min, float* out_max);
+/* Device bytes held by the bricked layout. */
+size_t vrc_volume_device_bytes(const vrc_volume* vol);
+
+/* ---- transfer function --------------------------------------------------- */
+typedef struct {
+    float intensity;      /* key position in [0,1] */
+    uint8_t color_l[4];   /* RGBA8 left of the key */
+    uint8_t color_r[4];   /* RGBA8 right of the key (== color_l unless split) */
+} vrc_tf_key;
+
+/* Host-only bake of a keyed 1D TF into a width x RGBA8 table. Keys must be
+ * sorted by intensity. gamma 1 and thresholds (0,1) are the defaults. */
+vrc_status vrc_tf_bake_keys(const vrc_tf_key* keys, int nkeys, int width, float gamma, float threshold_lo,
+                            float threshold_hi, uint8_t* out_rgba);
+/* TF table width for a volume dtype: 2^bits (float as 16 bit), capped at 4096. */
+int vrc_tf_table_width(int dtype);
+/* Device copy of a baked table with its real-world domain. width <= 4096. */
+vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float domain_lo, float domain_hi,
+                         vrc_tf** out);
+vrc_status vrc_tf_destroy(vrc_tf* tf);
+
+/* ---- camera ------------------------------------------------------------ */
+typedef struct {
+    float position[3], focus[3], up[3];  /* world coordinates */
+    float fovy_deg;                      /* vertical field of view */
+    float near_dist, far_dist;
+    float frustum_ratio;                 /* tgt::Frustum ratio, 1 by default */
+} vrc_camera;
+
+/* Row-major view, projection and inverse(projection * view * textureToWorld)
+ * for a W x H viewport, computed in double. Any output may be NULL. */
+vrc_status vrc_camera_matrices(const vrc_camera* cam, const vrc_volume_desc* vol, int width, int height,
+                               double* view, double* proj, double* inv_mvp_tex);
+
+/* ---- render ------------------------------------------------------------ */
+typedef struct {
+    int width, height;
+    float sampling_rate;        /* "samplingRate", default 2 */
+    int compositing;            /* vrc_compositing ("compositing": dvr / mip / iso) */
+    int shading;                /* vrc_shading ("shading": none / phong) */
+    float iso_value;            /* "isoValue", default 0.5 */
+    float ert_threshold;        /* 0.95; >= 1 disables early ray termination */
+    float light_position[4];    /* "lightPosition" (world), default (2.3, 1.5, 1.5, 1) */
+    float light_ambient[3];     /* "lightAmbient", default 0.4 */
+    float light_diffuse[3];     /* "lightDiffuse", default 0.8 */
+    float light_specular[3];    /* "lightSpecular", default 0.6 */
+    float material_shininess;   /* "materialShininess", default 60 */
+    int apply_attenuation;      /* "applyLightAttenuation", default 0 */
+    float light_attenuation[3]; /* "lightAttenuation", default (1, 0, 0) */
+    vrc_camera camera;          /* "camera": used for shading and analytic entry/exit */
+    int entry_exit_mode;        /* vrc_entry_exit_mode */
+    int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
+    int empty_space_skipping;   /* skip bricks whose TF opacity is zero (exact: results unchanged) */
+    int reserved[8];
+} vrc_render_params;
+
+/* Fills `p` with the reference's property defaults for a W x H image. */
+void vrc_render_params_default(vrc_render_params* p, int width, int height);
+
+typedef struct {
+    double samples;          /* loop iterations of all rays (the reference's sample count) */
+    double samples_fetched;  /* samples whose voxels were read (not skipped) */
+    double samples_shaded;   /* samples with TF alpha > 0 under shading */
+    float kernel_ms;         /* device time of the march kernel on the context stream */
+    float total_ms;          /* device time from first copy-in to last copy-out */
+    int device_status;       /* 0, or an internal error code from the kernel */
+} vrc_render_stats;
+
+/* Render one frame.
+ *   entry/exit: W*H float4 texture-space points (VRC_EE_BUFFERS), else ignored.
+ *   ee_on_device / out_on_device: 0 = host pointers (copied on the context
+ *   stream, call returns after the frame is on the host), 1 = device pointers
+ *   (call returns after the launch; synchronize before reading).
+ *   out: W*H pixels in `out_format`.
+ *   stats: may be NULL; sample counters need a synchronize, done when non-NULL. */
+vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                      const float* entry, const float* exit_pts, int ee_on_device, void* out, int out_format,
+                      int out_on_device, vrc_render_stats* stats);
+
+/* Analytic entry/exit points (texture space) for `p->camera`, written as
+ * float4 images, host or device destination. */
+vrc_status vrc_entry_exit(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, float* entry,
+                          float* exit_pts, int out_on_device);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

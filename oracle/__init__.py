@@ -1,0 +1,187 @@
+"""CPU oracle for the single-volume ray march -- TEST INFRASTRUCTURE ONLY.
+
+ctypes bindings over ``oracle/_build/liborc.so`` (oracle/cpu_raycaster.cpp),
+a C++ restatement of Voreen's CPURaycaster path plus the GLSL-only shading,
+MIP and ISO rules. Only tests, the smoke check and the benchmark's CPU
+baseline use it, as the checker; the product library never does.
+
+Parity status: the trilinear interpolation / normalisation and the camera
+matrices are pinned against the reference's own compiled code (golden
+vectors in tests/golden, made by tests/golden/make_golden.py through
+oracle/_ref). The TF bake and the march loop follow the cited reference
+lines but have no reference-produced golden outputs (parity unpinned for
+those parts).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+U8, U16, F32 = 0, 1, 2
+DVR, MIP, ISO = 0, 1, 2
+SHADE_NONE, SHADE_PHONG = 0, 1
+_DT = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
+
+
+class OrcVolume(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("dtype", C.c_int), ("dims", C.c_int * 3), ("spacing", C.c_float * 3),
+                ("offset", C.c_float * 3), ("rwm_scale", C.c_float), ("rwm_offset", C.c_float)]
+
+
+class OrcTF(C.Structure):
+    _fields_ = [("rgba", C.c_void_p), ("width", C.c_int), ("domain_lo", C.c_float), ("domain_hi", C.c_float)]
+
+
+class OrcParams(C.Structure):
+    _fields_ = [("sampling_rate", C.c_float), ("compositing", C.c_int), ("shading", C.c_int),
+                ("iso_value", C.c_float), ("ert_threshold", C.c_float), ("light_pos_phys", C.c_float * 3),
+                ("camera_pos_phys", C.c_float * 3), ("light_ambient", C.c_float * 3),
+                ("light_diffuse", C.c_float * 3), ("light_specular", C.c_float * 3), ("shininess", C.c_float),
+                ("apply_attenuation", C.c_int), ("attenuation", C.c_float * 3)]
+
+
+class OrcTFKey(C.Structure):
+    _fields_ = [("intensity", C.c_float), ("color_l", C.c_uint8 * 4), ("color_r", C.c_uint8 * 4)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = C.CDLL(path)
+        P = C.POINTER
+        L.oracle_bake_tf_keys.argtypes = [P(OrcTFKey), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_void_p]
+        L.oracle_entry_exit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        for name in ("oracle_render_f32", "oracle_render_f64"):
+            getattr(L, name).argtypes = [P(OrcVolume), P(OrcTF), P(OrcParams), C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.oracle_trilinear_f32.argtypes = [P(OrcVolume), C.c_void_p, C.c_int, C.c_void_p]
+        L.oracle_brick_minmax.argtypes = [P(OrcVolume), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def make_volume(vox: np.ndarray, spacing=(1, 1, 1), offset=(0, 0, 0), rwm=(1.0, 0.0)) -> OrcVolume:
+    """vox: (Z, Y, X) C-contiguous uint8/uint16/float32."""
+    assert vox.flags.c_contiguous and vox.ndim == 3
+    v = OrcVolume()
+    v.data = vox.ctypes.data
+    v.dtype = _DT[vox.dtype]
+    v.dims[:] = [vox.shape[2], vox.shape[1], vox.shape[0]]
+    v.spacing[:] = list(spacing)
+    v.offset[:] = list(offset)
+    v.rwm_scale, v.rwm_offset = rwm
+    v._keep = vox
+    return v
+
+
+def make_params(sampling_rate=2.0, compositing=DVR, shading=SHADE_NONE, iso_value=0.5, ert=0.95,
+                light_pos=(2.3, 1.5, 1.5), camera_pos=(0, 0, 3), ambient=(0.4,) * 3, diffuse=(0.8,) * 3,
+                specular=(0.6,) * 3, shininess=60.0, attenuation=None) -> OrcParams:
+    p = OrcParams()
+    p.sampling_rate = sampling_rate
+    p.compositing = compositing
+    p.shading = shading
+    p.iso_value = iso_value
+    p.ert_threshold = ert
+    p.light_pos_phys[:] = list(light_pos)[:3]
+    p.camera_pos_phys[:] = list(camera_pos)[:3]
+    p.light_ambient[:] = list(ambient)
+    p.light_diffuse[:] = list(diffuse)
+    p.light_specular[:] = list(specular)
+    p.shininess = shininess
+    p.apply_attenuation = 1 if attenuation is not None else 0
+    p.attenuation[:] = list(attenuation) if attenuation is not None else [1.0, 0.0, 0.0]
+    return p
+
+
+def bake_tf(keys, width, gamma=1.0, threshold=(0.0, 1.0)) -> np.ndarray:
+    """keys: list of (intensity, (r,g,b,a)) or (intensity, colorL, colorR)."""
+    arr = (OrcTFKey * max(1, len(keys)))()
+    for i, k in enumerate(keys):
+        arr[i].intensity = k[0]
+        arr[i].color_l[:] = list(k[1])
+        arr[i].color_r[:] = list(k[2] if len(k) > 2 else k[1])
+    out = np.zeros((width, 4), np.uint8)
+    lib().oracle_bake_tf_keys(arr, len(keys), width, gamma, threshold[0], threshold[1], _ptr(out))
+    return out
+
+
+def entry_exit(inv_mvp: np.ndarray, width: int, height: int, quantize16: bool = False):
+    m = np.ascontiguousarray(inv_mvp, dtype=np.float64)
+    e = np.zeros((height, width, 4), np.float32)
+    x = np.zeros((height, width, 4), np.float32)
+    lib().oracle_entry_exit(_ptr(m), width, height, 1 if quantize16 else 0, _ptr(e), _ptr(x))
+    return e, x
+
+
+def render(vol: OrcVolume, tf_rgba: np.ndarray, domain, params: OrcParams, entry: np.ndarray, exit_pts: np.ndarray,
+           precision: int = 32, rows=None, nthreads: int = 0):
+    """Returns (rgba (H,W,4), samples (H,W) int32, first_hit (H,W))."""
+    H, W = entry.shape[:2]
+    tf_rgba = np.ascontiguousarray(tf_rgba, dtype=np.uint8)
+    tf = OrcTF()
+    tf.rgba = tf_rgba.ctypes.data
+    tf.width = tf_rgba.shape[0]
+    tf.domain_lo, tf.domain_hi = domain
+    e = np.ascontiguousarray(entry, dtype=np.float32)
+    x = np.ascontiguousarray(exit_pts, dtype=np.float32)
+    ft = np.float32 if precision == 32 else np.float64
+    out = np.zeros((H, W, 4), ft)
+    samples = np.zeros((H, W), np.int32)
+    fh = np.full((H, W), -1, ft)
+    r0, r1 = (0, H) if rows is None else rows
+    fn = lib().oracle_render_f32 if precision == 32 else lib().oracle_render_f64
+    fn(C.byref(vol), C.byref(tf), C.byref(params), _ptr(e), _ptr(x), W, H, r0, r1, nthreads, _ptr(out),
+       _ptr(samples), _ptr(fh))
+    return out, samples, fh
+
+
+def trilinear(vol: OrcVolume, pos: np.ndarray) -> np.ndarray:
+    p = np.ascontiguousarray(pos, dtype=np.float32).reshape(-1, 3)
+    out = np.zeros(len(p), np.float32)
+    lib().oracle_trilinear_f32(C.byref(vol), _ptr(p), len(p), _ptr(out))
+    return out
+
+
+def brick_minmax(vol: OrcVolume, brick: int, apron_hi: int = 1):
+    nb = [(vol.dims[i] + brick - 1) // brick for i in range(3)]
+    mn = np.zeros(nb[0] * nb[1] * nb[2], np.float32)
+    mx = np.zeros_like(mn)
+    lib().oracle_brick_minmax(C.byref(vol), brick, apron_hi, _ptr(mn), _ptr(mx))
+    return mn, mx, nb
+
+
+# ---- the reference pin library (present only where the reference tree is) ----
+_ref = None
+
+
+def ref_lib(reference_root: str | None = None):
+    """The reference's own VolumeRAM trilinear + tgt math, or None."""
+    global _ref
+    if _ref is None:
+        path = _build.build_ref(reference_root or _build.DEFAULT_REFERENCE)
+        if path is None:
+            if os.path.exists(_build.REF_LIB):
+                path = _build.REF_LIB
+            else:
+                return None
+        L = C.CDLL(path)
+        L.ref_trilinear.argtypes = [C.c_int, C.c_void_p, C.POINTER(C.c_int), C.c_void_p, C.c_int, C.c_void_p]
+        L.ref_lookat.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_perspective.argtypes = [C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]
+        L.ref_iround.argtypes = [C.c_float]
+        L.ref_iround.restype = C.c_int
+        _ref = L
+    return _ref

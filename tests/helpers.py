@@ -1,0 +1,78 @@
+"""Shared helpers for the parity tests: run one case through the C ABI and
+through the oracle on identical inputs."""
+from __future__ import annotations
+
+import numpy as np
+
+import oracle
+import voreen_gb300 as v
+
+TOL = 1.0 / 255.0  # spec bound per RGBA channel against the FP64 oracle
+
+
+def oracle_params(w_params, light=None, cam=None):
+    p = w_params
+    return oracle.make_params(sampling_rate=p.sampling_rate, compositing=p.compositing, shading=p.shading,
+                              iso_value=p.iso_value, ert=p.ert_threshold,
+                              light_pos=list(p.light_position)[:3] if light is None else light,
+                              camera_pos=list(p.camera.position) if cam is None else cam,
+                              ambient=list(p.light_ambient), diffuse=list(p.light_diffuse),
+                              specular=list(p.light_specular), shininess=p.material_shininess,
+                              attenuation=list(p.light_attenuation) if p.apply_attenuation else None)
+
+
+def oracle_entry_exit(desc, params, quantize=False):
+    _, _, inv = v.camera_matrices(params.camera, desc, params.width, params.height)
+    return oracle.entry_exit(inv, params.width, params.height, quantize)
+
+
+class Case:
+    """One render on both sides. vox is (Z, Y, X)."""
+
+    def __init__(self, ctx, vox, tf_rgba, domain, params, spacing=(1, 1, 1), offset=(0, 0, 0), rwm=(1.0, 0.0),
+                 brick=0, entry=None, exit_pts=None):
+        self.ctx = ctx
+        self.vox = np.ascontiguousarray(vox)
+        self.tf_rgba = tf_rgba
+        self.domain = domain
+        self.params = params
+        self.spacing, self.offset, self.rwm = spacing, offset, rwm
+        self.vol = v.Volume(ctx, self.vox, spacing, offset, rwm, brick)
+        self.tf = v.TransferFunction(ctx, tf_rgba, domain)
+        if entry is None and params.entry_exit_mode == v.EE_BUFFERS:
+            entry, exit_pts = oracle_entry_exit(self.vol.desc, params)
+        self.entry, self.exit = entry, exit_pts
+        self.ovol = oracle.make_volume(self.vox, spacing, offset, rwm)
+
+    def gpu(self, out_format=v.OUT_RGBA32F, **over):
+        p = self.params
+        for k, val in over.items():
+            setattr(p, k, val)
+        return v.render(self.ctx, self.vol, self.tf, p, self.entry, self.exit, out_format)
+
+    def oracle(self, precision=32, rows=None, entry=None, exit_pts=None):
+        e = self.entry if entry is None else entry
+        x = self.exit if exit_pts is None else exit_pts
+        return oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params), e, x, precision, rows)
+
+
+def decision_divergent(s32, s64, fh32, fh64, comp):
+    """Rays where FP32 and FP64 take a different discrete decision: a
+    different number of samples (ERT step or the t > tend stop), or for MIP
+    and ISO a different selected sample."""
+    div = s32 != s64
+    if comp in (v.MIP, v.ISO):
+        div |= np.abs(fh32.astype(np.float64) - fh64) > 0
+    return div
+
+
+def assert_fp64_parity(gpu_img, s32, fh32, o64, s64, fh64, comp, max_div_frac=2e-3, tol=TOL):
+    """max |d| <= tol on every ray where FP32 and FP64 make the same discrete
+    decisions; the rest (reported) must be a tiny fraction of the hit rays."""
+    d = np.abs(gpu_img.astype(np.float64) - o64).max(axis=-1)
+    div = decision_divergent(s32, s64, fh32, fh64, comp)
+    hits = max(1, int((s32 > 0).sum()))
+    assert div.sum() <= max(2, max_div_frac * hits), f"{div.sum()} decision-divergent rays of {hits}"
+    ok = ~div
+    assert d[ok].max(initial=0.0) <= tol, f"max |d| on agreeing rays = {d[ok].max() * 255:.3f}/255"
+    return float(d[ok].max(initial=0.0)), int(div.sum())

@@ -1,0 +1,52 @@
+"""Oracle self-checks on the CPU: FP32 (faithful) against FP64, background
+and degenerate-ray rules, and the synthetic workload generators."""
+import numpy as np
+
+import oracle
+import voreen_gb300 as v
+from voreen_gb300 import synth
+
+from helpers import assert_fp64_parity, oracle_entry_exit, oracle_params
+
+
+def _run(w, **over):
+    p = w.params(**over)
+    desc = v.make_desc(v.U8 if w.voxels.dtype == np.uint8 else v.U16, w.dims, w.spacing)
+    e, x = oracle_entry_exit(desc, p)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    ov = oracle.make_volume(w.voxels, w.spacing)
+    op = oracle_params(p)
+    o32 = oracle.render(ov, tf, w.domain, op, e, x, 32)
+    o64 = oracle.render(ov, tf, w.domain, op, e, x, 64)
+    return o32, o64, e
+
+
+def test_fp32_vs_fp64_config1():
+    w = synth.config1(image=(256, 256))
+    (o32, s32, f32), (o64, s64, f64), e = _run(w)
+    assert s32.sum() > 100000
+    assert_fp64_parity(o32, s32, f32, o64, s64, f64, v.DVR)
+
+
+def test_fp32_vs_fp64_shaded_shells():
+    w = synth.config2(size=(80, 80, 80), image=(160, 120))
+    (o32, s32, f32), (o64, s64, f64), e = _run(w)
+    assert_fp64_parity(o32, s32, f32, o64, s64, f64, v.DVR)
+    assert (o32[..., 3] > 0.05).mean() > 0.05
+
+
+def test_background_rays_take_no_samples():
+    w = synth.config1(image=(64, 64))
+    (o32, s32, _), _, e = _run(w)
+    bg = (e == 0).all(axis=-1)
+    assert bg.any() and (s32[bg] == 0).all() and (o32[bg] == 0).all()
+
+
+def test_synth_is_deterministic_and_in_range():
+    a = v.synth_volume(1, v.U16, (40, 30, 20), 11)
+    b = v.synth_volume(1, v.U16, (40, 30, 20), 11)
+    c = v.synth_volume(1, v.U16, (40, 30, 20), 12)
+    assert (a == b).all() and not (a == c).all()
+    assert a.max() <= 4095
+    f = v.synth_volume(0, v.F32, (16, 16, 16), 3)
+    assert f.min() >= 0 and f.max() <= 1

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA march through the C ABI against the CPU oracle on the
+same seeded inputs. Unshaded paths must match the FP32 oracle bit for bit;
+every path must be within 1/255 per channel of the FP64 oracle on rays where
+FP32 and FP64 take the same discrete decisions."""
+import numpy as np
+import pytest
+
+import oracle
+import voreen_gb300 as v
+from voreen_gb300 import synth
+
+from helpers import Case, TOL, assert_fp64_parity, oracle_entry_exit
+
+pytestmark = pytest.mark.gpu
+
+
+def _bits(a):
+    return np.ascontiguousarray(a, dtype=np.float32).view(np.uint32)
+
+
+def _c1_case(ctx, **kw):
+    w = synth.config1(**kw)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    return w, Case(ctx, w.voxels, tf, w.domain, w.params(), w.spacing)
+
+
+def test_config1_full_size_bit_exact(ctx):
+    """Plain DVR, 128^3 u8, 512x512 (the CPU-runnable configuration)."""
+    w, c = _c1_case(ctx)
+    img, st = c.gpu()
+    o32, s32, fh32 = c.oracle(32)
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+    assert st.samples == s32.sum()
+    o64, s64, fh64 = c.oracle(64)
+    assert_fp64_parity(img, s32, fh32, o64, s64, fh64, v.DVR)
+
+
+@pytest.mark.parametrize("comp", [v.DVR, v.MIP, v.ISO])
+def test_ct_shells_unshaded_bit_exact(ctx, comp):
+    w = synth.config2(size=(96, 80, 72), image=(200, 150), compositing=comp)
+    p = w.params(shading=v.SHADE_NONE, iso_value=0.3)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing)
+    img, st = c.gpu()
+    o32, s32, fh32 = c.oracle(32)
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+    assert st.samples == s32.sum()
+    o64, s64, fh64 = c.oracle(64)
+    assert_fp64_parity(img, s32, fh32, o64, s64, fh64, comp)
+
+
+@pytest.mark.parametrize("comp", [v.DVR, v.ISO])
+def test_ct_shells_phong(ctx, comp):
+    """Phong + central differences: the gradient is computed from the brick
+    stencil (index shifts) instead of six texture-space lookups, so results
+    are close to, not bit-equal with, the FP32 oracle."""
+    w = synth.config2(size=(96, 96, 80), image=(220, 160), compositing=comp)
+    p = w.params(shading=v.SHADE_PHONG, iso_value=0.3)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing)
+    img, st = c.gpu()
+    o32, s32, fh32 = c.oracle(32)
+    assert st.samples == s32.sum()
+    assert st.samples_shaded > 0
+    assert np.abs(img - o32).max() <= 1e-4
+    o64, s64, fh64 = c.oracle(64)
+    assert_fp64_parity(img, s32, fh32, o64, s64, fh64, comp)
+
+
+def test_float_volume_and_rwm(ctx):
+    """float32 blobs with a non-identity real-world mapping and a domain."""
+    vox = v.synth_volume(0, v.F32, (40, 33, 27), 77)
+    keys = [(0.0, (0, 50, 200, 0)), (0.3, (20, 200, 40, 0)), (0.6, (220, 200, 10, 90)), (1.0, (255, 0, 0, 200))]
+    tf = v.TransferFunction.bake(keys, 4096)
+    p = v.default_params(96, 80)
+    p.camera = v.make_camera((60, 40, 90), (20, 16, 13))
+    rwm = (2.0, -0.25)
+    c = Case(ctx, vox, tf, (-0.2, 1.5), p, spacing=(1.2, 0.9, 1.1), rwm=rwm)
+    img, st = c.gpu()
+    o32, s32, fh32 = c.oracle(32)
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+
+
+@pytest.mark.parametrize("dims,brick", [((1, 1, 1), 8), ((2, 3, 5), 8), ((40, 40, 1), 16), ((17, 9, 33), 8),
+                                        ((65, 31, 7), 64), ((70, 70, 70), 32)])
+def test_odd_shapes_and_brick_sizes(ctx, dims, brick):
+    X, Y, Z = dims
+    rng = np.random.default_rng(X * 100 + Y * 10 + Z)
+    vox = rng.integers(0, 256, size=(Z, Y, X), dtype=np.uint8)
+    keys = [(0.0, (0, 0, 255, 0)), (0.2, (0, 255, 0, 40)), (1.0, (255, 0, 0, 200))]
+    tf = v.TransferFunction.bake(keys, 256)
+    p = v.default_params(64, 48)
+    diag = float(np.sqrt(X * X + Y * Y + Z * Z))
+    p.camera = v.make_camera((X * 0.5 + diag, Y * 0.5 + 0.6 * diag, Z * 0.5 + 1.2 * diag), (X / 2, Y / 2, Z / 2),
+                             near=0.1, far=10 * diag + 10)
+    p.sampling_rate = 3.0
+    c = Case(ctx, vox, tf, (0.0, 1.0), p, brick=brick)
+    img, st = c.gpu()
+    o32, s32, _ = c.oracle(32)
+    assert s32.sum() > 0
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+
+
+def test_empty_space_skipping_is_exact(ctx):
+    w = synth.config2(size=(128, 128, 128), image=(256, 192))
+    p = w.params(shading=v.SHADE_NONE)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing, brick=16)
+    a, sa = c.gpu(empty_space_skipping=1)
+    b, sb = c.gpu(empty_space_skipping=0)
+    np.testing.assert_array_equal(_bits(a), _bits(b))
+    assert sa.samples == sb.samples
+    assert sa.samples_fetched < 0.9 * sb.samples_fetched
+
+
+def test_brick_minmax_and_volume_minmax(ctx):
+    vox = v.synth_volume(1, v.U16, (70, 45, 33), 5)
+    vol = v.Volume(ctx, vox, brick_size=16)
+    mn, mx, nb = vol.brick_minmax()
+    ov = oracle.make_volume(vox)
+    omn, omx, onb = oracle.brick_minmax(ov, 16, 1)
+    assert tuple(nb) == tuple(onb)
+    np.testing.assert_array_equal(mn, omn)
+    np.testing.assert_array_equal(mx, omx)
+    lo, hi = vol.minmax()
+    assert lo == np.float32(vox.min()) / np.float32(65535) and hi == np.float32(vox.max()) / np.float32(65535)
+
+
+def test_analytic_entry_exit_matches_buffers(ctx):
+    """In-kernel analytic entry/exit equals rendering from the entry/exit
+    images the library writes; those agree with the FP64 oracle's rays."""
+    w = synth.config2(size=(64, 64, 64), image=(160, 120), compositing=v.DVR)
+    p = w.params(shading=v.SHADE_PHONG)
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing)
+    e, x = v.entry_exit(ctx, c.vol, p)
+    oe, ox = oracle_entry_exit(c.vol.desc, p)
+    hit = (e[..., 3] > 0) & (oe[..., 3] > 0)
+    assert ((e[..., 3] > 0) != (oe[..., 3] > 0)).sum() <= 0.002 * hit.sum() + 2
+    assert np.abs(e[hit] - oe[hit]).max() < 2e-5 and np.abs(x[hit] - ox[hit]).max() < 2e-5
+    pa = w.params(shading=v.SHADE_PHONG, entry_exit_mode=v.EE_ANALYTIC)
+    img_a, _ = v.render(ctx, c.vol, c.tf, pa, None, None, v.OUT_RGBA32F)
+    img_b, _ = v.render(ctx, c.vol, c.tf, p, e, x, v.OUT_RGBA32F)
+    np.testing.assert_array_equal(_bits(img_a), _bits(img_b))
+
+
+def test_output_formats(ctx):
+    w, c = _c1_case(ctx, size=(48, 40, 36), image=(96, 64))
+    f32, _ = c.gpu(v.OUT_RGBA32F)
+    u8, _ = c.gpu(v.OUT_RGBA8)
+    u16, _ = c.gpu(v.OUT_RGBA16)
+    q = lambda a, s: np.floor(np.clip(a, 0, 1) * np.float32(s) + np.float32(0.5))
+    np.testing.assert_array_equal(u8.astype(np.float32), q(f32, 255))
+    np.testing.assert_array_equal(u16.astype(np.float32), q(f32, 65535))
+
+
+def test_degenerate_and_background_rays(ctx):
+    """cpuraycaster.cpp:184 background (entry == exit == 0) and :226-227
+    degenerate rays (entry == exit != 0: one sample, tend = step / 2)."""
+    rng = np.random.default_rng(3)
+    vox = rng.integers(0, 256, size=(20, 20, 20), dtype=np.uint8)
+    tf = v.TransferFunction.bake([(0.0, (255, 255, 255, 255)), (1.0, (255, 0, 0, 255))], 256)
+    H, W = 8, 16
+    e = rng.uniform(0, 1, (H, W, 4)).astype(np.float32)
+    x = rng.uniform(0, 1, (H, W, 4)).astype(np.float32)
+    e[..., 3] = x[..., 3] = 1
+    e[0, :] = 0
+    x[0, :] = 0                      # background row
+    x[1, :] = e[1, :]                # degenerate rays
+    e[2, :, :3] = 0                  # entry at the origin, exit elsewhere
+    x[3, :, :3] = 0                  # exit at the origin
+    p = v.default_params(W, H)
+    c = Case(ctx, vox, tf, (0.0, 1.0), p, entry=e, exit_pts=x)
+    img, st = c.gpu()
+    o32, s32, _ = c.oracle(32)
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+    assert (s32[0] == 0).all() and (s32[1] == 1).all() and (img[0] == 0).all()
+
+
+def test_errors_are_statuses(ctx):
+    vox = np.zeros((4, 4, 4), np.uint8)
+    vol = v.Volume(ctx, vox)
+    tf = v.TransferFunction(ctx, np.zeros((256, 4), np.uint8))
+    p = v.default_params(8, 8)
+    with pytest.raises(v.VrcError) as ei:
+        v.render(ctx, vol, tf, p, None, None)       # buffer mode without entry/exit
+    assert ei.value.status == 6
+    p.sampling_rate = 0.0
+    e = np.zeros((8, 8, 4), np.float32)
+    with pytest.raises(v.VrcError) as ei:
+        v.render(ctx, vol, tf, p, e, e)
+    assert ei.value.status == 1
+    with pytest.raises(v.VrcError):
+        v.Volume(ctx, vox, brick_size=12)
+    with pytest.raises(v.VrcError):
+        v.TransferFunction(ctx, np.zeros((5000, 4), np.uint8))

@@ -1,0 +1,279 @@
+"""voreen_gb300 -- a GB300-native single-volume raycaster.
+
+Python view of the C ABI (include/vrc.h). The compute path is the in-tree
+CUDA library ``_build/libvrc.so``; there is no CPU fallback, and every call
+raises ``VrcError`` when the library reports a failure.
+
+Typical use (mirrors Voreen's CPURaycaster processor; see ``raycaster``)::
+
+    ctx = Context()
+    vol = Volume(ctx, voxels_zyx, spacing=(0.7, 0.7, 1.0))
+    tf = TransferFunction(ctx, TransferFunction.bake(keys, 4096), domain=(lo, hi))
+    p = default_params(1920, 1080)
+    img, stats = render(ctx, vol, tf, p, entry, exit_pts)
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import (DVR, EE_ANALYTIC, EE_BUFFERS, F32, ISO, MIP, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE,
+                   SHADE_PHONG, U8, U16, Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
+
+__all__ = ["VrcError", "Context", "Volume", "TransferFunction", "render", "entry_exit", "default_params",
+           "camera_matrices", "lib", "DVR", "MIP", "ISO", "SHADE_NONE", "SHADE_PHONG", "U8", "U16", "F32",
+           "OUT_RGBA8", "OUT_RGBA16", "OUT_RGBA32F", "EE_BUFFERS", "EE_ANALYTIC", "Camera", "RenderParams",
+           "RenderStats", "VolumeDesc", "TFKey"]
+
+_NP_DTYPE = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
+_DTYPE_NP = {U8: np.uint8, U16: np.uint16, F32: np.float32}
+
+
+def lib():
+    return _abi.load()
+
+
+class VrcError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def _check(status: int, ctx=None, what: str = ""):
+    if status != _abi.VRC_OK:
+        detail = ""
+        if ctx is not None and ctx.handle:
+            detail = (lib().vrc_last_error(ctx.handle) or b"").decode()
+        raise VrcError(status, f"{what}: {detail}" if detail else what)
+
+
+def _is_device(a) -> bool:
+    return hasattr(a, "data_ptr") and getattr(a, "is_cuda", False)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if _is_device(a):
+        return C.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One CUDA device and stream (vrc_context)."""
+
+    def __init__(self, device: int = 0):
+        self.handle = C.c_void_p()
+        _check(lib().vrc_context_create(device, C.byref(self.handle)), None, "vrc_context_create")
+        self.device = device
+
+    @property
+    def stream(self) -> int:
+        return lib().vrc_context_stream(self.handle) or 0
+
+    def synchronize(self):
+        _check(lib().vrc_context_synchronize(self.handle), self, "vrc_context_synchronize")
+
+    def close(self):
+        if self.handle:
+            lib().vrc_context_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_desc(dtype: int, dims_xyz, spacing=(1.0, 1.0, 1.0), offset=(0.0, 0.0, 0.0), rwm=(1.0, 0.0)) -> VolumeDesc:
+    d = VolumeDesc()
+    d.dtype = dtype
+    d.dims[:] = [int(v) for v in dims_xyz]
+    d.spacing[:] = [float(v) for v in spacing]
+    d.offset[:] = [float(v) for v in offset]
+    d.rwm_scale, d.rwm_offset = float(rwm[0]), float(rwm[1])
+    return d
+
+
+class Volume:
+    """A volume in the bricked device layout (vrc_volume).
+
+    ``voxels``: numpy (Z, Y, X) array (x fastest, VolumeAtomic::calcPos) of
+    uint8 / uint16 / float32, or a CUDA tensor of the same layout.
+    """
+
+    def __init__(self, ctx: Context, voxels, spacing=(1.0, 1.0, 1.0), offset=(0.0, 0.0, 0.0), rwm=(1.0, 0.0),
+                 brick_size: int = 0):
+        self.ctx = ctx
+        if _is_device(voxels):
+            import torch
+            dt = {torch.uint8: U8, torch.uint16: U16, torch.float32: F32}[voxels.dtype]
+            assert voxels.is_contiguous() and voxels.dim() == 3
+            shape = tuple(voxels.shape)
+        else:
+            voxels = np.ascontiguousarray(voxels)
+            dt = _NP_DTYPE[voxels.dtype]
+            shape = voxels.shape
+        self.desc = make_desc(dt, (shape[2], shape[1], shape[0]), spacing, offset, rwm)
+        self.handle = C.c_void_p()
+        _check(lib().vrc_volume_upload(ctx.handle, C.byref(self.desc), _ptr(voxels), 1 if _is_device(voxels) else 0,
+                                       brick_size, C.byref(self.handle)), ctx, "vrc_volume_upload")
+
+    @property
+    def dims(self):
+        return tuple(self.desc.dims)
+
+    @property
+    def dtype(self) -> int:
+        return self.desc.dtype
+
+    def minmax(self):
+        a, b = C.c_float(), C.c_float()
+        _check(lib().vrc_volume_minmax(self.handle, C.byref(a), C.byref(b)), self.ctx, "vrc_volume_minmax")
+        return a.value, b.value
+
+    def brick_minmax(self):
+        nb = (C.c_int * 3)()
+        _check(lib().vrc_volume_brick_minmax(self.handle, nb, None, None), self.ctx, "vrc_volume_brick_minmax")
+        n = nb[0] * nb[1] * nb[2]
+        mn = np.zeros(n, np.float32)
+        mx = np.zeros(n, np.float32)
+        _check(lib().vrc_volume_brick_minmax(self.handle, nb, _ptr(mn), _ptr(mx)), self.ctx, "vrc_volume_brick_minmax")
+        return mn, mx, tuple(nb)
+
+    @property
+    def device_bytes(self) -> int:
+        return int(lib().vrc_volume_device_bytes(self.handle))
+
+    def close(self):
+        if self.handle:
+            lib().vrc_volume_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class TransferFunction:
+    """A baked RGBA8 1D transfer function with its real-world domain (vrc_tf)."""
+
+    def __init__(self, ctx: Context, rgba: np.ndarray, domain=(0.0, 1.0)):
+        self.ctx = ctx
+        self.rgba = np.ascontiguousarray(rgba, dtype=np.uint8).reshape(-1, 4)
+        self.domain = (float(domain[0]), float(domain[1]))
+        self.handle = C.c_void_p()
+        _check(lib().vrc_tf_create(ctx.handle, _ptr(self.rgba), self.rgba.shape[0], self.domain[0], self.domain[1],
+                                   C.byref(self.handle)), ctx, "vrc_tf_create")
+
+    @staticmethod
+    def bake(keys, width: int, gamma: float = 1.0, threshold=(0.0, 1.0)) -> np.ndarray:
+        """Host-only TransFunc1DKeys bake. keys: [(intensity, rgba) or (intensity, rgbaL, rgbaR)]."""
+        arr = (TFKey * max(1, len(keys)))()
+        for i, k in enumerate(keys):
+            arr[i].intensity = float(k[0])
+            arr[i].color_l[:] = [int(v) for v in k[1]]
+            arr[i].color_r[:] = [int(v) for v in (k[2] if len(k) > 2 else k[1])]
+        out = np.zeros((width, 4), np.uint8)
+        _check(lib().vrc_tf_bake_keys(arr, len(keys), width, gamma, threshold[0], threshold[1], _ptr(out)), None,
+               "vrc_tf_bake_keys")
+        return out
+
+    @staticmethod
+    def table_width(dtype: int) -> int:
+        return int(lib().vrc_tf_table_width(dtype))
+
+    def close(self):
+        if self.handle:
+            lib().vrc_tf_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_params(width: int, height: int) -> RenderParams:
+    p = RenderParams()
+    lib().vrc_render_params_default(C.byref(p), width, height)
+    return p
+
+
+def make_camera(position, focus, up=(0.0, 1.0, 0.0), fovy=45.0, near=0.1, far=50.0, ratio=1.0) -> Camera:
+    c = Camera()
+    c.position[:] = [float(v) for v in position]
+    c.focus[:] = [float(v) for v in focus]
+    c.up[:] = [float(v) for v in up]
+    c.fovy_deg, c.near_dist, c.far_dist, c.frustum_ratio = fovy, near, far, ratio
+    return c
+
+
+def camera_matrices(cam: Camera, desc: VolumeDesc, width: int, height: int):
+    v = np.zeros(16, np.float64)
+    p = np.zeros(16, np.float64)
+    inv = np.zeros(16, np.float64)
+    _check(lib().vrc_camera_matrices(C.byref(cam), C.byref(desc), width, height, _ptr(v), _ptr(p), _ptr(inv)), None,
+           "vrc_camera_matrices")
+    return v.reshape(4, 4), p.reshape(4, 4), inv.reshape(4, 4)
+
+
+_OUT_NP = {OUT_RGBA8: (np.uint8, 4), OUT_RGBA16: (np.uint16, 4), OUT_RGBA32F: (np.float32, 4)}
+
+
+def render(ctx: Context, vol: Volume, tf: TransferFunction, params: RenderParams, entry=None, exit_pts=None,
+           out_format: int = OUT_RGBA32F, out=None):
+    """One frame. entry/exit: (H, W, 4) float32 host arrays or CUDA tensors
+    (ignored in analytic mode). Returns (image, RenderStats); image is `out`
+    if given (host array or CUDA tensor), else a new host array."""
+    H, W = params.height, params.width
+    if out is None:
+        dt, ch = _OUT_NP[out_format]
+        out = np.zeros((H, W, ch), dt)
+    ee_dev = 1 if (entry is not None and _is_device(entry)) else 0
+    if entry is not None and not ee_dev:
+        entry = np.ascontiguousarray(entry, dtype=np.float32)
+        exit_pts = np.ascontiguousarray(exit_pts, dtype=np.float32)
+    stats = RenderStats()
+    _check(lib().vrc_render(ctx.handle, vol.handle, tf.handle, C.byref(params), _ptr(entry), _ptr(exit_pts), ee_dev,
+                            _ptr(out), out_format, 1 if _is_device(out) else 0, C.byref(stats)), ctx, "vrc_render")
+    return out, stats
+
+
+def render_async(ctx: Context, vol: Volume, tf: TransferFunction, params: RenderParams, entry, exit_pts, out,
+                 out_format: int = OUT_RGBA32F):
+    """Device-resident frame: enqueue only (no stats, no synchronize)."""
+    ee_dev = 1 if (entry is not None and _is_device(entry)) else 0
+    _check(lib().vrc_render(ctx.handle, vol.handle, tf.handle, C.byref(params), _ptr(entry), _ptr(exit_pts), ee_dev,
+                            _ptr(out), out_format, 1, None), ctx, "vrc_render")
+
+
+def entry_exit(ctx: Context, vol: Volume, params: RenderParams):
+    """Analytic entry/exit points for params.camera (host arrays)."""
+    H, W = params.height, params.width
+    e = np.zeros((H, W, 4), np.float32)
+    x = np.zeros((H, W, 4), np.float32)
+    _check(lib().vrc_entry_exit(ctx.handle, vol.handle, C.byref(params), _ptr(e), _ptr(x), 0), ctx, "vrc_entry_exit")
+    return e, x
+
+
+def synth_volume(kind: int, dtype: int, dims_xyz, seed: int) -> np.ndarray:
+    """Seeded procedural volume (vrc_synth_volume), returned as (Z, Y, X)."""
+    X, Y, Z = dims_xyz
+    out = np.empty((Z, Y, X), _DTYPE_NP[dtype])
+    d = (C.c_int * 3)(X, Y, Z)
+    if lib().vrc_synth_volume(kind, dtype, d, seed, _ptr(out)) != 0:
+        raise VrcError(1, "vrc_synth_volume: invalid arguments")
+    return out

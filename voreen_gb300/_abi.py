@@ -1,0 +1,97 @@
+"""ctypes view of the C ABI in include/vrc.h and include/vrc_synth.h.
+
+The shared library is the in-tree build ``voreen_gb300/_build/libvrc.so``.
+There is no fallback: if it is missing or cannot be loaded, loading raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libvrc.so")
+
+VRC_OK = 0
+STATUS_NAMES = {0: "VRC_OK", 1: "VRC_ERR_INVALID_ARG", 2: "VRC_ERR_CUDA", 3: "VRC_ERR_OUT_OF_MEMORY",
+                4: "VRC_ERR_UNSUPPORTED", 5: "VRC_ERR_TIMEOUT", 6: "VRC_ERR_NOT_READY", 7: "VRC_ERR_DEVICE"}
+U8, U16, F32 = 0, 1, 2
+DVR, MIP, ISO = 0, 1, 2
+SHADE_NONE, SHADE_PHONG = 0, 1
+OUT_RGBA8, OUT_RGBA32F, OUT_RGBA16 = 0, 1, 2
+EE_BUFFERS, EE_ANALYTIC = 0, 1
+
+
+class VolumeDesc(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("dims", C.c_int * 3), ("spacing", C.c_float * 3), ("offset", C.c_float * 3),
+                ("rwm_scale", C.c_float), ("rwm_offset", C.c_float)]
+
+
+class TFKey(C.Structure):
+    _fields_ = [("intensity", C.c_float), ("color_l", C.c_uint8 * 4), ("color_r", C.c_uint8 * 4)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("focus", C.c_float * 3), ("up", C.c_float * 3),
+                ("fovy_deg", C.c_float), ("near_dist", C.c_float), ("far_dist", C.c_float),
+                ("frustum_ratio", C.c_float)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("sampling_rate", C.c_float), ("compositing", C.c_int),
+                ("shading", C.c_int), ("iso_value", C.c_float), ("ert_threshold", C.c_float),
+                ("light_position", C.c_float * 4), ("light_ambient", C.c_float * 3),
+                ("light_diffuse", C.c_float * 3), ("light_specular", C.c_float * 3),
+                ("material_shininess", C.c_float), ("apply_attenuation", C.c_int),
+                ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
+                ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("reserved", C.c_int * 8)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("samples", C.c_double), ("samples_fetched", C.c_double), ("samples_shaded", C.c_double),
+                ("kernel_ms", C.c_float), ("total_ms", C.c_float), ("device_status", C.c_int)]
+
+
+# name -> (restype, argtypes); every symbol declared in include/*.h
+P = C.POINTER
+VP = C.c_void_p
+SIGNATURES = {
+    "vrc_abi_version": (C.c_int, []),
+    "vrc_status_string": (C.c_char_p, [C.c_int]),
+    "vrc_last_error": (C.c_char_p, [VP]),
+    "vrc_context_create": (C.c_int, [C.c_int, P(VP)]),
+    "vrc_context_destroy": (C.c_int, [VP]),
+    "vrc_context_synchronize": (C.c_int, [VP]),
+    "vrc_context_stream": (VP, [VP]),
+    "vrc_volume_upload": (C.c_int, [VP, P(VolumeDesc), VP, C.c_int, C.c_int, P(VP)]),
+    "vrc_volume_destroy": (C.c_int, [VP]),
+    "vrc_volume_minmax": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),
+    "vrc_volume_brick_minmax": (C.c_int, [VP, P(C.c_int), VP, VP]),
+    "vrc_volume_device_bytes": (C.c_size_t, [VP]),
+    "vrc_tf_bake_keys": (C.c_int, [P(TFKey), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, VP]),
+    "vrc_tf_table_width": (C.c_int, [C.c_int]),
+    "vrc_tf_create": (C.c_int, [VP, VP, C.c_int, C.c_float, C.c_float, P(VP)]),
+    "vrc_tf_destroy": (C.c_int, [VP]),
+    "vrc_camera_matrices": (C.c_int, [P(Camera), P(VolumeDesc), C.c_int, C.c_int, VP, VP, VP]),
+    "vrc_render_params_default": (None, [P(RenderParams), C.c_int, C.c_int]),
+    "vrc_render": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, C.c_int, VP, C.c_int, C.c_int, P(RenderStats)]),
+    "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
+    "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
+}
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load libvrc.so. Raises OSError/RuntimeError when it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"voreen_gb300 CUDA library not built: {path} is missing (run __graft_entry__.build())")
+    L = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L

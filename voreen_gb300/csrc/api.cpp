@@ -1,0 +1,687 @@
+// Host side of the C ABI (include/vrc.h): context, volume ingest, transfer
+// function bake and tables, camera matrices, and the frame driver that
+// replaces CPURaycaster::process (modules/base/processors/render/cpuraycaster.cpp:90-206).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "vrc_internal.h"
+
+using vrc::BrickLayout;
+using vrc::MarchParams;
+
+namespace {
+
+vrc_status fail(vrc_context* ctx, vrc_status s, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return s;
+}
+
+vrc_status cuda_fail(vrc_context* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    if (e == cudaErrorMemoryAllocation) return fail(ctx, VRC_ERR_OUT_OF_MEMORY, m);
+    return fail(ctx, VRC_ERR_CUDA, m);
+}
+
+#define VRC_CUDA(ctx, call)                                    \
+    do {                                                       \
+        cudaError_t e_ = (call);                               \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+// Grow-only device scratch owned by the context.
+cudaError_t ensure(void** p, size_t* cap, size_t need) {
+    if (*cap >= need && *p) return cudaSuccess;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    cudaError_t e = cudaMalloc(p, need);
+    if (e == cudaSuccess) *cap = need;
+    return e;
+}
+
+// ---- 4x4 row-major double matrices (tgt::Matrix4 semantics) ----
+struct M4 {
+    double m[16];
+};
+M4 mul(const M4& a, const M4& b) {
+    M4 r{};
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) {
+            double s = 0;
+            for (int k = 0; k < 4; ++k) s += a.m[4 * i + k] * b.m[4 * k + j];
+            r.m[4 * i + j] = s;
+        }
+    return r;
+}
+bool invert(const M4& in, M4& out) {
+    double a[4][8];
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 8; ++j) a[i][j] = j < 4 ? in.m[4 * i + j] : (j - 4 == i ? 1.0 : 0.0);
+    for (int c = 0; c < 4; ++c) {
+        int piv = c;
+        for (int r = c + 1; r < 4; ++r)
+            if (std::fabs(a[r][c]) > std::fabs(a[piv][c])) piv = r;
+        if (std::fabs(a[piv][c]) < 1e-300) return false;
+        if (piv != c)
+            for (int j = 0; j < 8; ++j) std::swap(a[c][j], a[piv][j]);
+        const double d = a[c][c];
+        for (int j = 0; j < 8; ++j) a[c][j] /= d;
+        for (int r = 0; r < 4; ++r)
+            if (r != c) {
+                const double f = a[r][c];
+                for (int j = 0; j < 8; ++j) a[r][j] -= f * a[c][j];
+            }
+    }
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j) out.m[4 * i + j] = a[i][j + 4];
+    return true;
+}
+
+void norm3(double v[3]) {
+    const double l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    if (l > 0) {
+        v[0] /= l;
+        v[1] /= l;
+        v[2] /= l;
+    }
+}
+void cross3(const double a[3], const double b[3], double r[3]) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// Matrix4::createLookAt (ext/tgt/matrix.h:1196-1209)
+M4 look_at(const float e[3], const float f[3], const float u[3]) {
+    double look[3] = {double(f[0]) - e[0], double(f[1]) - e[1], double(f[2]) - e[2]};
+    norm3(look);
+    double up[3] = {u[0], u[1], u[2]};
+    norm3(up);
+    double strafe[3];
+    cross3(look, up, strafe);
+    norm3(strafe);
+    double up2[3];
+    cross3(strafe, look, up2);
+    M4 r{};
+    for (int j = 0; j < 3; ++j) {
+        r.m[j] = strafe[j];
+        r.m[4 + j] = up2[j];
+        r.m[8 + j] = -look[j];
+    }
+    r.m[15] = 1;
+    M4 t{};
+    for (int i = 0; i < 4; ++i) t.m[5 * i] = 1;
+    t.m[3] = -e[0];
+    t.m[7] = -e[1];
+    t.m[11] = -e[2];
+    return mul(r, t);
+}
+
+// Matrix4::createPerspective (ext/tgt/matrix.h:1229-1247) as used by
+// Camera::getProjectionMatrix for PERSPECTIVE (ext/tgt/camera.cpp:196-205).
+M4 perspective(const vrc_camera& c, double window_ratio) {
+    double fovy = c.fovy_deg;
+    if (fovy < 6.0) fovy = 6.0;
+    if (fovy > 175.0) fovy = 175.0;
+    const double ratio = c.frustum_ratio > 0 ? c.frustum_ratio : 1.0;
+    const double deg = M_PI / 180.0;
+    double fov = fovy * deg;
+    if (window_ratio < 1.0) fov = std::atan(std::tan(fovy * deg / 2.0) / (window_ratio * ratio)) * 2.0;
+    const double aspect = ratio * window_ratio;
+    const double f = 1.0 / std::tan(fov / 2.0);
+    const double n = c.near_dist, fa = c.far_dist;
+    M4 r{};
+    r.m[0] = f / aspect;
+    r.m[5] = f;
+    r.m[10] = (n + fa) / (n - fa);
+    r.m[11] = (2.0 * fa * n) / (n - fa);
+    r.m[14] = -1.0;
+    return r;
+}
+
+// textureToWorld = physicalToWorld (identity) * voxelToPhysical * textureToVoxel
+// (src/core/datastructures/volume/volumebase.cpp:194-229).
+M4 texture_to_world(const vrc_volume_desc& d) {
+    M4 r{};
+    for (int i = 0; i < 3; ++i) {
+        r.m[5 * i] = double(d.spacing[i]) * d.dims[i];
+        r.m[4 * i + 3] = double(d.offset[i]) - 0.5 * d.spacing[i];
+    }
+    r.m[15] = 1;
+    return r;
+}
+
+bool valid_desc(const vrc_volume_desc* d) {
+    if (!d) return false;
+    if (d->dtype < VRC_U8 || d->dtype > VRC_F32) return false;
+    for (int i = 0; i < 3; ++i) {
+        if (d->dims[i] < 1 || d->dims[i] > 65536) return false;
+        if (!(d->spacing[i] > 0.f) || !std::isfinite(d->spacing[i])) return false;
+    }
+    return true;
+}
+
+int ilog2(int v) {
+    int s = 0;
+    while ((1 << s) < v) ++s;
+    return s;
+}
+
+}  // namespace
+
+extern "C" {
+
+int vrc_abi_version(void) { return VRC_ABI_VERSION; }
+
+const char* vrc_status_string(vrc_status s) {
+    switch (s) {
+        case VRC_OK: return "ok";
+        case VRC_ERR_INVALID_ARG: return "invalid argument";
+        case VRC_ERR_CUDA: return "CUDA error";
+        case VRC_ERR_OUT_OF_MEMORY: return "out of memory";
+        case VRC_ERR_UNSUPPORTED: return "unsupported";
+        case VRC_ERR_TIMEOUT: return "timeout";
+        case VRC_ERR_NOT_READY: return "not ready";
+        case VRC_ERR_DEVICE: return "device error";
+    }
+    return "unknown status";
+}
+
+const char* vrc_last_error(const vrc_context* ctx) { return ctx ? ctx->last_error.c_str() : "no context"; }
+
+vrc_status vrc_context_create(int device, vrc_context** out) {
+    if (!out) return VRC_ERR_INVALID_ARG;
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return VRC_ERR_CUDA;
+    if (device < 0 || device >= n) return VRC_ERR_INVALID_ARG;
+    vrc_context* c = new (std::nothrow) vrc_context();
+    if (!c) return VRC_ERR_OUT_OF_MEMORY;
+    c->device = device;
+    if ((e = cudaSetDevice(device)) != cudaSuccess || (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device)) != cudaSuccess) {
+        delete c;
+        return VRC_ERR_CUDA;
+    }
+    for (auto& ev : c->ev) {
+        if (cudaEventCreate(&ev) != cudaSuccess) {
+            vrc_context_destroy(c);
+            return VRC_ERR_CUDA;
+        }
+    }
+    if (cudaMalloc(&c->d_counters, 16 * sizeof(unsigned long long)) != cudaSuccess) {
+        vrc_context_destroy(c);
+        return VRC_ERR_OUT_OF_MEMORY;
+    }
+    *out = c;
+    return VRC_OK;
+}
+
+vrc_status vrc_context_destroy(vrc_context* c) {
+    if (!c) return VRC_ERR_INVALID_ARG;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& ev : c->ev)
+        if (ev) cudaEventDestroy(ev);
+    cudaFree(c->d_ee);
+    cudaFree(c->d_out);
+    cudaFree(c->d_occ);
+    cudaFree(c->d_prefix);
+    cudaFree(c->d_counters);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return VRC_OK;
+}
+
+vrc_status vrc_context_synchronize(vrc_context* c) {
+    if (!c) return VRC_ERR_INVALID_ARG;
+    VRC_CUDA(c, cudaStreamSynchronize(c->stream));
+    return VRC_OK;
+}
+
+void* vrc_context_stream(vrc_context* c) { return c ? (void*)c->stream : nullptr; }
+
+vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels, int on_device,
+                             int brick_size, vrc_volume** out) {
+    if (!ctx || !out || !voxels) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: null argument");
+    *out = nullptr;
+    if (!valid_desc(desc)) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: invalid volume descriptor");
+    if (brick_size == 0) brick_size = 32;
+    if (brick_size != 8 && brick_size != 16 && brick_size != 32 && brick_size != 64)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: brick_size must be 8, 16, 32 or 64");
+    VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+    vrc_volume* v = new (std::nothrow) vrc_volume();
+    if (!v) return fail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: host allocation");
+    v->ctx = ctx;
+    v->desc = *desc;
+    BrickLayout& L = v->L;
+    for (int i = 0; i < 3; ++i) {
+        L.dims[i] = desc->dims[i];
+        L.nb[i] = (desc->dims[i] + brick_size - 1) / brick_size;
+    }
+    L.B = brick_size;
+    L.shift = ilog2(brick_size);
+    L.S = brick_size + vrc::APRON_LO + vrc::APRON_HI;
+    L.brick_stride = (((long long)L.S * L.S * L.S) + 63) / 64 * 64;
+    const int bpv = vrc::dtype_bytes(desc->dtype);
+    const size_t nvox = (size_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
+    const size_t brick_bytes = (size_t)L.nbricks() * L.brick_stride * bpv;
+    void* staging = nullptr;
+    cudaError_t e = cudaSuccess;
+    auto cleanup = [&](vrc_status s, const std::string& m) {
+        if (staging) cudaFree(staging);
+        vrc_volume_destroy(v);
+        return fail(ctx, s, m);
+    };
+    if ((e = cudaMalloc(&v->d_bricks, brick_bytes)) != cudaSuccess)
+        return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: brick pool allocation failed");
+    if ((e = cudaMalloc((void**)&v->d_bmin, L.nbricks() * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&v->d_bmax, L.nbricks() * sizeof(float))) != cudaSuccess)
+        return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: min/max table allocation failed");
+    v->bytes = brick_bytes + 2 * L.nbricks() * sizeof(float);
+    const void* lin = voxels;
+    if (!on_device) {
+        if ((e = cudaMalloc(&staging, nvox * bpv)) != cudaSuccess)
+            return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: staging allocation failed");
+        if ((e = cudaMemcpyAsync(staging, voxels, nvox * bpv, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
+            return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: copy: ") + cudaGetErrorString(e));
+        lin = staging;
+    }
+    if ((e = vrc::launch_brick_build(lin, desc->dtype, L, v->d_bricks, ctx->stream)) != cudaSuccess ||
+        (e = vrc::launch_brick_minmax(v->d_bricks, desc->dtype, L, v->d_bmin, v->d_bmax, ctx->stream)) != cudaSuccess)
+        return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: kernel: ") + cudaGetErrorString(e));
+    std::vector<float> mn(L.nbricks()), mx(L.nbricks());
+    if ((e = cudaMemcpyAsync(mn.data(), v->d_bmin, mn.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaMemcpyAsync(mx.data(), v->d_bmax, mx.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream)) !=
+            cudaSuccess ||
+        (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+        return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: ") + cudaGetErrorString(e));
+    if (staging) cudaFree(staging);
+    staging = nullptr;
+    v->vmin = *std::min_element(mn.begin(), mn.end());
+    v->vmax = *std::max_element(mx.begin(), mx.end());
+    *out = v;
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_destroy(vrc_volume* v) {
+    if (!v) return VRC_ERR_INVALID_ARG;
+    if (v->ctx) cudaSetDevice(v->ctx->device);
+    cudaFree(v->d_bricks);
+    cudaFree(v->d_bmin);
+    cudaFree(v->d_bmax);
+    delete v;
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_minmax(vrc_volume* v, float* mn, float* mx) {
+    if (!v || !mn || !mx) return VRC_ERR_INVALID_ARG;
+    *mn = v->vmin;
+    *mx = v->vmax;
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_brick_minmax(vrc_volume* v, int nb[3], float* out_min, float* out_max) {
+    if (!v || !nb) return VRC_ERR_INVALID_ARG;
+    for (int i = 0; i < 3; ++i) nb[i] = v->L.nb[i];
+    if (!out_min && !out_max) return VRC_OK;
+    vrc_context* ctx = v->ctx;
+    VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+    const size_t n = v->L.nbricks() * sizeof(float);
+    if (out_min) VRC_CUDA(ctx, cudaMemcpy(out_min, v->d_bmin, n, cudaMemcpyDeviceToHost));
+    if (out_max) VRC_CUDA(ctx, cudaMemcpy(out_max, v->d_bmax, n, cudaMemcpyDeviceToHost));
+    return VRC_OK;
+}
+
+size_t vrc_volume_device_bytes(const vrc_volume* v) { return v ? v->bytes : 0; }
+
+vrc_status vrc_tf_bake_keys(const vrc_tf_key* keys, int nkeys, int width, float gamma, float threshold_lo,
+                            float threshold_hi, uint8_t* out) {
+    if (!out || width < 2 || width > 65536 || nkeys < 0 || (nkeys > 0 && !keys)) return VRC_ERR_INVALID_ARG;
+    for (int k = 1; k < nkeys; ++k)
+        if (keys[k].intensity < keys[k - 1].intensity) return VRC_ERR_INVALID_ARG;
+    // TransFunc1D::createTextureData (transfunc1d.cpp:85-116)
+    const int front_end = (int)std::floor(threshold_lo * float(width) + 0.5f);
+    const int back_start = (int)std::floor(threshold_hi * float(width) + 0.5f);
+    for (int x = 0; x < width; ++x) {
+        uint8_t* o = out + 4 * x;
+        if (x < front_end || x > back_start || nkeys == 0) {
+            std::memset(o, 0, 4);
+            continue;
+        }
+        float value = float(x) / float(width - 1);
+        if (gamma != 1.f) value = powf(value, gamma);
+        // TransFunc1DKeys::getMappingForValueUByte (transfunc1dkeys.cpp:119-154)
+        value = value < 0.f ? 0.f : (value > 1.f ? 1.f : value);
+        int k = 0;
+        while (k < nkeys && value > keys[k].intensity) ++k;
+        if (k == 0) {
+            std::memcpy(o, keys[0].color_l, 4);
+        } else if (k == nkeys) {
+            std::memcpy(o, keys[nkeys - 1].color_r, 4);
+        } else {
+            const vrc_tf_key& a = keys[k - 1];
+            const vrc_tf_key& b = keys[k];
+            const float fraction = (value - a.intensity) / (b.intensity - a.intensity);
+            for (int ch = 0; ch < 4; ++ch) {
+                const float diff = float(int(b.color_l[ch]) - int(a.color_r[ch]));
+                const float prod = diff * fraction;  // separate statements: no fused multiply-add
+                const float sum = float(a.color_r[ch]) + prod;
+                o[ch] = static_cast<uint8_t>(sum);
+            }
+        }
+    }
+    return VRC_OK;
+}
+
+int vrc_tf_table_width(int dtype) {
+    // bits per voxel, float treated as 16 bit, capped at 4096 entries
+    int bits = dtype == VRC_U8 ? 8 : 16;
+    int w = 1 << bits;
+    return w > 4096 ? 4096 : w;
+}
+
+vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float lo, float hi, vrc_tf** out) {
+    if (!ctx || !rgba || !out || width < 2 || width > 4096)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_tf_create: width must be in [2, 4096]");
+    if (!(lo <= hi) || !std::isfinite(lo) || !std::isfinite(hi))
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_tf_create: invalid domain");
+    *out = nullptr;
+    VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+    vrc_tf* t = new (std::nothrow) vrc_tf();
+    if (!t) return fail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_tf_create: host allocation");
+    t->ctx = ctx;
+    t->width = width;
+    t->lo = lo;
+    t->hi = hi;
+    t->h_rgba = new (std::nothrow) uint8_t[4 * width];
+    if (!t->h_rgba) {
+        delete t;
+        return fail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_tf_create: host allocation");
+    }
+    std::memcpy(t->h_rgba, rgba, 4 * width);
+    std::vector<int> prefix(width + 1, 0);
+    for (int i = 0; i < width; ++i) prefix[i + 1] = prefix[i] + (rgba[4 * i + 3] > 0 ? 1 : 0);
+    cudaError_t e = cudaMalloc(&t->d_prefix, (width + 1) * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_prefix, prefix.data(), (width + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        vrc_tf_destroy(t);
+        return cuda_fail(ctx, e, "vrc_tf_create");
+    }
+    *out = t;
+    return VRC_OK;
+}
+
+vrc_status vrc_tf_destroy(vrc_tf* t) {
+    if (!t) return VRC_ERR_INVALID_ARG;
+    if (t->ctx) cudaSetDevice(t->ctx->device);
+    for (auto& kv : t->tables) cudaFree(kv.second);
+    cudaFree(t->d_prefix);
+    delete[] t->h_rgba;
+    delete t;
+    return VRC_OK;
+}
+
+vrc_status vrc_camera_matrices(const vrc_camera* cam, const vrc_volume_desc* vol, int W, int H, double* view,
+                               double* proj, double* inv_mvp) {
+    if (!cam || W < 1 || H < 1) return VRC_ERR_INVALID_ARG;
+    if (inv_mvp && !valid_desc(vol)) return VRC_ERR_INVALID_ARG;
+    const M4 V = look_at(cam->position, cam->focus, cam->up);
+    const M4 P = perspective(*cam, double(W) / double(H));
+    if (view) std::memcpy(view, V.m, sizeof(V.m));
+    if (proj) std::memcpy(proj, P.m, sizeof(P.m));
+    if (inv_mvp) {
+        const M4 mvp = mul(mul(P, V), texture_to_world(*vol));
+        M4 inv;
+        if (!invert(mvp, inv)) return VRC_ERR_INVALID_ARG;
+        std::memcpy(inv_mvp, inv.m, sizeof(inv.m));
+    }
+    return VRC_OK;
+}
+
+void vrc_render_params_default(vrc_render_params* p, int W, int H) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->width = W;
+    p->height = H;
+    p->sampling_rate = 2.f;              // volumeraycaster.cpp:56
+    p->compositing = VRC_DVR;
+    p->shading = VRC_SHADE_NONE;
+    p->iso_value = 0.5f;                 // volumeraycaster.cpp:57
+    p->ert_threshold = 0.95f;            // mod_raysetup.frag:36
+    const float lp[4] = {2.3f, 1.5f, 1.5f, 1.f};  // volumerenderer.cpp:43-53
+    std::memcpy(p->light_position, lp, sizeof(lp));
+    for (int i = 0; i < 3; ++i) {
+        p->light_ambient[i] = 0.4f;
+        p->light_diffuse[i] = 0.8f;
+        p->light_specular[i] = 0.6f;
+    }
+    p->material_shininess = 60.f;
+    p->apply_attenuation = 0;
+    p->light_attenuation[0] = 1.f;
+    p->camera.up[1] = 1.f;
+    p->camera.position[2] = 3.f;
+    p->camera.fovy_deg = 45.f;
+    p->camera.near_dist = 0.1f;
+    p->camera.far_dist = 50.f;
+    p->camera.frustum_ratio = 1.f;
+    p->entry_exit_mode = VRC_EE_BUFFERS;
+    p->quantize_entry_exit = 0;
+    p->empty_space_skipping = 1;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Float4 TF table for a render: (r/255, g/255, b/255, alpha') with alpha' the
+// opacity-corrected alpha for DVR (cpuraycaster.cpp:291) and the plain alpha
+// for MIP / ISO.
+vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float4** out) {
+    uint32_t bits = 0;
+    std::memcpy(&bits, &kcorr, 4);
+    const auto key = std::make_pair(corrected ? 1 : 0, corrected ? bits : 0u);
+    auto it = tf->tables.find(key);
+    if (it != tf->tables.end()) {
+        *out = it->second;
+        return VRC_OK;
+    }
+    std::vector<float4> h(tf->width);
+    for (int i = 0; i < tf->width; ++i) {
+        const uint8_t* c = tf->h_rgba + 4 * i;
+        float a = float(c[3]) / 255.f;
+        if (corrected) a = 1.f - powf(1.f - a, kcorr);
+        h[i] = make_float4(float(c[0]) / 255.f, float(c[1]) / 255.f, float(c[2]) / 255.f, a);
+    }
+    float4* d = nullptr;
+    VRC_CUDA(ctx, cudaMalloc(&d, tf->width * sizeof(float4)));
+    cudaError_t e = cudaMemcpy(d, h.data(), tf->width * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        cudaFree(d);
+        return cuda_fail(ctx, e, "tf table upload");
+    }
+    tf->tables[key] = d;
+    *out = d;
+    return VRC_OK;
+}
+
+vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P) {
+    std::memset(&P, 0, sizeof(P));
+    const vrc_volume_desc& d = vol->desc;
+    P.bricks = vol->d_bricks;
+    P.L = vol->L;
+    const int maxdim = std::max(d.dims[0], std::max(d.dims[1], d.dims[2]));
+    // samplingStepSize = 1 / (max(dim) * samplingRate) (cpuraycaster.cpp:104)
+    P.step = 1.f / (float(maxdim) * p->sampling_rate);
+    for (int i = 0; i < 3; ++i) {
+        P.dimf[i] = float(d.dims[i]);
+        P.dim_m1[i] = float(d.dims[i]) - 1.f;
+        P.offs[i] = 1.f / float(d.dims[i]);
+        P.spacing[i] = d.spacing[i];
+        P.spacing_rcp_half[i] = (1.f / d.spacing[i]) * 0.5f;
+        P.vol_offset[i] = d.offset[i];
+        // physicalToWorld is the identity: physical == world
+        P.light_phys[i] = p->light_position[i];
+        P.cam_phys[i] = p->camera.position[i];
+        P.amb[i] = p->light_ambient[i];
+        P.dif[i] = p->light_diffuse[i];
+        P.spec[i] = p->light_specular[i];
+        P.att[i] = p->light_attenuation[i];
+    }
+    P.rwm_scale = d.rwm_scale;
+    P.rwm_offset = d.rwm_offset;
+    P.ert = p->ert_threshold;
+    P.iso = p->iso_value;
+    P.shininess = p->material_shininess;
+    P.atten_on = p->apply_attenuation;
+    P.W = p->width;
+    P.H = p->height;
+    P.ee_mode = p->entry_exit_mode;
+    P.quantize = p->quantize_entry_exit;
+    P.tiles_x = (p->width + 7) / 8;
+    P.tiles_y = (p->height + 3) / 4;
+    if (p->entry_exit_mode == VRC_EE_ANALYTIC) {
+        double inv[16];
+        if (vrc_camera_matrices(&p->camera, &d, p->width, p->height, nullptr, nullptr, inv) != VRC_OK)
+            return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: camera matrix is singular");
+        for (int i = 0; i < 16; ++i) P.inv_mvp[i] = float(inv[i]);
+    }
+    return VRC_OK;
+}
+
+vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
+    if (!p) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: null params");
+    if (p->width < 1 || p->height < 1 || (long long)p->width * p->height > (1LL << 28))
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: image size out of range");
+    if (!(p->sampling_rate > 0.f) || !std::isfinite(p->sampling_rate))
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: sampling_rate must be > 0");
+    if (p->compositing < VRC_DVR || p->compositing > VRC_ISO)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown compositing mode");
+    if (p->shading < VRC_SHADE_NONE || p->shading > VRC_SHADE_PHONG)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
+    if (p->entry_exit_mode != VRC_EE_BUFFERS && p->entry_exit_mode != VRC_EE_ANALYTIC)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown entry/exit mode");
+    return VRC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
+                      const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
+                      int out_on_device, vrc_render_stats* stats) {
+    if (!ctx) return VRC_ERR_INVALID_ARG;
+    if (!vol || !tf_c) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: volume and transfer function are required");
+    if (vol->ctx != ctx || tf_c->ctx != ctx) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: handle from another context");
+    vrc_status st = check_params(ctx, p);
+    if (st != VRC_OK) return st;
+    if (!out) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: null output");
+    if (out_format < VRC_OUT_RGBA8 || out_format > VRC_OUT_RGBA16)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown output format");
+    if (p->entry_exit_mode == VRC_EE_BUFFERS && (!entry || !exitp))
+        return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: entry/exit points are required in buffer mode");
+    vrc_tf* tf = const_cast<vrc_tf*>(tf_c);
+    VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+    MarchParams P;
+    if ((st = fill_params(ctx, vol, p, P)) != VRC_OK) return st;
+    const bool dvr = p->compositing == VRC_DVR;
+    const float kcorr = P.step * 200.f;  // SAMPLING_BASE_INTERVAL_RCP
+    float4* table = nullptr;
+    if ((st = tf_table(ctx, tf, dvr, kcorr, &table)) != VRC_OK) return st;
+    P.tf_table = table;
+    P.tf_width = tf->width;
+    P.tf_lo = tf->lo;
+    P.tf_hi = tf->hi;
+    const size_t npix = (size_t)p->width * p->height;
+    cudaStream_t s = ctx->stream;
+    VRC_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+    if (p->entry_exit_mode == VRC_EE_BUFFERS) {
+        if (ee_on_device) {
+            P.entry = reinterpret_cast<const float4*>(entry);
+            P.exitp = reinterpret_cast<const float4*>(exitp);
+        } else {
+            VRC_CUDA(ctx, ensure(&ctx->d_ee, &ctx->ee_bytes, 2 * npix * sizeof(float4)));
+            float4* d = reinterpret_cast<float4*>(ctx->d_ee);
+            VRC_CUDA(ctx, cudaMemcpyAsync(d, entry, npix * sizeof(float4), cudaMemcpyHostToDevice, s));
+            VRC_CUDA(ctx, cudaMemcpyAsync(d + npix, exitp, npix * sizeof(float4), cudaMemcpyHostToDevice, s));
+            P.entry = d;
+            P.exitp = d + npix;
+        }
+    }
+    const size_t px_bytes = out_format == VRC_OUT_RGBA32F ? 16 : (out_format == VRC_OUT_RGBA16 ? 8 : 4);
+    if (out_on_device) {
+        P.out = out;
+    } else {
+        VRC_CUDA(ctx, ensure(&ctx->d_out, &ctx->out_bytes, npix * px_bytes));
+        P.out = ctx->d_out;
+    }
+    P.out_format = out_format;
+    if (p->empty_space_skipping) {
+        const long long nb = vol->L.nbricks();
+        VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, (size_t)nb));
+        VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, tf->d_prefix, tf->width, vol->desc.rwm_scale,
+                                            vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
+        P.occupancy = ctx->d_occ;
+    }
+    VRC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 16 * sizeof(unsigned long long), s));
+    P.counters = ctx->d_counters;
+    P.status = reinterpret_cast<int*>(ctx->d_counters + 4);
+    P.tile_counter = reinterpret_cast<unsigned int*>(ctx->d_counters + 5);
+    VRC_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
+    VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
+    VRC_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
+    if (!out_on_device) VRC_CUDA(ctx, cudaMemcpyAsync(out, P.out, npix * px_bytes, cudaMemcpyDeviceToHost, s));
+    VRC_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
+    if (stats || !out_on_device) VRC_CUDA(ctx, cudaStreamSynchronize(s));
+    if (stats) {
+        unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+        VRC_CUDA(ctx, cudaMemcpy(h, ctx->d_counters, sizeof(h), cudaMemcpyDeviceToHost));
+        stats->samples = double(h[0]);
+        stats->samples_fetched = double(h[1]);
+        stats->samples_shaded = double(h[2]);
+        stats->device_status = int(h[4] & 0xffffffffu);
+        VRC_CUDA(ctx, cudaEventElapsedTime(&stats->kernel_ms, ctx->ev[1], ctx->ev[2]));
+        VRC_CUDA(ctx, cudaEventElapsedTime(&stats->total_ms, ctx->ev[0], ctx->ev[3]));
+        if (stats->device_status != 0) return fail(ctx, VRC_ERR_DEVICE, "vrc_render: kernel reported an error status");
+    }
+    return VRC_OK;
+}
+
+vrc_status vrc_entry_exit(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, float* entry,
+                          float* exitp, int out_on_device) {
+    if (!ctx) return VRC_ERR_INVALID_ARG;
+    if (!vol || !entry || !exitp) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_entry_exit: null argument");
+    vrc_status st = check_params(ctx, p);
+    if (st != VRC_OK) return st;
+    VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+    vrc_render_params q = *p;
+    q.entry_exit_mode = VRC_EE_ANALYTIC;
+    MarchParams P;
+    if ((st = fill_params(ctx, vol, &q, P)) != VRC_OK) return st;
+    const size_t npix = (size_t)p->width * p->height;
+    float4 *de = reinterpret_cast<float4*>(entry), *dx = reinterpret_cast<float4*>(exitp);
+    if (!out_on_device) {
+        VRC_CUDA(ctx, ensure(&ctx->d_ee, &ctx->ee_bytes, 2 * npix * sizeof(float4)));
+        de = reinterpret_cast<float4*>(ctx->d_ee);
+        dx = de + npix;
+    }
+    VRC_CUDA(ctx, vrc::launch_entry_exit(P, de, dx, ctx->stream));
+    if (!out_on_device) {
+        VRC_CUDA(ctx, cudaMemcpyAsync(entry, de, npix * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+        VRC_CUDA(ctx, cudaMemcpyAsync(exitp, dx, npix * sizeof(float4), cudaMemcpyDeviceToHost, ctx->stream));
+        VRC_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return VRC_OK;
+}
+
+}  // extern "C"

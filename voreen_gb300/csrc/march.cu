@@ -1,0 +1,470 @@
+// The ray-march kernel: a GB300 restatement of CPURaycaster::directRendering
+// (modules/base/processors/render/cpuraycaster.cpp:210-326) with the GLSL-only
+// compositing and shading rules of rc_singlevolume.frag:116-312.
+//
+// Design:
+//  * persistent grid (a few CTAs per SM); each warp pulls 8x4 ray tiles from
+//    a global counter, so a warp's 32 rays are adjacent on screen and walk
+//    the same bricks;
+//  * the transfer function sits in shared memory as float4 (r, g, b, alpha')
+//    where alpha' already carries the opacity correction 1-(1-a)^(step*200)
+//    (computed on the host with the same powf the CPU path calls);
+//  * voxels come from the bricked layout (32^3 core + apron), so a stencil
+//    never crosses a brick; empty bricks (per-brick min/max against the TF)
+//    are skipped without reading voxels while t still advances sample by
+//    sample, which keeps results identical to the unskipped march;
+//  * every operation on the sample path is an explicitly rounded FP32
+//    intrinsic in the reference's order (no FMA contraction), so positions,
+//    trilinear values, TF indices, compositing and the t > tend stop match
+//    the FP32 CPU path bit for bit. Voxel normalisation v/255 and v/65535 is
+//    computed as q0 = v*r, q = fma(fma(-q0, d, v), r, q0), which equals the
+//    correctly rounded quotient for every 8- and 16-bit value;
+//  * gradients (central differences, mod_gradients.frag:202-214) read the
+//    32-voxel union stencil from the same brick by index shifts; Phong
+//    (mod_shading.frag:134-151) runs in registers.
+#include <cstdint>
+
+#include "vrc_internal.h"
+
+namespace vrc {
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int LOOP_CAP = 255 * 255;  // cpuraycaster.cpp:239
+
+__device__ __forceinline__ float m_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float a_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float s_(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); }
+
+template <int DT> struct Vox;
+template <> struct Vox<VRC_U8> {
+    using T = uint8_t;
+    static __device__ __forceinline__ float norm(T v) {
+        const float x = (float)v, r = 1.f / 255.f;
+        const float q0 = __fmul_rn(x, r);
+        return __fmaf_rn(__fmaf_rn(-q0, 255.f, x), r, q0);
+    }
+};
+template <> struct Vox<VRC_U16> {
+    using T = uint16_t;
+    static __device__ __forceinline__ float norm(T v) {
+        const float x = (float)v, r = 1.f / 65535.f;
+        const float q0 = __fmul_rn(x, r);
+        return __fmaf_rn(__fmaf_rn(-q0, 65535.f, x), r, q0);
+    }
+};
+template <> struct Vox<VRC_F32> {
+    using T = float;
+    static __device__ __forceinline__ float norm(T v) { return v; }
+};
+
+struct F3 {
+    float x, y, z;
+};
+
+// VolumeRAM::getVoxelNormalizedLinear summation order (volumeram.cpp:89-96).
+__device__ __forceinline__ float tri8(float v000, float v100, float v110, float v010, float v001, float v101,
+                                      float v111, float v011, float fx, float fy, float fz) {
+    const float ox = s_(1.f, fx), oy = s_(1.f, fy), oz = s_(1.f, fz);
+    float s = m_(m_(m_(v000, ox), oy), oz);
+    s = a_(s, m_(m_(m_(v100, fx), oy), oz));
+    s = a_(s, m_(m_(m_(v110, fx), fy), oz));
+    s = a_(s, m_(m_(m_(v010, ox), fy), oz));
+    s = a_(s, m_(m_(m_(v001, ox), oy), fz));
+    s = a_(s, m_(m_(m_(v101, fx), oy), fz));
+    s = a_(s, m_(m_(m_(v111, fx), fy), fz));
+    s = a_(s, m_(m_(m_(v011, ox), fy), fz));
+    return s;
+}
+
+template <int DT>
+__device__ __forceinline__ float tri_at(const typename Vox<DT>::T* __restrict__ b, int o, int S, int S2, float fx,
+                                        float fy, float fz) {
+    using V = Vox<DT>;
+    return tri8(V::norm(__ldg(b + o)), V::norm(__ldg(b + o + 1)), V::norm(__ldg(b + o + S + 1)),
+                V::norm(__ldg(b + o + S)), V::norm(__ldg(b + o + S2)), V::norm(__ldg(b + o + S2 + 1)),
+                V::norm(__ldg(b + o + S2 + S + 1)), V::norm(__ldg(b + o + S2 + S)), fx, fy, fz);
+}
+
+__device__ __forceinline__ float clampf_(float x, float lo, float hi) {
+    x = x > lo ? x : lo;
+    return x < hi ? x : hi;
+}
+
+__device__ __forceinline__ float rw_to_tf(float rw, float lo, float hi) {
+    if (rw < lo) return 0.f;
+    if (rw > hi) return 1.f;
+    if (lo == hi) return 0.f;
+    return d_(s_(rw, lo), s_(hi, lo));
+}
+
+__device__ __forceinline__ int tf_index(float x, int w) {
+    const float f = m_(x, (float)(w - 1));
+    const int i = (int)floorf(a_(f, 0.5f));
+    return i < 0 ? 0 : (i > w - 1 ? w - 1 : i);
+}
+
+__device__ __forceinline__ float len3(float x, float y, float z) {
+    float s = m_(x, x);
+    s = a_(s, m_(y, y));
+    s = a_(s, m_(z, z));
+    return __fsqrt_rn(s);
+}
+
+__device__ __forceinline__ F3 normalize3(F3 v) {
+    const float l = len3(v.x, v.y, v.z);
+    if (l == 0.f) return F3{0.f, 0.f, 0.f};
+    const float r = d_(1.f, l);
+    return F3{m_(v.x, r), m_(v.y, r), m_(v.z, r)};
+}
+
+__device__ __forceinline__ float dot3(F3 a, F3 b) {
+    float s = m_(a.x, b.x);
+    s = a_(s, m_(a.y, b.y));
+    s = a_(s, m_(a.z, b.z));
+    return s;
+}
+
+// Analytic entry/exit for pixel (px, py): the pixel-centre ray through the
+// unit texture cube, clipped to the near/far planes. Returns false for
+// background.
+__device__ bool analytic_entry_exit(const MarchParams& P, int px, int py, float4& e, float4& l) {
+    const float nx = s_(d_(m_(2.f, a_((float)px, 0.5f)), (float)P.W), 1.f);
+    const float ny = s_(d_(m_(2.f, a_((float)py, 0.5f)), (float)P.H), 1.f);
+    float pn[4], pf[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const float* M = P.inv_mvp + 4 * r;
+        const float base = a_(m_(M[0], nx), m_(M[1], ny));
+        pn[r] = a_(s_(base, M[2]), M[3]);
+        pf[r] = a_(a_(base, M[2]), M[3]);
+    }
+    float o[3], d[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        o[i] = d_(pn[i], pn[3]);
+        d[i] = s_(d_(pf[i], pf[3]), o[i]);
+    }
+    float s0 = 0.f, s1 = 1.f;
+    bool hit = true;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        if (d[i] == 0.f) {
+            if (o[i] < 0.f || o[i] > 1.f) hit = false;
+        } else {
+            float a = d_(s_(0.f, o[i]), d[i]), b = d_(s_(1.f, o[i]), d[i]);
+            if (a > b) {
+                const float t = a;
+                a = b;
+                b = t;
+            }
+            s0 = fmaxf(s0, a);
+            s1 = fminf(s1, b);
+        }
+    }
+    if (!hit || !(s0 < s1)) {
+        e = make_float4(0.f, 0.f, 0.f, 0.f);
+        l = e;
+        return false;
+    }
+    float en[3], ex[3];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        float a = clampf_(a_(o[i], m_(s0, d[i])), 0.f, 1.f);
+        float b = clampf_(a_(o[i], m_(s1, d[i])), 0.f, 1.f);
+        if (P.quantize) {
+            a = d_(floorf(a_(m_(a, 65535.f), 0.5f)), 65535.f);
+            b = d_(floorf(a_(m_(b, 65535.f), 0.5f)), 65535.f);
+        }
+        en[i] = a;
+        ex[i] = b;
+    }
+    e = make_float4(en[0], en[1], en[2], 1.f);
+    l = make_float4(ex[0], ex[1], ex[2], 1.f);
+    return true;
+}
+
+template <int EE> __device__ __forceinline__ F3 entry_point_at(const MarchParams& P, int x, int y) {
+    x = min(max(x, 0), P.W - 1);
+    y = min(max(y, 0), P.H - 1);
+    float4 e, l;
+    if (EE == VRC_EE_BUFFERS) {
+        e = P.entry[(size_t)y * P.W + x];
+    } else {
+        analytic_entry_exit(P, x, y, e, l);
+    }
+    return F3{e.x, e.y, e.z};
+}
+
+// fixClipBorderGradient (mod_gradients.frag:39-46)
+template <int EE> __device__ F3 clip_border_gradient(const MarchParams& P, F3 s, F3 dir, int px, int py) {
+    const F3 a = entry_point_at<EE>(P, px + 2, py), b = entry_point_at<EE>(P, px, py + 2);
+    const F3 v0 = normalize3(F3{s_(a.x, s.x), s_(a.y, s.y), s_(a.z, s.z)});
+    const F3 v1 = normalize3(F3{s_(b.x, s.x), s_(b.y, s.y), s_(b.z, s.z)});
+    F3 g{s_(m_(v0.y, v1.z), m_(v0.z, v1.y)), s_(m_(v0.z, v1.x), m_(v0.x, v1.z)), s_(m_(v0.x, v1.y), m_(v0.y, v1.x))};
+    if (!(dot3(g, dir) < 0.f)) g = F3{-g.x, -g.y, -g.z};
+    return g;
+}
+
+// phongShading (mod_shading.frag:134-151), ka = kd = TF colour, ks = 1.
+__device__ __forceinline__ F3 phong(const MarchParams& P, F3 n, F3 pos, F3 col) {
+    const F3 N = normalize3(n);
+    F3 L{s_(P.light_phys[0], pos.x), s_(P.light_phys[1], pos.y), s_(P.light_phys[2], pos.z)};
+    const F3 V = normalize3(F3{s_(P.cam_phys[0], pos.x), s_(P.cam_phys[1], pos.y), s_(P.cam_phys[2], pos.z)});
+    const float d = len3(L.x, L.y, L.z);
+    L = F3{d_(L.x, d), d_(L.y, d), d_(L.z, d)};
+    F3 out{m_(col.x, P.amb[0]), m_(col.y, P.amb[1]), m_(col.z, P.amb[2])};
+    float ndl = dot3(N, L);
+    ndl = ndl > 0.f ? ndl : 0.f;
+    out.x = a_(out.x, m_(m_(col.x, P.dif[0]), ndl));
+    out.y = a_(out.y, m_(m_(col.y, P.dif[1]), ndl));
+    out.z = a_(out.z, m_(m_(col.z, P.dif[2]), ndl));
+    const F3 Hh = normalize3(F3{a_(V.x, L.x), a_(V.y, L.y), a_(V.z, L.z)});
+    float ndh = dot3(N, Hh);
+    ndh = ndh > 0.f ? ndh : 0.f;
+    const float spec = powf(ndh, P.shininess);
+    out.x = a_(out.x, m_(P.spec[0], spec));
+    out.y = a_(out.y, m_(P.spec[1], spec));
+    out.z = a_(out.z, m_(P.spec[2], spec));
+    if (P.atten_on) {
+        float att = d_(1.f, a_(a_(P.att[0], m_(P.att[1], d)), m_(m_(P.att[2], d), d)));
+        att = att < 1.f ? att : 1.f;
+        out = F3{m_(out.x, att), m_(out.y, att), m_(out.z, att)};
+    }
+    return out;
+}
+
+__device__ __forceinline__ void write_out(const MarchParams& P, size_t pix, float4 r) {
+    if (P.out_format == VRC_OUT_RGBA32F) {
+        reinterpret_cast<float4*>(P.out)[pix] = r;
+    } else if (P.out_format == VRC_OUT_RGBA8) {
+        auto q = [](float v) -> unsigned {
+            v = fminf(fmaxf(v, 0.f), 1.f);
+            return (unsigned)floorf(v * 255.f + 0.5f);
+        };
+        reinterpret_cast<uchar4*>(P.out)[pix] = make_uchar4(q(r.x), q(r.y), q(r.z), q(r.w));
+    } else {
+        auto q = [](float v) -> unsigned {
+            v = fminf(fmaxf(v, 0.f), 1.f);
+            return (unsigned)floorf(v * 65535.f + 0.5f);
+        };
+        reinterpret_cast<ushort4*>(P.out)[pix] = make_ushort4(q(r.x), q(r.y), q(r.z), q(r.w));
+    }
+}
+
+struct Counters {
+    unsigned long long samples = 0, fetched = 0, shaded = 0;
+};
+
+// One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
+template <int DT, int COMP, int SHADE, int EE>
+__device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
+                            int py, Counters& cnt) {
+    using T = typename Vox<DT>::T;
+    const T* __restrict__ bricks = reinterpret_cast<const T*>(P.bricks);
+    const BrickLayout& L = P.L;
+    const int S = L.S, S2 = L.S * L.S;
+    const float step = P.step;
+    float dx = s_(l.x, f.x), dy = s_(l.y, f.y), dz = s_(l.z, f.z);
+    const bool dir0 = dx == 0.f && dy == 0.f && dz == 0.f;
+    const bool last0 = l.x == 0.f && l.y == 0.f && l.z == 0.f;
+    const bool first0 = f.x == 0.f && f.y == 0.f && f.z == 0.f;
+    float tend;
+    if (dir0 && !last0 && !first0) {
+        tend = d_(step, 2.f);
+    } else {
+        tend = len3(dx, dy, dz);
+        const float rl = d_(1.f, tend);
+        dx = m_(dx, rl);
+        dy = m_(dy, rl);
+        dz = m_(dz, rl);
+    }
+    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+    float max_int = 0.f;
+    float t = 0.f;
+    bool finished = false;
+    int loop = 0;
+    for (; !finished && loop < LOOP_CAP; ++loop) {
+        const float sx = a_(f.x, m_(t, dx)), sy = a_(f.y, m_(t, dy)), sz = a_(f.z, m_(t, dz));
+        const float vx = clampf_(s_(m_(P.dimf[0], sx), 0.5f), 0.f, P.dim_m1[0]);
+        const float vy = clampf_(s_(m_(P.dimf[1], sy), 0.5f), 0.f, P.dim_m1[1]);
+        const float vz = clampf_(s_(m_(P.dimf[2], sz), 0.5f), 0.f, P.dim_m1[2]);
+        const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
+        const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
+        const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
+        const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
+        const bool occupied = P.occupancy == nullptr || P.occupancy[brick] != 0;
+        if (occupied) {
+            ++cnt.fetched;
+            const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
+            const T* __restrict__ b = bricks + brick * L.brick_stride;
+            const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
+                      lz = iz - (bz << L.shift) + APRON_LO;
+            const int o = (lz * S + ly) * S + lx;
+            const float intensity = tri_at<DT>(b, o, S, S2, fx, fy, fz);
+            const float rw = a_(m_(intensity, P.rwm_scale), P.rwm_offset);
+            float4 c = s_tf[tf_index(rw_to_tf(rw, P.tf_lo, P.tf_hi), P.tf_width)];
+            if (c.w > 0.f) {
+                if (SHADE == VRC_SHADE_PHONG) {
+                    ++cnt.shaded;
+                    F3 g;
+                    if (t == 0.f) {
+                        g = clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py);
+                    } else {
+                        const float v0 = tri_at<DT>(b, o + 1, S, S2, fx, fy, fz);
+                        const float v1 = tri_at<DT>(b, o + S, S, S2, fx, fy, fz);
+                        const float v2 = tri_at<DT>(b, o + S2, S, S2, fx, fy, fz);
+                        const float v3 = tri_at<DT>(b, o - 1, S, S2, fx, fy, fz);
+                        const float v4 = tri_at<DT>(b, o - S, S, S2, fx, fy, fz);
+                        const float v5 = tri_at<DT>(b, o - S2, S, S2, fx, fy, fz);
+                        g = F3{m_(m_(s_(v3, v0), P.spacing_rcp_half[0]), P.rwm_scale),
+                               m_(m_(s_(v4, v1), P.spacing_rcp_half[1]), P.rwm_scale),
+                               m_(m_(s_(v5, v2), P.spacing_rcp_half[2]), P.rwm_scale)};
+                    }
+                    const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
+                                 a_(m_(s_(m_(sy, P.dimf[1]), 0.5f), P.spacing[1]), P.vol_offset[1]),
+                                 a_(m_(s_(m_(sz, P.dimf[2]), 0.5f), P.spacing[2]), P.vol_offset[2])};
+                    const F3 sh = phong(P, g, pos, F3{c.x, c.y, c.z});
+                    c.x = sh.x;
+                    c.y = sh.y;
+                    c.z = sh.z;
+                }
+                if (COMP == VRC_DVR) {
+                    const float w = m_(s_(1.f, res.w), c.w);
+                    res.x = a_(res.x, m_(w, c.x));
+                    res.y = a_(res.y, m_(w, c.y));
+                    res.z = a_(res.z, m_(w, c.z));
+                    res.w = a_(res.w, m_(s_(1.f, res.w), c.w));
+                } else if (COMP == VRC_MIP) {
+                    if (rw > max_int) {
+                        res = c;
+                        max_int = rw;
+                    }
+                } else {
+                    if (c.w >= s_(P.iso, 0.02f) && c.w <= a_(P.iso, 0.02f)) res = make_float4(c.x, c.y, c.z, 1.f);
+                }
+            }
+        }
+        if (COMP != VRC_MIP && res.w >= P.ert) {
+            res.w = 1.f;
+            finished = true;
+        }
+        t = a_(t, step);
+        finished = finished || (t > tend);
+    }
+    cnt.samples += (unsigned long long)loop;
+    return res;
+}
+
+template <int DT, int COMP, int SHADE, int EE>
+__global__ void __launch_bounds__(256) march_kernel(MarchParams P) {
+    extern __shared__ float4 s_tf[];
+    for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_table[i];
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int ntiles = P.tiles_x * P.tiles_y;
+    Counters cnt;
+    for (;;) {
+        int tile = 0;
+        if (lane == 0) tile = (int)atomicAdd(P.tile_counter, 1u);
+        tile = __shfl_sync(FULL, tile, 0);
+        if (tile >= ntiles) break;
+        const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
+        const int px = tx * 8 + (lane & 7), py = ty * 4 + (lane >> 3);
+        if (px < P.W && py < P.H) {
+            const size_t pix = (size_t)py * P.W + px;
+            float4 f, l;
+            if (EE == VRC_EE_BUFFERS) {
+                f = P.entry[pix];
+                l = P.exitp[pix];
+            } else {
+                analytic_entry_exit(P, px, py, f, l);
+            }
+            const bool bg = f.x == 0.f && f.y == 0.f && f.z == 0.f && f.w == 0.f && l.x == 0.f && l.y == 0.f &&
+                            l.z == 0.f && l.w == 0.f;
+            float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (!bg) r = march_ray<DT, COMP, SHADE, EE>(P, s_tf, f, l, px, py, cnt);
+            write_out(P, pix, r);
+        }
+    }
+    if (P.counters) {
+        unsigned long long a = cnt.samples, b = cnt.fetched, c = cnt.shaded;
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(FULL, a, o);
+            b += __shfl_xor_sync(FULL, b, o);
+            c += __shfl_xor_sync(FULL, c, o);
+        }
+        if (lane == 0) {
+            atomicAdd(P.counters + 0, a);
+            atomicAdd(P.counters + 1, b);
+            atomicAdd(P.counters + 2, c);
+        }
+    }
+}
+
+__global__ void entry_exit_kernel(MarchParams P, float4* entry, float4* exitp) {
+    const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
+    if (px >= P.W) return;
+    float4 e, l;
+    analytic_entry_exit(P, px, py, e, l);
+    entry[(size_t)py * P.W + px] = e;
+    exitp[(size_t)py * P.W + px] = l;
+}
+
+template <int DT, int COMP, int SHADE, int EE>
+cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
+    auto k = march_kernel<DT, COMP, SHADE, EE>;
+    const size_t smem = (size_t)p.tf_width * sizeof(float4);
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) per_sm = 1;
+    const long long tiles = (long long)p.tiles_x * p.tiles_y;
+    long long grid = (long long)num_sms * per_sm;
+    const long long need = (tiles + 7) / 8;  // 8 warps per CTA
+    if (grid > need) grid = need < 1 ? 1 : need;
+    k<<<(unsigned)grid, 256, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+template <int DT, int COMP, int SHADE>
+cudaError_t launch_ee(const MarchParams& p, int num_sms, cudaStream_t s) {
+    return p.ee_mode == VRC_EE_ANALYTIC ? launch_t<DT, COMP, SHADE, VRC_EE_ANALYTIC>(p, num_sms, s)
+                                        : launch_t<DT, COMP, SHADE, VRC_EE_BUFFERS>(p, num_sms, s);
+}
+
+template <int DT, int COMP>
+cudaError_t launch_sh(const MarchParams& p, int shading, int num_sms, cudaStream_t s) {
+    return shading == VRC_SHADE_PHONG ? launch_ee<DT, COMP, VRC_SHADE_PHONG>(p, num_sms, s)
+                                      : launch_ee<DT, COMP, VRC_SHADE_NONE>(p, num_sms, s);
+}
+
+template <int DT> cudaError_t launch_comp(const MarchParams& p, int comp, int shading, int num_sms, cudaStream_t s) {
+    switch (comp) {
+        case VRC_MIP: return launch_sh<DT, VRC_MIP>(p, shading, num_sms, s);
+        case VRC_ISO: return launch_sh<DT, VRC_ISO>(p, shading, num_sms, s);
+        default: return launch_sh<DT, VRC_DVR>(p, shading, num_sms, s);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
+                         cudaStream_t s) {
+    switch (dtype) {
+        case VRC_U8: return launch_comp<VRC_U8>(p, compositing, shading, num_sms, s);
+        case VRC_U16: return launch_comp<VRC_U16>(p, compositing, shading, num_sms, s);
+        default: return launch_comp<VRC_F32>(p, compositing, shading, num_sms, s);
+    }
+}
+
+cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp, cudaStream_t s) {
+    dim3 grid((p.W + 127) / 128, p.H);
+    entry_exit_kernel<<<grid, 128, 0, s>>>(p, entry, exitp);
+    return cudaGetLastError();
+}
+
+}  // namespace vrc

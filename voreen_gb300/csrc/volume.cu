@@ -1,0 +1,162 @@
+// Volume ingest: linear VolumeRAM layout -> bricked device layout, per-brick
+// min/max, and the per-(volume, TF) brick occupancy used for empty-space
+// skipping.
+//
+// Reference behaviour this replaces / follows:
+//   VolumeGL upload (linear 3D texture)       src/core/datastructures/volume/volumegl.cpp:126-168
+//   per-region min/max with 1-voxel overlap   modules/base/processors/proxygeometry/optimizedproxygeometry.cpp:894-987
+//   region emptiness from TF opacity          optimizedproxygeometry.cpp:878-880
+// The brick test here is exact for the march: a brick is empty when every TF
+// entry its trilinear samples can select has alpha 0.
+#include <cstdint>
+
+#include "vrc_internal.h"
+
+namespace vrc {
+namespace {
+
+template <typename T>
+__global__ void brick_build_kernel(const T* __restrict__ lin, BrickLayout L, T* __restrict__ bricks) {
+    const long long S3 = (long long)L.S * L.S * L.S;
+    const long long total = L.nbricks() * S3;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const long long b = i / S3;
+        const int r = (int)(i - b * S3);
+        const int lx = r % L.S, ly = (r / L.S) % L.S, lz = r / (L.S * L.S);
+        const int bx = (int)(b % L.nb[0]);
+        const int by = (int)((b / L.nb[0]) % L.nb[1]);
+        const int bz = (int)(b / ((long long)L.nb[0] * L.nb[1]));
+        int gx = bx * L.B + lx - APRON_LO, gy = by * L.B + ly - APRON_LO, gz = bz * L.B + lz - APRON_LO;
+        gx = min(max(gx, 0), L.dims[0] - 1);
+        gy = min(max(gy, 0), L.dims[1] - 1);
+        gz = min(max(gz, 0), L.dims[2] - 1);
+        bricks[b * L.brick_stride + r] = lin[((long long)gz * L.dims[1] + gy) * L.dims[0] + gx];
+    }
+}
+
+template <typename T> __device__ __forceinline__ float raw_to_float(T v) { return (float)v; }
+
+// One CTA per brick: min/max of the stored values over local [APRON_LO,
+// APRON_LO + B] on each axis (core + one voxel on the high side), i.e. the
+// voxels any trilinear stencil whose floor lies in the brick can touch.
+template <typename T>
+__global__ void brick_minmax_kernel(const T* __restrict__ bricks, BrickLayout L, float norm, float* bmin,
+                                    float* bmax) {
+    const long long b = blockIdx.x;
+    const T* base = bricks + b * L.brick_stride;
+    const int E = L.B + 1;
+    float mn = INFINITY, mx = -INFINITY;
+    for (int i = threadIdx.x; i < E * E * E; i += blockDim.x) {
+        const int x = i % E + APRON_LO, y = (i / E) % E + APRON_LO, z = i / (E * E) + APRON_LO;
+        const float v = raw_to_float(base[(z * L.S + y) * L.S + x]);
+        mn = fminf(mn, v);
+        mx = fmaxf(mx, v);
+    }
+    __shared__ float smn[32], smx[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (lane == 0) { smn[w] = mn; smx[w] = mx; }
+    __syncthreads();
+    if (w == 0) {
+        const int nw = blockDim.x >> 5;
+        mn = lane < nw ? smn[lane] : INFINITY;
+        mx = lane < nw ? smx[lane] : -INFINITY;
+        for (int o = 16; o > 0; o >>= 1) {
+            mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+            mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        }
+        if (lane == 0) {
+            // getTypeAsFloat: value / rangeMax, correctly rounded (monotone)
+            bmin[b] = norm > 0.f ? __fdiv_rn(mn, norm) : mn;
+            bmax[b] = norm > 0.f ? __fdiv_rn(mx, norm) : mx;
+        }
+    }
+}
+
+__device__ __forceinline__ float rw_to_tf(float rw, float lo, float hi) {
+    if (rw < lo) return 0.f;
+    if (rw > hi) return 1.f;
+    if (lo == hi) return 0.f;
+    return __fdiv_rn(__fsub_rn(rw, lo), __fsub_rn(hi, lo));
+}
+
+__device__ __forceinline__ int tf_index(float x, int w) {
+    const float f = __fmul_rn(x, (float)(w - 1));
+    int i = (int)floorf(__fadd_rn(f, 0.5f));
+    return i < 0 ? 0 : (i > w - 1 ? w - 1 : i);
+}
+
+// occ[b] = 1 if any TF entry with index in [idx(min) - 1, idx(max) + 1] has
+// alpha > 0. alpha_prefix[i] = number of entries < i with alpha > 0.
+__global__ void occupancy_kernel(const float* bmin, const float* bmax, long long n, const int* prefix, int w,
+                                 float rs, float ro, float lo, float hi, uint8_t* occ) {
+    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n;
+         b += (long long)gridDim.x * blockDim.x) {
+        const float r0 = __fadd_rn(__fmul_rn(bmin[b], rs), ro);
+        const float r1 = __fadd_rn(__fmul_rn(bmax[b], rs), ro);
+        int i0 = tf_index(rw_to_tf(fminf(r0, r1), lo, hi), w);
+        int i1 = tf_index(rw_to_tf(fmaxf(r0, r1), lo, hi), w);
+        i0 = max(i0 - 1, 0);
+        i1 = min(i1 + 1, w - 1);
+        occ[b] = (prefix[i1 + 1] - prefix[i0]) > 0 ? 1 : 0;
+    }
+}
+
+int grid_for(long long n, int block) {
+    long long g = (n + block - 1) / block;
+    if (g > 152LL * 64) g = 152LL * 64;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s) {
+    const long long total = L.nbricks() * (long long)L.S * L.S * L.S;
+    const int g = grid_for(total, 256);
+    switch (dtype) {
+        case VRC_U8:
+            brick_build_kernel<uint8_t><<<g, 256, 0, s>>>((const uint8_t*)linear, L, (uint8_t*)bricks);
+            break;
+        case VRC_U16:
+            brick_build_kernel<uint16_t><<<g, 256, 0, s>>>((const uint16_t*)linear, L, (uint16_t*)bricks);
+            break;
+        default:
+            brick_build_kernel<float><<<g, 256, 0, s>>>((const float*)linear, L, (float*)bricks);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
+                                cudaStream_t s) {
+    const long long n = L.nbricks();
+    if (n > 0x7fffffffLL) return cudaErrorInvalidValue;
+    switch (dtype) {
+        case VRC_U8:
+            brick_minmax_kernel<uint8_t><<<(unsigned)n, 256, 0, s>>>((const uint8_t*)bricks, L, 255.f, bmin, bmax);
+            break;
+        case VRC_U16:
+            brick_minmax_kernel<uint16_t><<<(unsigned)n, 256, 0, s>>>((const uint16_t*)bricks, L, 65535.f, bmin,
+                                                                      bmax);
+            break;
+        default:
+            brick_minmax_kernel<float><<<(unsigned)n, 256, 0, s>>>((const float*)bricks, L, 0.f, bmin, bmax);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nbricks, const int* alpha_prefix,
+                             int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
+                             uint8_t* occ, cudaStream_t s) {
+    occupancy_kernel<<<grid_for(nbricks, 256), 256, 0, s>>>(bmin, bmax, nbricks, alpha_prefix, tf_width, rwm_scale,
+                                                            rwm_offset, tf_lo, tf_hi, occ);
+    return cudaGetLastError();
+}
+
+}  // namespace vrc

@@ -1,0 +1,121 @@
+// Internal declarations shared by the host API (api.cpp) and the CUDA
+// translation units. Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <utility>
+
+#include "../../include/vrc.h"
+
+namespace vrc {
+
+// Bricked volume layout: bricks of B^3 core voxels stored with an apron of
+// APRON_LO voxel below and APRON_HI voxels above on every axis, filled with
+// the clamp-to-edge value. A sample whose floor voxel lies in a brick then
+// reads its trilinear stencil (+1) and the central-difference stencil
+// (-1 .. +2) from that brick alone.
+constexpr int APRON_LO = 1;
+constexpr int APRON_HI = 2;
+
+inline int dtype_bytes(int dt) { return dt == VRC_U8 ? 1 : (dt == VRC_U16 ? 2 : 4); }
+
+struct BrickLayout {
+    int dims[3];
+    int B;        // core edge
+    int shift;    // log2(B)
+    int S;        // stored edge = B + APRON_LO + APRON_HI
+    int nb[3];    // brick grid
+    long long brick_stride;  // voxels per stored brick (S^3 rounded up to 64)
+#ifdef __CUDACC__
+    __host__ __device__
+#endif
+    long long nbricks() const { return (long long)nb[0] * nb[1] * nb[2]; }
+};
+
+// Parameters of one march launch (passed by value).
+struct MarchParams {
+    const void* bricks;
+    const uint8_t* occupancy;   // one byte per brick; nullptr = no skipping
+    const float4* tf_table;     // (r, g, b, alpha') per TF entry
+    int tf_width;
+    BrickLayout L;
+    float dimf[3], dim_m1[3], offs[3];
+    float spacing[3], spacing_rcp_half[3], vol_offset[3];
+    float rwm_scale, rwm_offset, tf_lo, tf_hi;
+    float step, ert;
+    int use_ert;
+    float iso;
+    float light_phys[3], cam_phys[3];
+    float amb[3], dif[3], spec[3];
+    float shininess;
+    int atten_on;
+    float att[3];
+    int W, H;
+    int ee_mode;                 // VRC_EE_BUFFERS / VRC_EE_ANALYTIC
+    int quantize;
+    const float4* entry;
+    const float4* exitp;
+    float inv_mvp[16];
+    void* out;
+    int out_format;
+    unsigned long long* counters;  // [samples, fetched, shaded]
+    int* status;
+    unsigned int* tile_counter;
+    int tiles_x, tiles_y;
+};
+
+// Kernel launchers (march.cu / volume.cu). Return cudaError_t.
+cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
+                         cudaStream_t s);
+cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp, cudaStream_t s);
+cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s);
+cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
+                                cudaStream_t s);
+cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nbricks, const int* alpha_prefix,
+                             int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
+                             uint8_t* occ, cudaStream_t s);
+
+}  // namespace vrc
+
+// Opaque handle definitions.
+struct vrc_context {
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::string last_error;
+    // scratch (grown on demand, owned by the context)
+    void* d_ee = nullptr;
+    size_t ee_bytes = 0;
+    void* d_out = nullptr;
+    size_t out_bytes = 0;
+    uint8_t* d_occ = nullptr;
+    size_t occ_bytes = 0;
+    int* d_prefix = nullptr;
+    size_t prefix_bytes = 0;
+    unsigned long long* d_counters = nullptr;  // 4 counters + status + tile counter
+};
+
+struct vrc_volume {
+    vrc_context* ctx = nullptr;
+    vrc_volume_desc desc{};
+    vrc::BrickLayout L{};
+    void* d_bricks = nullptr;
+    float* d_bmin = nullptr;
+    float* d_bmax = nullptr;
+    size_t bytes = 0;
+    float vmin = 0.f, vmax = 0.f;
+};
+
+struct vrc_tf {
+    vrc_context* ctx = nullptr;
+    int width = 0;
+    float lo = 0.f, hi = 1.f;
+    uint8_t* h_rgba = nullptr;
+    // device float4 tables keyed by (opacity-corrected?, correction exponent bits)
+    std::map<std::pair<int, uint32_t>, float4*> tables;
+    int* d_prefix = nullptr;  // prefix count of entries with alpha > 0 (width + 1 ints)
+};
