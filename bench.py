@@ -160,11 +160,13 @@ def run_cpu(w, entry, exit_pts, target_s: float):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=1000)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--profile", action="store_true",
+                    help="device frames only (no e2e, no CPU baseline): the command line for ncu captures")
     args = ap.parse_args()
     warmup = max(3, args.warmup)
     ws, rank, local = _dist()
@@ -241,6 +243,12 @@ def main():
         _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
         kernel_ms.append(st.kernel_ms)
 
+    if args.profile:
+        for _ in range(args.steps):
+            v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
+        ctx.synchronize()
+        print(json.dumps({"profile_run": True, "samples_per_frame": samples, "kernel_ms": kernel_ms}))
+        return
     for _ in range(warmup):
         v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
     torch.cuda.synchronize()

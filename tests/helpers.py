@@ -50,27 +50,43 @@ class Case:
             setattr(p, k, val)
         return v.render(self.ctx, self.vol, self.tf, p, self.entry, self.exit, out_format)
 
+    @property
+    def step(self):
+        return 1.0 / (max(self.vol.dims) * self.params.sampling_rate)
+
     def oracle(self, precision=32, rows=None, entry=None, exit_pts=None):
         e = self.entry if entry is None else entry
         x = self.exit if exit_pts is None else exit_pts
         return oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params), e, x, precision, rows)
 
 
-def decision_divergent(s32, s64, fh32, fh64, comp):
+def sample_index(first_hit, step):
+    """Loop index of the selected sample from its ray parameter (-1: none)."""
+    fh = np.asarray(first_hit, np.float64)
+    return np.where(fh >= 0, np.rint(fh / step), -1).astype(np.int64)
+
+
+def decision_divergent(o32, s32, fh32, o64, s64, fh64, comp, step, shaded=False):
     """Rays where FP32 and FP64 take a different discrete decision: a
-    different number of samples (ERT step or the t > tend stop), or for MIP
-    and ISO a different selected sample."""
+    different number of samples (ERT step or the t > tend stop), a different
+    selected sample (first hit, MIP maximum, ISO hit), or for MIP / ISO a
+    different TF entry for the selected sample (the output is that entry)."""
     div = s32 != s64
+    div |= sample_index(fh32, step) != sample_index(fh64, step)
     if comp in (v.MIP, v.ISO):
-        div |= np.abs(fh32.astype(np.float64) - fh64) > 0
+        d = np.abs(o32.astype(np.float64) - o64)
+        div |= d[..., 3] > 1e-6
+        if not shaded:
+            div |= d.max(axis=-1) > 1e-5
     return div
 
 
-def assert_fp64_parity(gpu_img, s32, fh32, o64, s64, fh64, comp, max_div_frac=2e-3, tol=TOL):
+def assert_fp64_parity(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded=False, max_div_frac=2e-3,
+                       tol=TOL):
     """max |d| <= tol on every ray where FP32 and FP64 make the same discrete
     decisions; the rest (reported) must be a tiny fraction of the hit rays."""
     d = np.abs(gpu_img.astype(np.float64) - o64).max(axis=-1)
-    div = decision_divergent(s32, s64, fh32, fh64, comp)
+    div = decision_divergent(o32, s32, fh32, o64, s64, fh64, comp, step, shaded)
     hits = max(1, int((s32 > 0).sum()))
     assert div.sum() <= max(2, max_div_frac * hits), f"{div.sum()} decision-divergent rays of {hits}"
     ok = ~div

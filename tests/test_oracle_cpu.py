@@ -25,13 +25,13 @@ def test_fp32_vs_fp64_config1():
     w = synth.config1(image=(256, 256))
     (o32, s32, f32), (o64, s64, f64), e = _run(w)
     assert s32.sum() > 100000
-    assert_fp64_parity(o32, s32, f32, o64, s64, f64, v.DVR)
+    assert_fp64_parity(o32, o32, s32, f32, o64, s64, f64, v.DVR, 1.0 / (max(w.dims) * w.sampling_rate))
 
 
 def test_fp32_vs_fp64_shaded_shells():
     w = synth.config2(size=(80, 80, 80), image=(160, 120))
     (o32, s32, f32), (o64, s64, f64), e = _run(w)
-    assert_fp64_parity(o32, s32, f32, o64, s64, f64, v.DVR)
+    assert_fp64_parity(o32, o32, s32, f32, o64, s64, f64, v.DVR, 1.0 / (max(w.dims) * w.sampling_rate))
     assert (o32[..., 3] > 0.05).mean() > 0.05
 
 

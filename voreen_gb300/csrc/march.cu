@@ -19,9 +19,12 @@
 //    the FP32 CPU path bit for bit. Voxel normalisation v/255 and v/65535 is
 //    computed as q0 = v*r, q = fma(fma(-q0, d, v), r, q0), which equals the
 //    correctly rounded quotient for every 8- and 16-bit value;
-//  * gradients (central differences, mod_gradients.frag:202-214) read the
-//    32-voxel union stencil from the same brick by index shifts; Phong
-//    (mod_shading.frag:134-151) runs in registers.
+//  * gradients (central differences, mod_gradients.frag:202-214) are six
+//    lookups at +-1/dim in texture space, clamped and interpolated exactly as
+//    the intensity sample; each lookup finds its own brick, so lookups that
+//    cross a brick face stay exact. Phong (mod_shading.frag:134-151) runs in
+//    registers; its pow is CUDA's powf, the only step that is not bit-equal
+//    with the CPU path.
 #include <cstdint>
 
 #include "vrc_internal.h"
@@ -85,6 +88,21 @@ __device__ __forceinline__ float tri_at(const typename Vox<DT>::T* __restrict__ 
     return tri8(V::norm(__ldg(b + o)), V::norm(__ldg(b + o + 1)), V::norm(__ldg(b + o + S + 1)),
                 V::norm(__ldg(b + o + S)), V::norm(__ldg(b + o + S2)), V::norm(__ldg(b + o + S2 + 1)),
                 V::norm(__ldg(b + o + S2 + S + 1)), V::norm(__ldg(b + o + S2 + S)), fx, fy, fz);
+}
+
+// Trilinear value at a clamped voxel position, from the brick that holds
+// its floor voxel (VolumeRAM::getVoxelNormalizedLinear on the bricked layout).
+template <int DT>
+__device__ __forceinline__ float sample_at(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
+                                           float vx, float vy, float vz) {
+    const BrickLayout& L = P.L;
+    const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
+    const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
+    const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
+    const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
+    const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
+                  (ix - (bx << L.shift) + APRON_LO);
+    return tri_at<DT>(bricks + brick * L.brick_stride, o, L.S, L.S * L.S, s_(vx, flx), s_(vy, fly), s_(vz, flz));
 }
 
 __device__ __forceinline__ float clampf_(float x, float lo, float hi) {
@@ -312,12 +330,20 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     if (t == 0.f) {
                         g = clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py);
                     } else {
-                        const float v0 = tri_at<DT>(b, o + 1, S, S2, fx, fy, fz);
-                        const float v1 = tri_at<DT>(b, o + S, S, S2, fx, fy, fz);
-                        const float v2 = tri_at<DT>(b, o + S2, S, S2, fx, fy, fz);
-                        const float v3 = tri_at<DT>(b, o - 1, S, S2, fx, fy, fz);
-                        const float v4 = tri_at<DT>(b, o - S, S, S2, fx, fy, fz);
-                        const float v5 = tri_at<DT>(b, o - S2, S, S2, fx, fy, fz);
+                        // calcGradientA: six lookups at +-1/dim in texture space, each
+                        // clamped and interpolated exactly like the intensity sample
+                        const float vxp = clampf_(s_(m_(P.dimf[0], a_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
+                        const float vyp = clampf_(s_(m_(P.dimf[1], a_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
+                        const float vzp = clampf_(s_(m_(P.dimf[2], a_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
+                        const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
+                        const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
+                        const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
+                        const float v0 = sample_at<DT>(P, bricks, vxp, vy, vz);
+                        const float v1 = sample_at<DT>(P, bricks, vx, vyp, vz);
+                        const float v2 = sample_at<DT>(P, bricks, vx, vy, vzp);
+                        const float v3 = sample_at<DT>(P, bricks, vxm, vy, vz);
+                        const float v4 = sample_at<DT>(P, bricks, vx, vym, vz);
+                        const float v5 = sample_at<DT>(P, bricks, vx, vy, vzm);
                         g = F3{m_(m_(s_(v3, v0), P.spacing_rcp_half[0]), P.rwm_scale),
                                m_(m_(s_(v4, v1), P.spacing_rcp_half[1]), P.rwm_scale),
                                m_(m_(s_(v5, v2), P.spacing_rcp_half[2]), P.rwm_scale)};
