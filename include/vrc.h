@@ -152,8 +152,9 @@ typedef struct {
     vrc_camera camera;          /* "camera": used for shading and analytic entry/exit */
     int entry_exit_mode;        /* vrc_entry_exit_mode */
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
-    int empty_space_skipping;   /* skip bricks whose TF opacity is zero (exact: results unchanged) */
-    int reserved[8];
+    int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
+    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (8), else 8, 16 or the brick size */
+    int reserved[7];
 } vrc_render_params;
 
 /* Fills `p` with the reference's property defaults for a W x H image. */

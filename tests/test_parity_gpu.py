@@ -101,16 +101,22 @@ def test_odd_shapes_and_brick_sizes(ctx, dims, brick):
     np.testing.assert_array_equal(_bits(img), _bits(o32))
 
 
-def test_empty_space_skipping_is_exact(ctx):
-    w = synth.config2(size=(128, 128, 128), image=(256, 192))
-    p = w.params(shading=v.SHADE_NONE)
+@pytest.mark.parametrize("cell,brick,shading", [(8, 32, v.SHADE_NONE), (16, 32, v.SHADE_PHONG), (32, 32, v.SHADE_NONE),
+                                                (8, 16, v.SHADE_PHONG), (64, 64, v.SHADE_NONE)])
+def test_empty_space_skipping_is_exact(ctx, cell, brick, shading):
+    """Skipping empty cells (8^3, 16^3 or whole bricks) leaves every pixel
+    and the sample count unchanged."""
+    w = synth.config2(size=(130, 128, 127), image=(256, 192))
+    p = w.params(shading=shading, skip_cell_size=cell)
     tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
-    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing, brick=16)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing, brick=brick)
     a, sa = c.gpu(empty_space_skipping=1)
     b, sb = c.gpu(empty_space_skipping=0)
     np.testing.assert_array_equal(_bits(a), _bits(b))
     assert sa.samples == sb.samples
-    assert sa.samples_fetched < 0.9 * sb.samples_fetched
+    assert sa.samples_fetched <= sb.samples_fetched
+    if cell <= 16:
+        assert sa.samples_fetched < 0.9 * sb.samples_fetched
 
 
 def test_brick_minmax_and_volume_minmax(ctx):

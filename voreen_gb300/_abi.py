@@ -43,7 +43,8 @@ class RenderParams(C.Structure):
                 ("light_diffuse", C.c_float * 3), ("light_specular", C.c_float * 3),
                 ("material_shininess", C.c_float), ("apply_attenuation", C.c_int),
                 ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
-                ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("reserved", C.c_int * 8)]
+                ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("skip_cell_size", C.c_int),
+                ("reserved", C.c_int * 7)]
 
 
 class RenderStats(C.Structure):

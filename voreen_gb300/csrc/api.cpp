@@ -298,6 +298,20 @@ vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, cons
     if ((e = vrc::launch_brick_build(lin, desc->dtype, L, v->d_bricks, ctx->stream)) != cudaSuccess ||
         (e = vrc::launch_brick_minmax(v->d_bricks, desc->dtype, L, v->d_bmin, v->d_bmax, ctx->stream)) != cudaSuccess)
         return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: kernel: ") + cudaGetErrorString(e));
+    // finer empty-space cells (8^3, 16^3) below the brick size
+    for (int li = 0; li < 2; ++li) {
+        const int C = li == 0 ? 8 : 16;
+        if (C >= brick_size) continue;
+        vrc_cell_level& lv = v->levels[li];
+        lv.C = C;
+        for (int i = 0; i < 3; ++i) lv.nc[i] = (desc->dims[i] + C - 1) / C;
+        if ((e = cudaMalloc((void**)&lv.d_min, lv.count() * sizeof(float))) != cudaSuccess ||
+            (e = cudaMalloc((void**)&lv.d_max, lv.count() * sizeof(float))) != cudaSuccess)
+            return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: cell table allocation failed");
+        v->bytes += 2 * lv.count() * sizeof(float);
+        if ((e = vrc::launch_cell_minmax(lin, desc->dtype, desc->dims, C, lv.d_min, lv.d_max, ctx->stream)) != cudaSuccess)
+            return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: cell kernel: ") + cudaGetErrorString(e));
+    }
     std::vector<float> mn(L.nbricks()), mx(L.nbricks());
     if ((e = cudaMemcpyAsync(mn.data(), v->d_bmin, mn.size() * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream)) !=
             cudaSuccess ||
@@ -319,6 +333,10 @@ vrc_status vrc_volume_destroy(vrc_volume* v) {
     cudaFree(v->d_bricks);
     cudaFree(v->d_bmin);
     cudaFree(v->d_bmax);
+    for (auto& lv : v->levels) {
+        cudaFree(lv.d_min);
+        cudaFree(lv.d_max);
+    }
     delete v;
     return VRC_OK;
 }
@@ -570,6 +588,9 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
         return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
     if (p->entry_exit_mode != VRC_EE_BUFFERS && p->entry_exit_mode != VRC_EE_ANALYTIC)
         return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown entry/exit mode");
+    if (p->skip_cell_size != 0 && p->skip_cell_size != 8 && p->skip_cell_size != 16 && p->skip_cell_size != 32 &&
+        p->skip_cell_size != 64)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 8, 16, 32 or 64");
     return VRC_OK;
 }
 
@@ -627,11 +648,28 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
     }
     P.out_format = out_format;
     if (p->empty_space_skipping) {
-        const long long nb = vol->L.nbricks();
-        VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, (size_t)nb));
-        VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, tf->d_prefix, tf->width, vol->desc.rwm_scale,
+        // skip cells: the requested edge if the volume holds that level, else the brick
+        const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
+        const float* cmin = vol->d_bmin;
+        const float* cmax = vol->d_bmax;
+        int C = vol->L.B;
+        int nc[3] = {vol->L.nb[0], vol->L.nb[1], vol->L.nb[2]};
+        for (const auto& lv : vol->levels)
+            if (lv.C == want && lv.d_min) {
+                cmin = lv.d_min;
+                cmax = lv.d_max;
+                C = lv.C;
+                for (int i = 0; i < 3; ++i) nc[i] = lv.nc[i];
+            }
+        const long long n = (long long)nc[0] * nc[1] * nc[2];
+        VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, (size_t)n));
+        VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, tf->d_prefix, tf->width, vol->desc.rwm_scale,
                                             vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
         P.occupancy = ctx->d_occ;
+        P.cshift = ilog2(C);
+        for (int i = 0; i < 3; ++i) P.nc[i] = nc[i];
+        const int maxdim = std::max(vol->desc.dims[0], std::max(vol->desc.dims[1], vol->desc.dims[2]));
+        P.skip_margin = 0.01f + 2e-5f * float(maxdim);
     }
     VRC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 16 * sizeof(unsigned long long), s));
     P.counters = ctx->d_counters;

@@ -275,6 +275,29 @@ struct Counters {
     unsigned long long samples = 0, fetched = 0, shaded = 0;
 };
 
+// Largest ray parameter up to which every sample's floor voxel stays in skip
+// cell (cx, cy, cz): per axis, where the unclamped voxel coordinate
+// dim * (first + t * dir) - 0.5 reaches the cell face it moves toward, pulled
+// in by skip_margin voxels to absorb rounding. Cells on the volume border have
+// no face on their outer side (clamping keeps samples there).
+__device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, float dx, float dy, float dz, int cx,
+                                             int cy, int cz) {
+    const int C = 1 << P.cshift;
+    const float fo[3] = {f.x, f.y, f.z}, di[3] = {dx, dy, dz};
+    const int ci[3] = {cx, cy, cz};
+    float tmax = INFINITY;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float a = P.dimf[i] * fo[i] - 0.5f, b = P.dimf[i] * di[i];
+        if (b > 0.f && ci[i] < P.nc[i] - 1) {
+            tmax = fminf(tmax, ((float)((ci[i] + 1) * C) - P.skip_margin - a) / b);
+        } else if (b < 0.f && ci[i] > 0) {
+            tmax = fminf(tmax, ((float)(ci[i] * C) + P.skip_margin - a) / b);
+        }
+    }
+    return tmax;
+}
+
 // One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
 template <int DT, int COMP, int SHADE, int EE>
 __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
@@ -303,17 +326,31 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     float t = 0.f;
     bool finished = false;
     int loop = 0;
-    for (; !finished && loop < LOOP_CAP; ++loop) {
+    while (!finished && loop < LOOP_CAP) {
         const float sx = a_(f.x, m_(t, dx)), sy = a_(f.y, m_(t, dy)), sz = a_(f.z, m_(t, dz));
         const float vx = clampf_(s_(m_(P.dimf[0], sx), 0.5f), 0.f, P.dim_m1[0]);
         const float vy = clampf_(s_(m_(P.dimf[1], sy), 0.5f), 0.f, P.dim_m1[1]);
         const float vz = clampf_(s_(m_(P.dimf[2], sz), 0.5f), 0.f, P.dim_m1[2]);
         const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
         const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
-        const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
-        const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
-        const bool occupied = P.occupancy == nullptr || P.occupancy[brick] != 0;
-        if (occupied) {
+        if (P.occupancy) {
+            const int cx = ix >> P.cshift, cy = iy >> P.cshift, cz = iz >> P.cshift;
+            if (P.occupancy[((long long)cz * P.nc[1] + cy) * P.nc[0] + cx] == 0) {
+                // This sample lies in a cell where every reachable TF entry has
+                // alpha 0: it changes nothing. So do all following samples that
+                // provably stay in the cell; only t and the count advance.
+                const float tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz);
+                do {
+                    t = a_(t, step);
+                    ++loop;
+                    finished = t > tend;
+                } while (!finished && loop < LOOP_CAP && t <= tsafe);
+                continue;
+            }
+        }
+        {
+            const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
+            const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
             ++cnt.fetched;
             const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
             const T* __restrict__ b = bricks + brick * L.brick_stride;
@@ -377,6 +414,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             finished = true;
         }
         t = a_(t, step);
+        ++loop;
         finished = finished || (t > tend);
     }
     cnt.samples += (unsigned long long)loop;

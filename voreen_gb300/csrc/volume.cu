@@ -77,6 +77,32 @@ __global__ void brick_minmax_kernel(const T* __restrict__ bricks, BrickLayout L,
     }
 }
 
+// One thread per cell: min/max over the cell's voxels plus one voxel on the
+// high side of every axis (clamped), i.e. the trilinear support of all
+// samples whose floor voxel lies in the cell.
+template <typename T>
+__global__ void cell_minmax_kernel(const T* __restrict__ lin, int X, int Y, int Z, int C, int ncx, int ncy,
+                                   long long ncells, float norm, float* cmin, float* cmax) {
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < ncells;
+         c += (long long)gridDim.x * blockDim.x) {
+        const int cx = (int)(c % ncx), cy = (int)((c / ncx) % ncy), cz = (int)(c / ((long long)ncx * ncy));
+        const int x0 = cx * C, y0 = cy * C, z0 = cz * C;
+        const int x1 = min(x0 + C, X - 1), y1 = min(y0 + C, Y - 1), z1 = min(z0 + C, Z - 1);
+        float mn = INFINITY, mx = -INFINITY;
+        for (int z = z0; z <= z1; ++z)
+            for (int y = y0; y <= y1; ++y) {
+                const T* row = lin + ((long long)z * Y + y) * X;
+                for (int x = x0; x <= x1; ++x) {
+                    const float v = raw_to_float(row[x]);
+                    mn = fminf(mn, v);
+                    mx = fmaxf(mx, v);
+                }
+            }
+        cmin[c] = norm > 0.f ? __fdiv_rn(mn, norm) : mn;
+        cmax[c] = norm > 0.f ? __fdiv_rn(mx, norm) : mx;
+    }
+}
+
 __device__ __forceinline__ float rw_to_tf(float rw, float lo, float hi) {
     if (rw < lo) return 0.f;
     if (rw > hi) return 1.f;
@@ -146,6 +172,28 @@ cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout
             break;
         default:
             brick_minmax_kernel<float><<<(unsigned)n, 256, 0, s>>>((const float*)bricks, L, 0.f, bmin, bmax);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_cell_minmax(const void* linear, int dtype, const int d[3], int C, float* cmin, float* cmax,
+                               cudaStream_t s) {
+    const int ncx = (d[0] + C - 1) / C, ncy = (d[1] + C - 1) / C, ncz = (d[2] + C - 1) / C;
+    const long long n = (long long)ncx * ncy * ncz;
+    const int g = grid_for(n, 128);
+    switch (dtype) {
+        case VRC_U8:
+            cell_minmax_kernel<uint8_t><<<g, 128, 0, s>>>((const uint8_t*)linear, d[0], d[1], d[2], C, ncx, ncy, n,
+                                                          255.f, cmin, cmax);
+            break;
+        case VRC_U16:
+            cell_minmax_kernel<uint16_t><<<g, 128, 0, s>>>((const uint16_t*)linear, d[0], d[1], d[2], C, ncx, ncy, n,
+                                                           65535.f, cmin, cmax);
+            break;
+        default:
+            cell_minmax_kernel<float><<<g, 128, 0, s>>>((const float*)linear, d[0], d[1], d[2], C, ncx, ncy, n, 0.f,
+                                                        cmin, cmax);
             break;
     }
     return cudaGetLastError();

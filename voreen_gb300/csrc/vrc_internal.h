@@ -38,7 +38,10 @@ struct BrickLayout {
 // Parameters of one march launch (passed by value).
 struct MarchParams {
     const void* bricks;
-    const uint8_t* occupancy;   // one byte per brick; nullptr = no skipping
+    const uint8_t* occupancy;   // one byte per skip cell; nullptr = no skipping
+    int cshift;                 // log2(skip cell edge)
+    int nc[3];                  // skip cell grid
+    float skip_margin;          // voxels kept clear of a cell face when skipping by t range
     const float4* tf_table;     // (r, g, b, alpha') per TF entry
     int tf_width;
     BrickLayout L;
@@ -74,6 +77,10 @@ cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp
 cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
                                 cudaStream_t s);
+// Min/max of normalised intensity per cell of edge C over the cell's voxels
+// plus one voxel on the high side (clamped), from the linear volume.
+cudaError_t launch_cell_minmax(const void* linear, int dtype, const int dims[3], int C, float* cmin, float* cmax,
+                               cudaStream_t s);
 cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nbricks, const int* alpha_prefix,
                              int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
                              uint8_t* occ, cudaStream_t s);
@@ -99,6 +106,14 @@ struct vrc_context {
     unsigned long long* d_counters = nullptr;  // 4 counters + status + tile counter
 };
 
+struct vrc_cell_level {
+    int C = 0;
+    int nc[3] = {0, 0, 0};
+    float* d_min = nullptr;
+    float* d_max = nullptr;
+    long long count() const { return (long long)nc[0] * nc[1] * nc[2]; }
+};
+
 struct vrc_volume {
     vrc_context* ctx = nullptr;
     vrc_volume_desc desc{};
@@ -106,6 +121,7 @@ struct vrc_volume {
     void* d_bricks = nullptr;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
+    vrc_cell_level levels[2];  // skip cells of edge 8 and 16 (when smaller than the brick)
     size_t bytes = 0;
     float vmin = 0.f, vmax = 0.f;
 };
