@@ -278,8 +278,10 @@ struct Counters {
 // Largest ray parameter up to which every sample's floor voxel stays in skip
 // cell (cx, cy, cz): per axis, where the unclamped voxel coordinate
 // dim * (first + t * dir) - 0.5 reaches the cell face it moves toward, pulled
-// in by skip_margin voxels to absorb rounding. Cells on the volume border have
-// no face on their outer side (clamping keeps samples there).
+// in by skip_margin voxels to absorb rounding (the margin exceeds the error of
+// the sample-position arithmetic and of the fast division here by orders of
+// magnitude). Cells on the volume border have no face on their outer side:
+// clamping keeps samples there.
 __device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, float dx, float dy, float dz, int cx,
                                              int cy, int cz) {
     const int C = 1 << P.cshift;
@@ -290,12 +292,41 @@ __device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, flo
     for (int i = 0; i < 3; ++i) {
         const float a = P.dimf[i] * fo[i] - 0.5f, b = P.dimf[i] * di[i];
         if (b > 0.f && ci[i] < P.nc[i] - 1) {
-            tmax = fminf(tmax, ((float)((ci[i] + 1) * C) - P.skip_margin - a) / b);
+            tmax = fminf(tmax, __fdividef((float)((ci[i] + 1) * C) - P.skip_margin - a, b));
         } else if (b < 0.f && ci[i] > 0) {
-            tmax = fminf(tmax, ((float)(ci[i] * C) + P.skip_margin - a) / b);
+            tmax = fminf(tmax, __fdividef((float)(ci[i] * C) + P.skip_margin - a, b));
         }
     }
     return tmax;
+}
+
+// Advances (t, loop) over the samples of an empty run in closed form: every
+// sample with t <= lim is processed (and changes nothing). The FP32 sum
+// t + step, for t on the grid of its binade [2^(e-1), 2^e) with spacing u,
+// is exactly t + q with q = round(step / u) * u unless step / u ends in .5
+// (a rounding tie, left to the caller's exact loop). So n steps inside the
+// binade give exactly t + n * q, the value the reference's one-at-a-time
+// accumulation t += samplingStepSize produces. Stops short of the binade end
+// and of LOOP_CAP; the caller finishes with exact single steps.
+__device__ __forceinline__ void jump_empty_run(float& t, int& loop, float step, float lim) {
+    const int bits = __float_as_int(t);
+    const int ex = (bits >> 23) & 0xff;  // biased exponent, t normal and > 0
+    if (ex < 24 || ex > 250) return;
+    const float u = __int_as_float((ex - 23) << 23);     // ulp of t: 2^(ex - 127 - 23)
+    const float top = __int_as_float((ex + 1) << 23);    // 2^(ex - 127 + 1): end of t's binade
+    const float k = __fmul_rn(step, __int_as_float((127 + 150 - ex) << 23));  // step / u, exact
+    const float kf = floorf(k);
+    if (__fsub_rn(k, kf) == 0.5f) return;
+    const float q = __fmul_rn(rintf(k), u);
+    if (q <= 0.f) return;
+    float nf = floorf(__fdividef(__fsub_rn(lim, t), q)) + 1.f;
+    nf = fminf(nf, floorf(__fdividef(__fsub_rn(top, t), q)));
+    nf = fminf(nf, (float)(LOOP_CAP - loop));
+    int n = nf > 0.f ? (int)nf : 0;
+    while (n > 0 && (__fadd_rn(t, __fmul_rn((float)(n - 1), q)) > lim || __fadd_rn(t, __fmul_rn((float)n, q)) >= top))
+        --n;
+    t = __fadd_rn(t, __fmul_rn((float)n, q));
+    loop += n;
 }
 
 // One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
@@ -340,11 +371,15 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                 // alpha 0: it changes nothing. So do all following samples that
                 // provably stay in the cell; only t and the count advance.
                 const float tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz);
-                do {
+                t = a_(t, step);
+                ++loop;
+                const float lim = fminf(tsafe, tend);
+                if (t <= lim && loop < LOOP_CAP) jump_empty_run(t, loop, step, lim);
+                while (!(t > tend) && loop < LOOP_CAP && t <= tsafe) {
                     t = a_(t, step);
                     ++loop;
-                    finished = t > tend;
-                } while (!finished && loop < LOOP_CAP && t <= tsafe);
+                }
+                finished = t > tend;
                 continue;
             }
         }
