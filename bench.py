@@ -165,6 +165,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--profile", action="store_true",
                     help="device frames only (no e2e, no CPU baseline): the command line for ncu captures")
     args = ap.parse_args()
@@ -183,7 +184,7 @@ def main():
     import voreen_gb300 as v
 
     w = build_workload(args.small)
-    p = w.params()
+    p = w.params(skip_cell_size=args.skip_cell)
     npix = w.width * w.height
     config = {"workload": w.name, "volume": list(w.dims), "dtype_volume": "uint16", "spacing": list(w.spacing),
               "image": [w.width, w.height], "sampling_rate": w.sampling_rate, "tf_width": w.tf_width,

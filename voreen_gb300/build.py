@@ -55,6 +55,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
+    """Compile and link libvrc.so. VRC_MARCH_MIN_BLOCKS (environment) sets the
+    march kernel's minimum resident CTAs per SM for register allocation."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
@@ -64,7 +66,12 @@ def build(verbose: bool = False, force: bool = False) -> str:
         path = os.path.join(CSRC, src)
         obj = os.path.join(BUILD, src.replace(".", "_") + ".o")
         objs.append(obj)
-        if force or _stale(obj, [path] + hdrs):
+        if src == "march.cu" and os.environ.get("VRC_MARCH_MIN_BLOCKS"):
+            extra = extra + [f"-DVRC_MARCH_MIN_BLOCKS={int(os.environ['VRC_MARCH_MIN_BLOCKS'])}"]
+            force_this = True
+        else:
+            force_this = False
+        if force or force_this or _stale(obj, [path] + hdrs):
             cmd = [cc, *ARCH, *COMMON, *extra, "-c", path, "-o", obj]
             if src.endswith(".cpp"):
                 cmd.insert(1, "-x")

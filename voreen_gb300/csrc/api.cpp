@@ -546,6 +546,8 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
         P.offs[i] = 1.f / float(d.dims[i]);
         P.spacing[i] = d.spacing[i];
         P.spacing_rcp_half[i] = (1.f / d.spacing[i]) * 0.5f;
+        const float range = d.dtype == VRC_U8 ? 255.f : (d.dtype == VRC_U16 ? 65535.f : 1.f);
+        P.gscale[i] = P.spacing_rcp_half[i] * d.rwm_scale / range;
         P.vol_offset[i] = d.offset[i];
         // physicalToWorld is the identity: physical == world
         P.light_phys[i] = p->light_position[i];

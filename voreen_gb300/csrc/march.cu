@@ -20,11 +20,13 @@
 //    computed as q0 = v*r, q = fma(fma(-q0, d, v), r, q0), which equals the
 //    correctly rounded quotient for every 8- and 16-bit value;
 //  * gradients (central differences, mod_gradients.frag:202-214) are six
-//    lookups at +-1/dim in texture space, clamped and interpolated exactly as
-//    the intensity sample; each lookup finds its own brick, so lookups that
-//    cross a brick face stay exact. Phong (mod_shading.frag:134-151) runs in
-//    registers; its pow is CUDA's powf, the only step that is not bit-equal
-//    with the CPU path.
+//    lookups at +-1/dim in texture space, clamped like the intensity sample
+//    and read from the centre's brick apron (another brick only when rounding
+//    puts a tap two voxels away); they interpolate raw voxel values with FMA
+//    lerps. Phong (mod_shading.frag:134-151) runs in registers with fast
+//    reciprocal square roots and __powf. Shading only colours samples whose
+//    alpha is already decided, so it changes no discrete decision; its
+//    colours differ from the CPU path by ~1e-6.
 #include <cstdint>
 
 #include "vrc_internal.h"
@@ -90,21 +92,6 @@ __device__ __forceinline__ float tri_at(const typename Vox<DT>::T* __restrict__ 
                 V::norm(__ldg(b + o + S2 + S + 1)), V::norm(__ldg(b + o + S2 + S)), fx, fy, fz);
 }
 
-// Trilinear value at a clamped voxel position, from the brick that holds
-// its floor voxel (VolumeRAM::getVoxelNormalizedLinear on the bricked layout).
-template <int DT>
-__device__ __forceinline__ float sample_at(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
-                                           float vx, float vy, float vz) {
-    const BrickLayout& L = P.L;
-    const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
-    const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
-    const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
-    const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
-    const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
-                  (ix - (bx << L.shift) + APRON_LO);
-    return tri_at<DT>(bricks + brick * L.brick_stride, o, L.S, L.S * L.S, s_(vx, flx), s_(vy, fly), s_(vz, flz));
-}
-
 __device__ __forceinline__ float clampf_(float x, float lo, float hi) {
     x = x > lo ? x : lo;
     return x < hi ? x : hi;
@@ -142,6 +129,91 @@ __device__ __forceinline__ float dot3(F3 a, F3 b) {
     s = a_(s, m_(a.y, b.y));
     s = a_(s, m_(a.z, b.z));
     return s;
+}
+
+// ---- shading path ----------------------------------------------------
+// Shading feeds only the colour of samples with alpha > 0; it has no
+// discrete decision and its pow is not correctly rounded on any platform, so
+// it uses fused multiply-adds, fast reciprocal square roots and __powf. The
+// resulting colour differs from the CPU path by ~1e-6 relative.
+__device__ __forceinline__ F3 fnormalize(F3 v) {
+    const float l2 = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, __fmul_rn(v.z, v.z)));
+    if (l2 == 0.f) return F3{0.f, 0.f, 0.f};
+    const float r = rsqrtf(l2);
+    return F3{v.x * r, v.y * r, v.z * r};
+}
+__device__ __forceinline__ float fdot(F3 a, F3 b) { return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, __fmul_rn(a.z, b.z))); }
+
+// Trilinear interpolation of raw voxel values with FMA lerps (gradient taps).
+template <int DT>
+__device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__ b, int o, int S, int S2, float fx,
+                                         float fy, float fz) {
+    const float v000 = (float)__ldg(b + o), v100 = (float)__ldg(b + o + 1);
+    const float v010 = (float)__ldg(b + o + S), v110 = (float)__ldg(b + o + S + 1);
+    const float v001 = (float)__ldg(b + o + S2), v101 = (float)__ldg(b + o + S2 + 1);
+    const float v011 = (float)__ldg(b + o + S2 + S), v111 = (float)__ldg(b + o + S2 + S + 1);
+    const float x00 = __fmaf_rn(fx, v100 - v000, v000), x10 = __fmaf_rn(fx, v110 - v010, v010);
+    const float x01 = __fmaf_rn(fx, v101 - v001, v001), x11 = __fmaf_rn(fx, v111 - v011, v011);
+    const float y0 = __fmaf_rn(fy, x10 - x00, x00), y1 = __fmaf_rn(fy, x11 - x01, x01);
+    return __fmaf_rn(fz, y1 - y0, y0);
+}
+
+// Raw trilinear value at a clamped voxel position from the brick holding it.
+template <int DT>
+__device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
+                                                float vx, float vy, float vz) {
+    const BrickLayout& L = P.L;
+    const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
+    const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
+    const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
+    const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
+    const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
+                  (ix - (bx << L.shift) + APRON_LO);
+    return tri_raw<DT>(bricks + brick * L.brick_stride, o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
+}
+
+// One central-difference lookup displaced along one axis: tap position `vt`
+// (clamped voxel coordinate on that axis, as calcGradientA's texture lookup
+// gives it) with the centre's coordinates on the other axes. Reads from the
+// centre's brick when the stencil fits in its apron.
+template <int DT, int AXIS>
+__device__ __forceinline__ float grad_tap(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
+                                          const typename Vox<DT>::T* __restrict__ b, int o, int lc, int ic, float vt,
+                                          float vx, float vy, float vz, float fx, float fy, float fz) {
+    const float fl = floorf(vt);
+    const int it = (int)fl;
+    const int lt = lc + (it - ic);
+    const int S = P.L.S, S2 = P.L.S * P.L.S;
+    if (lt >= 0 && lt <= P.L.B + 1) {
+        const int stride = AXIS == 0 ? 1 : (AXIS == 1 ? S : S2);
+        const float ft = vt - fl;
+        return tri_raw<DT>(b, o + (it - ic) * stride, S, S2, AXIS == 0 ? ft : fx, AXIS == 1 ? ft : fy,
+                           AXIS == 2 ? ft : fz);
+    }
+    return tap_raw_any_brick<DT>(P, bricks, AXIS == 0 ? vt : vx, AXIS == 1 ? vt : vy, AXIS == 2 ? vt : vz);
+}
+
+// phongShading (mod_shading.frag:134-151), ka = kd = TF colour, ks = 1.
+__device__ __forceinline__ F3 phong_fast(const MarchParams& P, F3 n, F3 pos, F3 col) {
+    const F3 N = fnormalize(n);
+    F3 L{P.light_phys[0] - pos.x, P.light_phys[1] - pos.y, P.light_phys[2] - pos.z};
+    const F3 V = fnormalize(F3{P.cam_phys[0] - pos.x, P.cam_phys[1] - pos.y, P.cam_phys[2] - pos.z});
+    const float d2 = fdot(L, L);
+    const float rd = d2 > 0.f ? rsqrtf(d2) : 0.f;
+    const float d = d2 * rd;
+    L = F3{L.x * rd, L.y * rd, L.z * rd};
+    const float ndl = fmaxf(fdot(N, L), 0.f);
+    const F3 Hh = fnormalize(F3{V.x + L.x, V.y + L.y, V.z + L.z});
+    const float ndh = fmaxf(fdot(N, Hh), 0.f);
+    const float spec = __powf(ndh, P.shininess);
+    F3 out{__fmaf_rn(col.x * P.dif[0], ndl, __fmaf_rn(P.spec[0], spec, col.x * P.amb[0])),
+           __fmaf_rn(col.y * P.dif[1], ndl, __fmaf_rn(P.spec[1], spec, col.y * P.amb[1])),
+           __fmaf_rn(col.z * P.dif[2], ndl, __fmaf_rn(P.spec[2], spec, col.z * P.amb[2]))};
+    if (P.atten_on) {
+        const float att = fminf(__fdividef(1.f, __fmaf_rn(P.att[2] * d, d, __fmaf_rn(P.att[1], d, P.att[0]))), 1.f);
+        out = F3{out.x * att, out.y * att, out.z * att};
+    }
+    return out;
 }
 
 // Analytic entry/exit for pixel (px, py): the pixel-centre ray through the
@@ -223,34 +295,6 @@ template <int EE> __device__ F3 clip_border_gradient(const MarchParams& P, F3 s,
     F3 g{s_(m_(v0.y, v1.z), m_(v0.z, v1.y)), s_(m_(v0.z, v1.x), m_(v0.x, v1.z)), s_(m_(v0.x, v1.y), m_(v0.y, v1.x))};
     if (!(dot3(g, dir) < 0.f)) g = F3{-g.x, -g.y, -g.z};
     return g;
-}
-
-// phongShading (mod_shading.frag:134-151), ka = kd = TF colour, ks = 1.
-__device__ __forceinline__ F3 phong(const MarchParams& P, F3 n, F3 pos, F3 col) {
-    const F3 N = normalize3(n);
-    F3 L{s_(P.light_phys[0], pos.x), s_(P.light_phys[1], pos.y), s_(P.light_phys[2], pos.z)};
-    const F3 V = normalize3(F3{s_(P.cam_phys[0], pos.x), s_(P.cam_phys[1], pos.y), s_(P.cam_phys[2], pos.z)});
-    const float d = len3(L.x, L.y, L.z);
-    L = F3{d_(L.x, d), d_(L.y, d), d_(L.z, d)};
-    F3 out{m_(col.x, P.amb[0]), m_(col.y, P.amb[1]), m_(col.z, P.amb[2])};
-    float ndl = dot3(N, L);
-    ndl = ndl > 0.f ? ndl : 0.f;
-    out.x = a_(out.x, m_(m_(col.x, P.dif[0]), ndl));
-    out.y = a_(out.y, m_(m_(col.y, P.dif[1]), ndl));
-    out.z = a_(out.z, m_(m_(col.z, P.dif[2]), ndl));
-    const F3 Hh = normalize3(F3{a_(V.x, L.x), a_(V.y, L.y), a_(V.z, L.z)});
-    float ndh = dot3(N, Hh);
-    ndh = ndh > 0.f ? ndh : 0.f;
-    const float spec = powf(ndh, P.shininess);
-    out.x = a_(out.x, m_(P.spec[0], spec));
-    out.y = a_(out.y, m_(P.spec[1], spec));
-    out.z = a_(out.z, m_(P.spec[2], spec));
-    if (P.atten_on) {
-        float att = d_(1.f, a_(a_(P.att[0], m_(P.att[1], d)), m_(m_(P.att[2], d), d)));
-        att = att < 1.f ? att : 1.f;
-        out = F3{m_(out.x, att), m_(out.y, att), m_(out.z, att)};
-    }
-    return out;
 }
 
 __device__ __forceinline__ void write_out(const MarchParams& P, size_t pix, float4 r) {
@@ -403,27 +447,25 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                         g = clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py);
                     } else {
                         // calcGradientA: six lookups at +-1/dim in texture space, each
-                        // clamped and interpolated exactly like the intensity sample
+                        // clamped like the intensity sample; interpolated on raw values
                         const float vxp = clampf_(s_(m_(P.dimf[0], a_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
                         const float vyp = clampf_(s_(m_(P.dimf[1], a_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
                         const float vzp = clampf_(s_(m_(P.dimf[2], a_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
                         const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
                         const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
                         const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float v0 = sample_at<DT>(P, bricks, vxp, vy, vz);
-                        const float v1 = sample_at<DT>(P, bricks, vx, vyp, vz);
-                        const float v2 = sample_at<DT>(P, bricks, vx, vy, vzp);
-                        const float v3 = sample_at<DT>(P, bricks, vxm, vy, vz);
-                        const float v4 = sample_at<DT>(P, bricks, vx, vym, vz);
-                        const float v5 = sample_at<DT>(P, bricks, vx, vy, vzm);
-                        g = F3{m_(m_(s_(v3, v0), P.spacing_rcp_half[0]), P.rwm_scale),
-                               m_(m_(s_(v4, v1), P.spacing_rcp_half[1]), P.rwm_scale),
-                               m_(m_(s_(v5, v2), P.spacing_rcp_half[2]), P.rwm_scale)};
+                        const float v0 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
+                        const float v1 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
+                        const float v2 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
+                        const float v3 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
+                        const float v4 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
+                        const float v5 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
+                        g = F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
                     }
                     const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
                                  a_(m_(s_(m_(sy, P.dimf[1]), 0.5f), P.spacing[1]), P.vol_offset[1]),
                                  a_(m_(s_(m_(sz, P.dimf[2]), 0.5f), P.spacing[2]), P.vol_offset[2])};
-                    const F3 sh = phong(P, g, pos, F3{c.x, c.y, c.z});
+                    const F3 sh = phong_fast(P, g, pos, F3{c.x, c.y, c.z});
                     c.x = sh.x;
                     c.y = sh.y;
                     c.z = sh.z;
@@ -456,8 +498,12 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     return res;
 }
 
+#ifndef VRC_MARCH_MIN_BLOCKS
+#define VRC_MARCH_MIN_BLOCKS 3
+#endif
+
 template <int DT, int COMP, int SHADE, int EE>
-__global__ void __launch_bounds__(256) march_kernel(MarchParams P) {
+__global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchParams P) {
     extern __shared__ float4 s_tf[];
     for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_table[i];
     __syncthreads();

@@ -47,6 +47,7 @@ struct MarchParams {
     BrickLayout L;
     float dimf[3], dim_m1[3], offs[3];
     float spacing[3], spacing_rcp_half[3], vol_offset[3];
+    float gscale[3];            // raw-value central difference -> gradient: 0.5/spacing * rwmScale / rangeMax
     float rwm_scale, rwm_offset, tf_lo, tf_hi;
     float step, ert;
     int use_ert;
