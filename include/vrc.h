@@ -54,7 +54,8 @@ typedef enum {
     VRC_ERR_UNSUPPORTED = 4,   /* valid request the library does not implement */
     VRC_ERR_TIMEOUT = 5,       /* a bounded device-side wait gave up */
     VRC_ERR_NOT_READY = 6,     /* missing input (isReady() == false in the reference) */
-    VRC_ERR_DEVICE = 7         /* a kernel reported an internal error status */
+    VRC_ERR_DEVICE = 7,        /* a kernel reported an internal error status */
+    VRC_ERR_SCRATCH_LIMIT = 8  /* request exceeds vrc_render_noalloc's fixed scratch capacity */
 } vrc_status;
 
 typedef enum { VRC_U8 = 0, VRC_U16 = 1, VRC_F32 = 2 } vrc_dtype;
@@ -179,6 +180,27 @@ typedef struct {
 vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                       const float* entry, const float* exit_pts, int ee_on_device, void* out, int out_format,
                       int out_on_device, vrc_render_stats* stats);
+
+/* ---- render without allocating ---------------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot call
+ * cudaMalloc while they render -- code inside a CUDA graph capture or a
+ * real-time frame loop (cudaMalloc can synchronise the device), or hosts
+ * whose device memory belongs to their own fixed-budget pool or to another
+ * runtime. It renders like vrc_render but keeps its scratch (sample and tile
+ * counters, the per-render TF table, the empty-space cell map) in one
+ * fixed-size array in device global memory that every GPU loading the
+ * library holds until exit, and it allocates nothing.
+ * Limits: at most VRC_NOALLOC_MAX_CELLS empty-space cells when skipping is on
+ * (a 1024^3 volume at the default 8^3 cells) and TF width <= 4096; larger
+ * requests return VRC_ERR_SCRATCH_LIMIT and render nothing.
+ * The caller passes the inputs (an uploaded volume, a TF, device entry/exit
+ * images unless analytic), the device output image and the cudaStream_t to
+ * run on; the call returns after enqueueing. Its first call on a device sets
+ * up the scratch address for that device: make that call before any stream
+ * capture. All calls share the array: calls that overlap on the GPU race. */
+#define VRC_NOALLOC_MAX_CELLS 2097152
+vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                              const float* d_entry, const float* d_exit, void* d_out, int out_format, void* stream);
 
 /* Analytic entry/exit points (texture space) for `p->camera`, written as
  * float4 images, host or device destination. */

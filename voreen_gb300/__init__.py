@@ -19,7 +19,7 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (DVR, EE_ANALYTIC, EE_BUFFERS, F32, ISO, MIP, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE,
+from ._abi import (DVR, EE_ANALYTIC, EE_BUFFERS, F32, ISO, MIP, NOALLOC_MAX_CELLS, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE,
                    SHADE_PHONG, U8, U16, Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
 
 __all__ = ["VrcError", "Context", "Volume", "TransferFunction", "render", "entry_exit", "default_params",
@@ -258,6 +258,15 @@ def render_async(ctx: Context, vol: Volume, tf: TransferFunction, params: Render
     ee_dev = 1 if (entry is not None and _is_device(entry)) else 0
     _check(lib().vrc_render(ctx.handle, vol.handle, tf.handle, C.byref(params), _ptr(entry), _ptr(exit_pts), ee_dev,
                             _ptr(out), out_format, 1, None), ctx, "vrc_render")
+
+
+def render_noalloc(vol: Volume, tf: TransferFunction, params: RenderParams, entry, exit_pts, out,
+                   out_format: int = OUT_RGBA32F, stream: int = 0):
+    """vrc_render_noalloc: enqueue a frame on `stream` with no allocation.
+    entry/exit/out are CUDA tensors (entry/exit may be None in analytic mode)."""
+    st = lib().vrc_render_noalloc(vol.handle, tf.handle, C.byref(params), _ptr(entry), _ptr(exit_pts), _ptr(out),
+                                  out_format, C.c_void_p(stream))
+    _check(st, None, "vrc_render_noalloc")
 
 
 def entry_exit(ctx: Context, vol: Volume, params: RenderParams):

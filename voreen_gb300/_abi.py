@@ -13,12 +13,14 @@ LIB_PATH = os.path.join(_HERE, "_build", "libvrc.so")
 
 VRC_OK = 0
 STATUS_NAMES = {0: "VRC_OK", 1: "VRC_ERR_INVALID_ARG", 2: "VRC_ERR_CUDA", 3: "VRC_ERR_OUT_OF_MEMORY",
-                4: "VRC_ERR_UNSUPPORTED", 5: "VRC_ERR_TIMEOUT", 6: "VRC_ERR_NOT_READY", 7: "VRC_ERR_DEVICE"}
+                4: "VRC_ERR_UNSUPPORTED", 5: "VRC_ERR_TIMEOUT", 6: "VRC_ERR_NOT_READY", 7: "VRC_ERR_DEVICE",
+                8: "VRC_ERR_SCRATCH_LIMIT"}
 U8, U16, F32 = 0, 1, 2
 DVR, MIP, ISO = 0, 1, 2
 SHADE_NONE, SHADE_PHONG = 0, 1
 OUT_RGBA8, OUT_RGBA32F, OUT_RGBA16 = 0, 1, 2
 EE_BUFFERS, EE_ANALYTIC = 0, 1
+NOALLOC_MAX_CELLS = 2097152
 
 
 class VolumeDesc(C.Structure):
@@ -76,6 +78,7 @@ SIGNATURES = {
     "vrc_render_params_default": (None, [P(RenderParams), C.c_int, C.c_int]),
     "vrc_render": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, C.c_int, VP, C.c_int, C.c_int, P(RenderStats)]),
     "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
+    "vrc_render_noalloc": (C.c_int, [VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
 }
 

@@ -28,6 +28,7 @@ SOURCES = [
     ("synth.cpp", []),
     ("volume.cu", []),
     ("march.cu", ["-fmad=false"]),
+    ("noalloc.cu", []),
 ]
 
 

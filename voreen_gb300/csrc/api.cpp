@@ -190,6 +190,7 @@ const char* vrc_status_string(vrc_status s) {
         case VRC_ERR_TIMEOUT: return "timeout";
         case VRC_ERR_NOT_READY: return "not ready";
         case VRC_ERR_DEVICE: return "device error";
+        case VRC_ERR_SCRATCH_LIMIT: return "request exceeds the fixed scratch of vrc_render_noalloc";
     }
     return "unknown status";
 }
@@ -532,6 +533,10 @@ vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, f
     return VRC_OK;
 }
 
+}  // namespace
+
+namespace vrc {
+
 vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P) {
     std::memset(&P, 0, sizeof(P));
     const vrc_volume_desc& d = vol->desc;
@@ -572,31 +577,35 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
     if (p->entry_exit_mode == VRC_EE_ANALYTIC) {
         double inv[16];
         if (vrc_camera_matrices(&p->camera, &d, p->width, p->height, nullptr, nullptr, inv) != VRC_OK)
-            return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: camera matrix is singular");
+            return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: camera matrix is singular");
         for (int i = 0; i < 16; ++i) P.inv_mvp[i] = float(inv[i]);
     }
     return VRC_OK;
 }
 
 vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
-    if (!p) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: null params");
+    if (!p) return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: null params");
     if (p->width < 1 || p->height < 1 || (long long)p->width * p->height > (1LL << 28))
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: image size out of range");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: image size out of range");
     if (!(p->sampling_rate > 0.f) || !std::isfinite(p->sampling_rate))
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: sampling_rate must be > 0");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: sampling_rate must be > 0");
     if (p->compositing < VRC_DVR || p->compositing > VRC_ISO)
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown compositing mode");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown compositing mode");
     if (p->shading < VRC_SHADE_NONE || p->shading > VRC_SHADE_PHONG)
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
     if (p->entry_exit_mode != VRC_EE_BUFFERS && p->entry_exit_mode != VRC_EE_ANALYTIC)
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown entry/exit mode");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown entry/exit mode");
     if (p->skip_cell_size != 0 && p->skip_cell_size != 8 && p->skip_cell_size != 16 && p->skip_cell_size != 32 &&
         p->skip_cell_size != 64)
-        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 8, 16, 32 or 64");
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 8, 16, 32 or 64");
     return VRC_OK;
 }
 
-}  // namespace
+}  // namespace vrc
+
+using vrc::check_params;
+using vrc::fill_params;
+
 
 extern "C" {
 

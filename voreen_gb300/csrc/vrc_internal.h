@@ -71,6 +71,10 @@ struct MarchParams {
     int tiles_x, tiles_y;
 };
 
+// Host helpers shared by the render entry points (api.cpp).
+vrc_status check_params(vrc_context* ctx, const vrc_render_params* p);
+vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P);
+
 // Kernel launchers (march.cu / volume.cu). Return cudaError_t.
 cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                          cudaStream_t s);
