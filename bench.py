@@ -166,6 +166,8 @@ def main():
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
+    ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
+    ap.add_argument("--no-skip", action="store_true", help="disable empty-space skipping (exploration only)")
     ap.add_argument("--profile", action="store_true",
                     help="device frames only (no e2e, no CPU baseline): the command line for ncu captures")
     args = ap.parse_args()
@@ -184,7 +186,8 @@ def main():
     import voreen_gb300 as v
 
     w = build_workload(args.small)
-    p = w.params(skip_cell_size=args.skip_cell)
+    p = w.params(skip_cell_size=args.skip_cell, empty_space_skipping=0 if args.no_skip else 1,
+                 shading=v.SHADE_PHONG if args.shading == "phong" else v.SHADE_NONE)
     npix = w.width * w.height
     config = {"workload": w.name, "volume": list(w.dims), "dtype_volume": "uint16", "spacing": list(w.spacing),
               "image": [w.width, w.height], "sampling_rate": w.sampling_rate, "tf_width": w.tf_width,
@@ -298,7 +301,7 @@ def main():
             "dtype": "f32", "data": "synthetic (seeded procedural 512^3 u16 CT-like shells)", "config": config,
             "gsamples_per_s": samples / (ms * 1e-3) / 1e9 * ws,
             "samples_per_frame": samples, "shaded_samples_per_frame": shaded,
-            "samples_fetched_per_frame": st.samples_fetched,
+            "samples_fetched_per_frame": st.samples_fetched, "skip_runs_per_frame": st.skip_runs,
             "kernel_ms": k_ms,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

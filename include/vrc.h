@@ -165,6 +165,7 @@ typedef struct {
     double samples;          /* loop iterations of all rays (the reference's sample count) */
     double samples_fetched;  /* samples whose voxels were read (not skipped) */
     double samples_shaded;   /* samples with TF alpha > 0 under shading */
+    double skip_runs;        /* runs of samples skipped through empty cells */
     float kernel_ms;         /* device time of the march kernel on the context stream */
     float total_ms;          /* device time from first copy-in to last copy-out */
     int device_status;       /* 0, or an internal error code from the kernel */

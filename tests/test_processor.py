@@ -1,0 +1,54 @@
+"""The processor-shaped interface (voreen_gb300.raycaster.CudaRaycaster):
+port and property names and defaults as in the reference (CPU), and one
+render through it against the oracle (GPU)."""
+import numpy as np
+import pytest
+
+import voreen_gb300 as v
+from voreen_gb300 import synth
+from voreen_gb300.raycaster import CudaRaycaster, VolumeData
+
+
+def test_ports_and_property_defaults(vrc_lib):
+    r = CudaRaycaster()
+    assert r.volumeInport.name == "volumehandle.volumehandle"
+    assert r.entryPort.name == "image.entrypoints" and r.exitPort.name == "image.exitpoints"
+    assert r.outport.name == "image.output"
+    assert r.samplingRate == 2.0 and r.isoValue == 0.5
+    assert r.compositing == "dvr" and r.gradient == "central-differences"
+    assert r.lightPosition == (2.3, 1.5, 1.5, 1.0) and r.materialShininess == 60.0
+    assert not r.isReady()
+
+
+def test_process_not_ready_logs_and_returns(vrc_lib):
+    r = CudaRaycaster()
+    r._ctx = object()  # no device needed: process() must stop before touching it
+    r.process()
+    assert "not ready" in r.lastError and not r.outport.hasData()
+
+
+@pytest.mark.gpu
+def test_process_renders_like_the_oracle(ctx):
+    import oracle
+    from helpers import oracle_entry_exit, oracle_params
+    w = synth.config2(size=(64, 60, 56), image=(96, 72))
+    r = CudaRaycaster()
+    r.volumeInport.setData(VolumeData(w.voxels, w.spacing))
+    r.transferFunction.keys = w.tf_keys
+    p = w.params(shading=v.SHADE_NONE)
+    r.camera = p.camera
+    desc = v.make_desc(v.U16, w.dims, w.spacing)
+    e, x = oracle_entry_exit(desc, p)
+    r.entryPort.setData(e)
+    r.exitPort.setData(x)
+    r.process()
+    assert r.lastError == ""
+    img = r.outport.getData()
+    # domain fitted to the volume's real-world min/max, width 4096 for u16
+    assert r.transferFunction.width == 4096
+    lo, hi = r.transferFunction.domain
+    assert np.isclose(lo, w.voxels.min() / 65535.0) and np.isclose(hi, w.voxels.max() / 65535.0)
+    tf = v.TransferFunction.bake(w.tf_keys, 4096)
+    ref, _, _ = oracle.render(oracle.make_volume(w.voxels, w.spacing), tf, (lo, hi), oracle_params(p), e, x, 32)
+    np.testing.assert_array_equal(img.view(np.uint32), ref.view(np.uint32))
+    r.deinitialize()

@@ -43,6 +43,27 @@ def exact(t, loop, step, lim, tend):
     return t, loop
 
 
+def skip(t, loop, step, lim):
+    """The march's skip loop: jump inside a binade, single-step across its edge."""
+    while t <= lim and loop < CAP:
+        t, loop = jump(t, loop, step, lim)
+        if t <= lim and loop < CAP:
+            t = f32(t + step)
+            loop += 1
+    return t, loop
+
+
+def test_skip_loop_across_binades():
+    rng = np.random.default_rng(1)
+    for _ in range(3000):
+        step = f32(1.0 / (f32(rng.choice([100, 256, 333, 1024, 3072])) * f32(rng.choice([1, 1.5, 2, 3.7]))))
+        t = f32(rng.uniform(0.05, 1.2))
+        lim = f32(t + rng.uniform(0, 0.9))   # runs that cross binade edges (0.125, 0.25, 0.5, 1)
+        tend = f32(rng.uniform(float(t), 1.74))
+        L = min(lim, tend)
+        assert skip(t, 0, step, L) == exact(t, 0, step, L, tend)
+
+
 def test_jump_equals_accumulation():
     rng = np.random.default_rng(0)
     for _ in range(5000):

@@ -56,8 +56,9 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    """Compile and link libvrc.so. VRC_MARCH_MIN_BLOCKS (environment) sets the
-    march kernel's minimum resident CTAs per SM for register allocation."""
+    """Compile and link libvrc.so. Environment tuning knobs for the march
+    kernel: VRC_MARCH_MIN_BLOCKS (minimum resident CTAs per SM, bounds the
+    registers) and VRC_MARCH_ROUND (loop iterations per lane between refills)."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
@@ -67,11 +68,10 @@ def build(verbose: bool = False, force: bool = False) -> str:
         path = os.path.join(CSRC, src)
         obj = os.path.join(BUILD, src.replace(".", "_") + ".o")
         objs.append(obj)
-        if src == "march.cu" and os.environ.get("VRC_MARCH_MIN_BLOCKS"):
-            extra = extra + [f"-DVRC_MARCH_MIN_BLOCKS={int(os.environ['VRC_MARCH_MIN_BLOCKS'])}"]
-            force_this = True
-        else:
-            force_this = False
+        tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS", "VRC_MARCH_ROUND")
+                if src == "march.cu" and os.environ.get(k)]
+        extra = extra + tune
+        force_this = bool(tune)
         if force or force_this or _stale(obj, [path] + hdrs):
             cmd = [cc, *ARCH, *COMMON, *extra, "-c", path, "-o", obj]
             if src.endswith(".cpp"):

@@ -235,6 +235,7 @@ vrc_status vrc_context_destroy(vrc_context* c) {
     cudaFree(c->d_ee);
     cudaFree(c->d_out);
     cudaFree(c->d_occ);
+    cudaFree(c->d_occ_coarse);
     cudaFree(c->d_prefix);
     cudaFree(c->d_counters);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -673,7 +674,7 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
                 for (int i = 0; i < 3; ++i) nc[i] = lv.nc[i];
             }
         const long long n = (long long)nc[0] * nc[1] * nc[2];
-        VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, (size_t)n));
+        VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, vrc::occupancy_bytes(n)));
         VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, tf->d_prefix, tf->width, vol->desc.rwm_scale,
                                             vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
         P.occupancy = ctx->d_occ;
@@ -681,6 +682,17 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
         for (int i = 0; i < 3; ++i) P.nc[i] = nc[i];
         const int maxdim = std::max(vol->desc.dims[0], std::max(vol->desc.dims[1], vol->desc.dims[2]));
         P.skip_margin = 0.01f + 2e-5f * float(maxdim);
+        if (C < vol->L.B) {
+            // coarse level: whole bricks, tested first
+            const long long nb = vol->L.nbricks();
+            VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes, vrc::occupancy_bytes(nb)));
+            VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, tf->d_prefix, tf->width,
+                                                vol->desc.rwm_scale, vol->desc.rwm_offset, tf->lo, tf->hi,
+                                                ctx->d_occ_coarse, s));
+            P.occ_coarse = ctx->d_occ_coarse;
+            P.cshift_coarse = vol->L.shift;
+            for (int i = 0; i < 3; ++i) P.ncc[i] = vol->L.nb[i];
+        }
     }
     VRC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 16 * sizeof(unsigned long long), s));
     P.counters = ctx->d_counters;
@@ -698,6 +710,7 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
         stats->samples = double(h[0]);
         stats->samples_fetched = double(h[1]);
         stats->samples_shaded = double(h[2]);
+        stats->skip_runs = double(h[3]);
         stats->device_status = int(h[4] & 0xffffffffu);
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->kernel_ms, ctx->ev[1], ctx->ev[2]));
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->total_ms, ctx->ev[0], ctx->ev[3]));

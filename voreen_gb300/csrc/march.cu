@@ -316,7 +316,7 @@ __device__ __forceinline__ void write_out(const MarchParams& P, size_t pix, floa
 }
 
 struct Counters {
-    unsigned long long samples = 0, fetched = 0, shaded = 0;
+    unsigned long long samples = 0, fetched = 0, shaded = 0, runs = 0;
 };
 
 // Largest ray parameter up to which every sample's floor voxel stays in skip
@@ -327,15 +327,15 @@ struct Counters {
 // magnitude). Cells on the volume border have no face on their outer side:
 // clamping keeps samples there.
 __device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, float dx, float dy, float dz, int cx,
-                                             int cy, int cz) {
-    const int C = 1 << P.cshift;
+                                             int cy, int cz, int shift, const int* nc) {
+    const int C = 1 << shift;
     const float fo[3] = {f.x, f.y, f.z}, di[3] = {dx, dy, dz};
     const int ci[3] = {cx, cy, cz};
     float tmax = INFINITY;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         const float a = P.dimf[i] * fo[i] - 0.5f, b = P.dimf[i] * di[i];
-        if (b > 0.f && ci[i] < P.nc[i] - 1) {
+        if (b > 0.f && ci[i] < nc[i] - 1) {
             tmax = fminf(tmax, __fdividef((float)((ci[i] + 1) * C) - P.skip_margin - a, b));
         } else if (b < 0.f && ci[i] > 0) {
             tmax = fminf(tmax, __fdividef((float)(ci[i] * C) + P.skip_margin - a, b));
@@ -409,19 +409,43 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
         const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
         const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
         if (P.occupancy) {
-            const int cx = ix >> P.cshift, cy = iy >> P.cshift, cz = iz >> P.cshift;
-            if (P.occupancy[((long long)cz * P.nc[1] + cy) * P.nc[0] + cx] == 0) {
+            // Two skip levels: a whole empty brick-sized cell first, else an
+            // empty fine cell (8^3 by default).
+            float tsafe = 0.f;
+            bool empty = false;
+            if (P.occ_coarse) {
+                const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
+                const long long c = ((long long)cz * P.ncc[1] + cy) * P.ncc[0] + cx;
+                if (((__ldg(P.occ_coarse + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
+                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift_coarse, P.ncc);
+                    empty = true;
+                }
+            }
+            if (!empty) {
+                const int cx = ix >> P.cshift, cy = iy >> P.cshift, cz = iz >> P.cshift;
+                const long long c = ((long long)cz * P.nc[1] + cy) * P.nc[0] + cx;
+                if (((__ldg(P.occupancy + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
+                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift, P.nc);
+                    empty = true;
+                }
+            }
+            if (empty) {
                 // This sample lies in a cell where every reachable TF entry has
                 // alpha 0: it changes nothing. So do all following samples that
                 // provably stay in the cell; only t and the count advance.
-                const float tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz);
+                ++cnt.runs;
                 t = a_(t, step);
                 ++loop;
+                // samples are processed while t <= tend and t <= tsafe: jump to
+                // the end of t's binade in closed form, step across the binade
+                // edge (or a rounding tie) singly, repeat
                 const float lim = fminf(tsafe, tend);
-                if (t <= lim && loop < LOOP_CAP) jump_empty_run(t, loop, step, lim);
-                while (!(t > tend) && loop < LOOP_CAP && t <= tsafe) {
-                    t = a_(t, step);
-                    ++loop;
+                while (t <= lim && loop < LOOP_CAP) {
+                    jump_empty_run(t, loop, step, lim);
+                    if (t <= lim && loop < LOOP_CAP) {
+                        t = a_(t, step);
+                        ++loop;
+                    }
                 }
                 finished = t > tend;
                 continue;
@@ -534,16 +558,18 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
         }
     }
     if (P.counters) {
-        unsigned long long a = cnt.samples, b = cnt.fetched, c = cnt.shaded;
+        unsigned long long a = cnt.samples, b = cnt.fetched, c = cnt.shaded, d = cnt.runs;
         for (int o = 16; o > 0; o >>= 1) {
             a += __shfl_xor_sync(FULL, a, o);
             b += __shfl_xor_sync(FULL, b, o);
             c += __shfl_xor_sync(FULL, c, o);
+            d += __shfl_xor_sync(FULL, d, o);
         }
         if (lane == 0) {
             atomicAdd(P.counters + 0, a);
             atomicAdd(P.counters + 1, b);
             atomicAdd(P.counters + 2, c);
+            atomicAdd(P.counters + 3, d);
         }
     }
 }

@@ -29,7 +29,7 @@ namespace {
 constexpr size_t COUNTER_BYTES = 256;                        // 16 x u64 counters, padded
 constexpr size_t TF_BYTES = (size_t)4096 * sizeof(float4);    // widest TF table
 constexpr size_t OCC_OFFSET = COUNTER_BYTES + TF_BYTES;
-constexpr size_t SCRATCH_BYTES = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS;
+constexpr size_t SCRATCH_BYTES = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS / 8;  // one bit per cell
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
@@ -122,7 +122,7 @@ extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf
     P.out = d_out;
     P.out_format = out_format;
     if (p->empty_space_skipping) {
-        uint8_t* occ = scratch + OCC_OFFSET;
+        uint32_t* occ = reinterpret_cast<uint32_t*>(scratch + OCC_OFFSET);
         if ((e = vrc::launch_occupancy(cmin, cmax, ncells, tf->d_prefix, tf->width, vol->desc.rwm_scale,
                                        vol->desc.rwm_offset, tf->lo, tf->hi, occ, s)) != cudaSuccess)
             return cuda_status(e);

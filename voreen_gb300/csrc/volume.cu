@@ -116,19 +116,27 @@ __device__ __forceinline__ int tf_index(float x, int w) {
     return i < 0 ? 0 : (i > w - 1 ? w - 1 : i);
 }
 
-// occ[b] = 1 if any TF entry with index in [idx(min) - 1, idx(max) + 1] has
-// alpha > 0. alpha_prefix[i] = number of entries < i with alpha > 0.
+// Bit c of the map is set if any TF entry with index in
+// [idx(min_c) - 1, idx(max_c) + 1] has alpha > 0 (alpha_prefix[i] = number of
+// entries below i with alpha > 0). One thread per 32-cell word.
 __global__ void occupancy_kernel(const float* bmin, const float* bmax, long long n, const int* prefix, int w,
-                                 float rs, float ro, float lo, float hi, uint8_t* occ) {
-    for (long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x; b < n;
-         b += (long long)gridDim.x * blockDim.x) {
-        const float r0 = __fadd_rn(__fmul_rn(bmin[b], rs), ro);
-        const float r1 = __fadd_rn(__fmul_rn(bmax[b], rs), ro);
-        int i0 = tf_index(rw_to_tf(fminf(r0, r1), lo, hi), w);
-        int i1 = tf_index(rw_to_tf(fmaxf(r0, r1), lo, hi), w);
-        i0 = max(i0 - 1, 0);
-        i1 = min(i1 + 1, w - 1);
-        occ[b] = (prefix[i1 + 1] - prefix[i0]) > 0 ? 1 : 0;
+                                 float rs, float ro, float lo, float hi, uint32_t* occ) {
+    const long long nwords = (n + 31) / 32;
+    for (long long wd = blockIdx.x * (long long)blockDim.x + threadIdx.x; wd < nwords;
+         wd += (long long)gridDim.x * blockDim.x) {
+        uint32_t bits = 0;
+        for (int k = 0; k < 32; ++k) {
+            const long long b = wd * 32 + k;
+            if (b >= n) break;
+            const float r0 = __fadd_rn(__fmul_rn(bmin[b], rs), ro);
+            const float r1 = __fadd_rn(__fmul_rn(bmax[b], rs), ro);
+            int i0 = tf_index(rw_to_tf(fminf(r0, r1), lo, hi), w);
+            int i1 = tf_index(rw_to_tf(fmaxf(r0, r1), lo, hi), w);
+            i0 = max(i0 - 1, 0);
+            i1 = min(i1 + 1, w - 1);
+            if (prefix[i1 + 1] - prefix[i0] > 0) bits |= 1u << k;
+        }
+        occ[wd] = bits;
     }
 }
 
@@ -199,11 +207,11 @@ cudaError_t launch_cell_minmax(const void* linear, int dtype, const int d[3], in
     return cudaGetLastError();
 }
 
-cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nbricks, const int* alpha_prefix,
+cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long ncells, const int* alpha_prefix,
                              int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
-                             uint8_t* occ, cudaStream_t s) {
-    occupancy_kernel<<<grid_for(nbricks, 256), 256, 0, s>>>(bmin, bmax, nbricks, alpha_prefix, tf_width, rwm_scale,
-                                                            rwm_offset, tf_lo, tf_hi, occ);
+                             uint32_t* occ, cudaStream_t s) {
+    occupancy_kernel<<<grid_for((ncells + 31) / 32, 128), 128, 0, s>>>(bmin, bmax, ncells, alpha_prefix, tf_width,
+                                                                       rwm_scale, rwm_offset, tf_lo, tf_hi, occ);
     return cudaGetLastError();
 }
 

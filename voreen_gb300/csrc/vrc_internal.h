@@ -38,10 +38,13 @@ struct BrickLayout {
 // Parameters of one march launch (passed by value).
 struct MarchParams {
     const void* bricks;
-    const uint8_t* occupancy;   // one byte per skip cell; nullptr = no skipping
+    const uint32_t* occupancy;  // one bit per skip cell (cell index order); nullptr = no skipping
     int cshift;                 // log2(skip cell edge)
     int nc[3];                  // skip cell grid
     float skip_margin;          // voxels kept clear of a cell face when skipping by t range
+    const uint32_t* occ_coarse; // optional coarser skip level (one bit per brick); nullptr = single level
+    int cshift_coarse;
+    int ncc[3];
     const float4* tf_table;     // (r, g, b, alpha') per TF entry
     int tf_width;
     BrickLayout L;
@@ -86,9 +89,12 @@ cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout
 // plus one voxel on the high side (clamped), from the linear volume.
 cudaError_t launch_cell_minmax(const void* linear, int dtype, const int dims[3], int C, float* cmin, float* cmax,
                                cudaStream_t s);
-cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nbricks, const int* alpha_prefix,
+// Writes ceil(ncells / 32) words: bit (c & 31) of word (c >> 5) is set when
+// cell c may hold a sample with TF alpha > 0.
+cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long ncells, const int* alpha_prefix,
                              int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
-                             uint8_t* occ, cudaStream_t s);
+                             uint32_t* occ, cudaStream_t s);
+inline size_t occupancy_bytes(long long ncells) { return (size_t)((ncells + 31) / 32) * 4; }
 
 }  // namespace vrc
 
@@ -104,8 +110,10 @@ struct vrc_context {
     size_t ee_bytes = 0;
     void* d_out = nullptr;
     size_t out_bytes = 0;
-    uint8_t* d_occ = nullptr;
+    uint32_t* d_occ = nullptr;
     size_t occ_bytes = 0;
+    uint32_t* d_occ_coarse = nullptr;
+    size_t occ_coarse_bytes = 0;
     int* d_prefix = nullptr;
     size_t prefix_bytes = 0;
     unsigned long long* d_counters = nullptr;  // 4 counters + status + tile counter

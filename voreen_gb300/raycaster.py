@@ -1,0 +1,185 @@
+"""Processor-shaped host interface mirroring Voreen's CPURaycaster /
+SingleVolumeRaycaster surface over the C ABI.
+
+Port names, property names, defaults and error behaviour follow the
+reference so tests read like its processor code:
+  ports       volumehandle.volumehandle, image.entrypoints, image.exitpoints,
+              image.output                       (volumeraycaster.cpp:44-47)
+  properties  samplingRate (2.0, 0.01..20), isoValue (0.5), compositing
+              (dvr/mip/iso), shading (none/phong), gradient
+              (central-differences), classification (transfer-function),
+              transferFunction (keys + domain + gamma + thresholds),
+              lightPosition, lightAmbient, lightDiffuse, lightSpecular,
+              materialShininess, applyLightAttenuation, lightAttenuation,
+              camera                              (volumeraycaster.cpp:42-157,
+                                                   volumerenderer.cpp:41-53)
+  process()   fits the TF width to the volume's bit depth and, on first use,
+              its domain to the volume's real-world min/max
+              (transfuncpropertybase.cpp:134-174,
+              transfunc1dkeysproperty.cpp:94-140), uploads the volume when the
+              inport changes, renders into image.output. On a failure it logs
+              an error and returns without output, as CPURaycaster::process does
+              (cpuraycaster.cpp:125-146); `lastError` keeps the message.
+"""
+from __future__ import annotations
+
+import logging
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import (DVR, EE_ANALYTIC, EE_BUFFERS, ISO, MIP, OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, Context,
+               TransferFunction, Volume, VrcError, default_params, make_camera, render)
+
+log = logging.getLogger("voreen.CudaRaycaster")
+
+COMPOSITING = {"dvr": DVR, "mip": MIP, "iso": ISO}
+SHADING = {"none": SHADE_NONE, "phong": SHADE_PHONG}
+
+
+@dataclass
+class VolumeData:
+    """What a VolumePort carries: voxels (Z, Y, X) plus the metadata the
+    march uses (spacing, offset, real-world mapping)."""
+    voxels: np.ndarray
+    spacing: tuple = (1.0, 1.0, 1.0)
+    offset: tuple = (0.0, 0.0, 0.0)
+    rwm: tuple = (1.0, 0.0)
+
+
+class Port:
+    def __init__(self, name: str):
+        self.name = name
+        self.data = None
+
+    def setData(self, d):
+        self.data = d
+
+    def getData(self):
+        return self.data
+
+    def hasData(self) -> bool:
+        return self.data is not None
+
+    def isConnected(self) -> bool:
+        return self.data is not None
+
+
+@dataclass
+class TransFunc1DKeys:
+    keys: list = field(default_factory=lambda: [(0.0, (0, 0, 0, 0)), (1.0, (255, 255, 255, 255))])
+    domain: tuple = (0.0, 1.0)
+    gamma: float = 1.0
+    threshold: tuple = (0.0, 1.0)
+    width: int = 256
+    domain_fitted: bool = False
+
+
+class CudaRaycaster:
+    className = "CudaRaycaster"
+    category = "Raycasting"
+
+    def __init__(self, device: int = 0):
+        self.volumeInport = Port("volumehandle.volumehandle")
+        self.entryPort = Port("image.entrypoints")
+        self.exitPort = Port("image.exitpoints")
+        self.outport = Port("image.output")
+        self.samplingRate = 2.0
+        self.isoValue = 0.5
+        self.compositing = "dvr"
+        self.shading = "none"
+        self.gradient = "central-differences"
+        self.classification = "transfer-function"
+        self.transferFunction = TransFunc1DKeys()
+        self.lightPosition = (2.3, 1.5, 1.5, 1.0)
+        self.lightAmbient = (0.4, 0.4, 0.4, 1.0)
+        self.lightDiffuse = (0.8, 0.8, 0.8, 1.0)
+        self.lightSpecular = (0.6, 0.6, 0.6, 1.0)
+        self.materialShininess = 60.0
+        self.applyLightAttenuation = False
+        self.lightAttenuation = (1.0, 0.0, 0.0)
+        self.camera = make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0))
+        self.lastError = ""
+        self._device = device
+        self._ctx = None
+        self._vol = None
+        self._vol_src = None
+
+    # Processor lifecycle ---------------------------------------------------
+    def initialize(self):
+        self._ctx = Context(self._device)
+
+    def deinitialize(self):
+        if self._vol is not None:
+            self._vol.close()
+        self._vol = None
+        if self._ctx is not None:
+            self._ctx.close()
+        self._ctx = None
+
+    def isReady(self) -> bool:
+        """volume + entry/exit ports, as CPURaycaster::isReady (cpuraycaster.cpp:82-84)."""
+        return self.volumeInport.hasData() and self.entryPort.isConnected() and self.exitPort.isConnected()
+
+    def _error(self, msg: str):
+        self.lastError = msg
+        log.error(msg)
+
+    def _fit_tf(self, vol: Volume):
+        tf = self.transferFunction
+        tf.width = TransferFunction.table_width(vol.dtype)
+        if not tf.domain_fitted and tf.domain == (0.0, 1.0):
+            lo, hi = vol.minmax()
+            s, o = vol.desc.rwm_scale, vol.desc.rwm_offset
+            tf.domain = (lo * s + o, hi * s + o)
+            tf.domain_fitted = True
+
+    def process(self, analytic_entry_exit: bool = False):
+        if self._ctx is None:
+            self.initialize()
+        if not (self.volumeInport.hasData() and (analytic_entry_exit or self.isReady())):
+            self._error("not ready: volume and entry/exit points are required")
+            return
+        if self.compositing not in COMPOSITING or self.shading not in SHADING:
+            self._error(f"unsupported compositing/shading: {self.compositing}/{self.shading}")
+            return
+        if not (0.01 <= self.samplingRate <= 20.0):
+            self._error(f"samplingRate {self.samplingRate} outside [0.01, 20]")
+            return
+        vd: VolumeData = self.volumeInport.getData()
+        try:
+            if self._vol is None or self._vol_src is not vd:
+                if self._vol is not None:
+                    self._vol.close()
+                self._vol = Volume(self._ctx, vd.voxels, vd.spacing, vd.offset, vd.rwm)
+                self._vol_src = vd
+            self._fit_tf(self._vol)
+            t = self.transferFunction
+            rgba = TransferFunction.bake(t.keys, t.width, t.gamma, t.threshold)
+            tf = TransferFunction(self._ctx, rgba, t.domain)
+            if analytic_entry_exit:
+                H, W = self.outport.getData().shape[:2] if self.outport.hasData() else (512, 512)
+                entry = exit_pts = None
+            else:
+                entry, exit_pts = self.entryPort.getData(), self.exitPort.getData()
+                H, W = entry.shape[:2]
+            p = default_params(W, H)
+            p.sampling_rate = self.samplingRate
+            p.compositing = COMPOSITING[self.compositing]
+            p.shading = SHADING[self.shading]
+            p.iso_value = self.isoValue
+            p.light_position[:] = list(self.lightPosition)
+            p.light_ambient[:] = list(self.lightAmbient)[:3]
+            p.light_diffuse[:] = list(self.lightDiffuse)[:3]
+            p.light_specular[:] = list(self.lightSpecular)[:3]
+            p.material_shininess = self.materialShininess
+            p.apply_attenuation = 1 if self.applyLightAttenuation else 0
+            p.light_attenuation[:] = list(self.lightAttenuation)
+            p.camera = self.camera
+            p.entry_exit_mode = EE_ANALYTIC if analytic_entry_exit else EE_BUFFERS
+            img, stats = render(self._ctx, self._vol, tf, p, entry, exit_pts, OUT_RGBA32F)
+            tf.close()
+            self.outport.setData(img)
+            self.lastStats = stats
+        except VrcError as e:
+            self._error(str(e))
