@@ -242,6 +242,7 @@ def main():
     # per-frame stats (sample counts, kernel time) from untimed frames
     _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
     samples, shaded = st.samples, st.samples_shaded
+    launches_per_frame = st.kernel_launches
     kernel_ms = []
     for _ in range(3):
         _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
@@ -309,7 +310,7 @@ def main():
                          "note": "algorithmic bytes = 16 B/sample + 48 B/shaded sample + 4 B/pixel"},
             "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "frames/s", "h2d_bytes_per_step": 2 * npix * 16,
                     "d2h_bytes_per_step": npix * 4},
-            "gpu_launches": 2 * args.steps,
+            "gpu_launches": launches_per_frame * args.steps,
             "clocks": clocks,
             "volume_upload_bytes": int(w.voxels.nbytes), "volume_device_bytes": vol.device_bytes}
 

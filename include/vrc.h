@@ -169,6 +169,7 @@ typedef struct {
     float kernel_ms;         /* device time of the march kernel on the context stream */
     float total_ms;          /* device time from first copy-in to last copy-out */
     int device_status;       /* 0, or an internal error code from the kernel */
+    int kernel_launches;     /* kernels this frame launched (occupancy levels + march) */
 } vrc_render_stats;
 
 /* Render one frame.

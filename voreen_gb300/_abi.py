@@ -52,7 +52,8 @@ class RenderParams(C.Structure):
 class RenderStats(C.Structure):
     _fields_ = [("samples", C.c_double), ("samples_fetched", C.c_double), ("samples_shaded", C.c_double),
                 ("skip_runs", C.c_double),
-                ("kernel_ms", C.c_float), ("total_ms", C.c_float), ("device_status", C.c_int)]
+                ("kernel_ms", C.c_float), ("total_ms", C.c_float), ("device_status", C.c_int),
+                ("kernel_launches", C.c_int)]
 
 
 # name -> (restype, argtypes); every symbol declared in include/*.h

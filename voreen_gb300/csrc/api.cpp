@@ -712,6 +712,7 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
         stats->samples_shaded = double(h[2]);
         stats->skip_runs = double(h[3]);
         stats->device_status = int(h[4] & 0xffffffffu);
+        stats->kernel_launches = 1 + (P.occupancy ? 1 : 0) + (P.occ_coarse ? 1 : 0);
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->kernel_ms, ctx->ev[1], ctx->ev[2]));
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->total_ms, ctx->ev[0], ctx->ev[3]));
         if (stats->device_status != 0) return fail(ctx, VRC_ERR_DEVICE, "vrc_render: kernel reported an error status");
