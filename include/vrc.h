@@ -155,7 +155,8 @@ typedef struct {
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
     int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (8), else 8, 16 or the brick size */
-    int reserved[7];
+    int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
+    int reserved[6];
 } vrc_render_params;
 
 /* Fills `p` with the reference's property defaults for a W x H image. */
@@ -182,6 +183,42 @@ typedef struct {
 vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                       const float* entry, const float* exit_pts, int ee_on_device, void* out, int out_format,
                       int out_on_device, vrc_render_stats* stats);
+
+/* ---- batched persistent render ----------------------------------------------
+ * No counterpart in the reference (it renders one request per processor
+ * call). Many requests -- uneven volumes, dtypes and image sizes -- march in
+ * ONE persistent kernel launch; the whole per-launch sequence (state reset,
+ * every request's empty-space maps, the march) is captured once as a CUDA
+ * graph on the context's stream and replayed by vrc_batch_launch. All items
+ * share compositing and shading and use analytic entry/exit (the camera in
+ * their params); each writes its own device image. */
+typedef struct {
+    const vrc_volume* volume;
+    const vrc_tf* tf;
+    vrc_render_params params;
+    void* out;          /* device image, params.width x params.height pixels */
+    int out_format;     /* vrc_out_format */
+} vrc_batch_item;
+
+typedef struct vrc_batch vrc_batch;
+
+typedef struct {
+    double samples;          /* loop iterations of all rays of all requests */
+    float total_ms;          /* device time of the last launch (first kernel start to last tile) */
+    float latency_p50_ms;    /* per-request completion time after the launch start: median */
+    float latency_p99_ms;    /* ... 99th percentile */
+    float latency_max_ms;
+} vrc_batch_stats;
+
+/* Builds device descriptors and TF tables (allocating), orders requests
+ * longest first and captures the launch sequence. Items are copied. */
+vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n, vrc_batch** out);
+/* Enqueues one replay of the captured graph on the context's stream. */
+vrc_status vrc_batch_launch(vrc_batch* b);
+/* Synchronizes the context stream, then reports the last launch:
+ * latency_ms (nullable, n floats in item order) and totals. */
+vrc_status vrc_batch_stats_get(vrc_batch* b, float* latency_ms, vrc_batch_stats* st);
+vrc_status vrc_batch_destroy(vrc_batch* b);
 
 /* ---- render without allocating ---------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call

@@ -269,6 +269,46 @@ def render_noalloc(vol: Volume, tf: TransferFunction, params: RenderParams, entr
     _check(st, None, "vrc_render_noalloc")
 
 
+class Batch:
+    """Many requests in one persistent launch replayed from a captured CUDA
+    graph (vrc_batch_*). items: [(Volume, TransferFunction, RenderParams,
+    out CUDA tensor, out_format)]; params must use analytic entry/exit and
+    share compositing and shading."""
+
+    def __init__(self, ctx: Context, items):
+        self.ctx = ctx
+        self.items = list(items)
+        arr = (_abi.BatchItem * len(self.items))()
+        for i, (vol, tf, p, out, fmt) in enumerate(self.items):
+            arr[i].volume = vol.handle.value
+            arr[i].tf = tf.handle.value
+            arr[i].params = p
+            arr[i].out = out.data_ptr()
+            arr[i].out_format = fmt
+        self.handle = C.c_void_p()
+        _check(lib().vrc_batch_create(ctx.handle, arr, len(self.items), C.byref(self.handle)), ctx, "vrc_batch_create")
+
+    def launch(self):
+        _check(lib().vrc_batch_launch(self.handle), self.ctx, "vrc_batch_launch")
+
+    def stats(self):
+        lat = np.zeros(len(self.items), np.float32)
+        st = _abi.BatchStats()
+        _check(lib().vrc_batch_stats_get(self.handle, _ptr(lat), C.byref(st)), self.ctx, "vrc_batch_stats_get")
+        return st, lat
+
+    def close(self):
+        if self.handle:
+            lib().vrc_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def entry_exit(ctx: Context, vol: Volume, params: RenderParams):
     """Analytic entry/exit points for params.camera (host arrays)."""
     H, W = params.height, params.width

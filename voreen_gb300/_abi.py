@@ -46,7 +46,17 @@ class RenderParams(C.Structure):
                 ("material_shininess", C.c_float), ("apply_attenuation", C.c_int),
                 ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
                 ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("skip_cell_size", C.c_int),
-                ("reserved", C.c_int * 7)]
+                ("tile_width", C.c_int), ("reserved", C.c_int * 6)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("volume", C.c_void_p), ("tf", C.c_void_p), ("params", RenderParams), ("out", C.c_void_p),
+                ("out_format", C.c_int)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("samples", C.c_double), ("total_ms", C.c_float), ("latency_p50_ms", C.c_float),
+                ("latency_p99_ms", C.c_float), ("latency_max_ms", C.c_float)]
 
 
 class RenderStats(C.Structure):
@@ -80,6 +90,10 @@ SIGNATURES = {
     "vrc_render_params_default": (None, [P(RenderParams), C.c_int, C.c_int]),
     "vrc_render": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, C.c_int, VP, C.c_int, C.c_int, P(RenderStats)]),
     "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
+    "vrc_batch_create": (C.c_int, [VP, P(BatchItem), C.c_int, P(VP)]),
+    "vrc_batch_launch": (C.c_int, [VP]),
+    "vrc_batch_stats_get": (C.c_int, [VP, VP, P(BatchStats)]),
+    "vrc_batch_destroy": (C.c_int, [VP]),
     "vrc_render_noalloc": (C.c_int, [VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
 }

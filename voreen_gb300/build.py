@@ -29,6 +29,7 @@ SOURCES = [
     ("volume.cu", []),
     ("march.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
+    ("batch.cpp", []),
 ]
 
 

@@ -503,6 +503,10 @@ void vrc_render_params_default(vrc_render_params* p, int W, int H) {
 
 namespace {
 
+}  // namespace
+
+namespace vrc {
+
 // Float4 TF table for a render: (r/255, g/255, b/255, alpha') with alpha' the
 // opacity-corrected alpha for DVR (cpuraycaster.cpp:291) and the plain alpha
 // for MIP / ISO.
@@ -523,7 +527,8 @@ vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, f
         h[i] = make_float4(float(c[0]) / 255.f, float(c[1]) / 255.f, float(c[2]) / 255.f, a);
     }
     float4* d = nullptr;
-    VRC_CUDA(ctx, cudaMalloc(&d, tf->width * sizeof(float4)));
+    cudaError_t e0 = cudaMalloc(&d, tf->width * sizeof(float4));
+    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "tf table allocation");
     cudaError_t e = cudaMemcpy(d, h.data(), tf->width * sizeof(float4), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(d);
@@ -533,10 +538,6 @@ vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, f
     *out = d;
     return VRC_OK;
 }
-
-}  // namespace
-
-namespace vrc {
 
 vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P) {
     std::memset(&P, 0, sizeof(P));
@@ -573,8 +574,10 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
     P.H = p->height;
     P.ee_mode = p->entry_exit_mode;
     P.quantize = p->quantize_entry_exit;
-    P.tiles_x = (p->width + 7) / 8;
-    P.tiles_y = (p->height + 3) / 4;
+    const int tw = p->tile_width == 0 ? 8 : p->tile_width;
+    P.tile_wshift = ilog2(tw);
+    P.tiles_x = (p->width + tw - 1) / tw;
+    P.tiles_y = (p->height + (32 / tw) - 1) / (32 / tw);
     if (p->entry_exit_mode == VRC_EE_ANALYTIC) {
         double inv[16];
         if (vrc_camera_matrices(&p->camera, &d, p->width, p->height, nullptr, nullptr, inv) != VRC_OK)
@@ -596,6 +599,9 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
     if (p->entry_exit_mode != VRC_EE_BUFFERS && p->entry_exit_mode != VRC_EE_ANALYTIC)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown entry/exit mode");
+    if (p->tile_width != 0 && p->tile_width != 1 && p->tile_width != 2 && p->tile_width != 4 && p->tile_width != 8 &&
+        p->tile_width != 16 && p->tile_width != 32)
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: tile_width must be 0, 1, 2, 4, 8, 16 or 32");
     if (p->skip_cell_size != 0 && p->skip_cell_size != 8 && p->skip_cell_size != 16 && p->skip_cell_size != 32 &&
         p->skip_cell_size != 64)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 8, 16, 32 or 64");
@@ -606,6 +612,7 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
 
 using vrc::check_params;
 using vrc::fill_params;
+using vrc::tf_table;
 
 
 extern "C" {

@@ -1,0 +1,261 @@
+// Batched persistent render (host side): descriptors, launch order, graph
+// capture and per-request latency statistics for vrc_batch_* (include/vrc.h).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "vrc_internal.h"
+
+struct vrc_batch {
+    vrc_context* ctx = nullptr;
+    int n = 0;
+    int compositing = 0, shading = 0;
+    std::vector<int> order;                 // launch position -> item index
+    vrc::BatchReq* d_reqs = nullptr;
+    unsigned* d_prefix = nullptr;
+    unsigned long long* d_state = nullptr;  // [tile counter, start ns, samples, end ns per launch position]
+    std::vector<uint32_t*> occ;             // per request: fine and coarse bitmaps
+    unsigned total_tiles = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+namespace {
+
+vrc_status bfail(vrc_context* ctx, vrc_status s, const std::string& m) {
+    if (ctx) ctx->last_error = m;
+    return s;
+}
+
+void release(vrc_batch* b) {
+    if (!b) return;
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    cudaFree(b->d_reqs);
+    cudaFree(b->d_prefix);
+    cudaFree(b->d_state);
+    for (auto* p : b->occ) cudaFree(p);
+    delete b;
+}
+
+// Select the empty-space level for a request (as vrc_render does).
+void pick_level(const vrc_volume* vol, int want, const float** mn, const float** mx, int* C, int nc[3]) {
+    *mn = vol->d_bmin;
+    *mx = vol->d_bmax;
+    *C = vol->L.B;
+    for (int i = 0; i < 3; ++i) nc[i] = vol->L.nb[i];
+    for (const auto& lv : vol->levels)
+        if (lv.C == want && lv.d_min) {
+            *mn = lv.d_min;
+            *mx = lv.d_max;
+            *C = lv.C;
+            for (int i = 0; i < 3; ++i) nc[i] = lv.nc[i];
+        }
+}
+
+}  // namespace
+
+extern "C" {
+
+vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n, vrc_batch** out) {
+    if (!ctx || !items || !out || n < 1) return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: bad arguments");
+    *out = nullptr;
+    for (int i = 0; i < n; ++i) {
+        const vrc_batch_item& it = items[i];
+        if (!it.volume || !it.tf || !it.out || it.volume->ctx != ctx || it.tf->ctx != ctx)
+            return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: item " + std::to_string(i) + " is incomplete");
+        vrc_status st = vrc::check_params(ctx, &it.params);
+        if (st != VRC_OK) return st;
+        if (it.params.entry_exit_mode != VRC_EE_ANALYTIC)
+            return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: batched requests use analytic entry/exit");
+        if (it.params.compositing != items[0].params.compositing || it.params.shading != items[0].params.shading)
+            return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: all requests must share compositing and shading");
+        if (it.out_format < VRC_OUT_RGBA8 || it.out_format > VRC_OUT_RGBA16)
+            return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: unknown output format");
+    }
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e != cudaSuccess) return bfail(ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
+    vrc_batch* b = new (std::nothrow) vrc_batch();
+    if (!b) return VRC_ERR_OUT_OF_MEMORY;
+    b->ctx = ctx;
+    b->n = n;
+    b->compositing = items[0].params.compositing;
+    b->shading = items[0].params.shading;
+
+    std::vector<vrc::BatchReq> reqs(n);
+    std::vector<double> cost(n);
+    struct Occ {
+        const float *mn, *mx;
+        long long cells;
+        uint32_t* map;
+        const vrc_tf* tf;
+        const vrc_volume* vol;
+    };
+    std::vector<Occ> occ_jobs;
+    for (int i = 0; i < n; ++i) {
+        const vrc_batch_item& it = items[i];
+        vrc::BatchReq& R = reqs[i];
+        std::memset(&R, 0, sizeof(R));
+        vrc_status st = vrc::fill_params(ctx, it.volume, &it.params, R.P);
+        if (st != VRC_OK) {
+            release(b);
+            return st;
+        }
+        R.dtype = it.volume->desc.dtype;
+        float4* table = nullptr;
+        if ((st = vrc::tf_table(ctx, const_cast<vrc_tf*>(it.tf), it.params.compositing == VRC_DVR, R.P.step * 200.f,
+                                &table)) != VRC_OK) {
+            release(b);
+            return st;
+        }
+        R.P.tf_table = table;
+        R.P.tf_width = it.tf->width;
+        R.P.tf_lo = it.tf->lo;
+        R.P.tf_hi = it.tf->hi;
+        R.P.out = it.out;
+        R.P.out_format = it.out_format;
+        if (it.params.empty_space_skipping) {
+            const float *mn, *mx;
+            int C, nc[3];
+            pick_level(it.volume, it.params.skip_cell_size == 0 ? 8 : it.params.skip_cell_size, &mn, &mx, &C, nc);
+            const long long cells = (long long)nc[0] * nc[1] * nc[2];
+            uint32_t* map = nullptr;
+            if ((e = cudaMalloc((void**)&map, vrc::occupancy_bytes(cells))) != cudaSuccess) {
+                release(b);
+                return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: occupancy allocation");
+            }
+            b->occ.push_back(map);
+            occ_jobs.push_back({mn, mx, cells, map, it.tf, it.volume});
+            R.P.occupancy = map;
+            int sh = 0;
+            while ((1 << sh) < C) ++sh;
+            R.P.cshift = sh;
+            for (int k = 0; k < 3; ++k) R.P.nc[k] = nc[k];
+            const int maxdim = std::max(it.volume->desc.dims[0], std::max(it.volume->desc.dims[1], it.volume->desc.dims[2]));
+            R.P.skip_margin = 0.01f + 2e-5f * float(maxdim);
+            if (C < it.volume->L.B) {
+                const long long nb = it.volume->L.nbricks();
+                uint32_t* cm = nullptr;
+                if ((e = cudaMalloc((void**)&cm, vrc::occupancy_bytes(nb))) != cudaSuccess) {
+                    release(b);
+                    return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: occupancy allocation");
+                }
+                b->occ.push_back(cm);
+                occ_jobs.push_back({it.volume->d_bmin, it.volume->d_bmax, nb, cm, it.tf, it.volume});
+                R.P.occ_coarse = cm;
+                R.P.cshift_coarse = it.volume->L.shift;
+                for (int k = 0; k < 3; ++k) R.P.ncc[k] = it.volume->L.nb[k];
+            }
+        }
+        const int maxdim = std::max(it.volume->desc.dims[0], std::max(it.volume->desc.dims[1], it.volume->desc.dims[2]));
+        cost[i] = double(it.params.width) * it.params.height * maxdim * it.params.sampling_rate;
+    }
+    // longest requests first, so the tail of the launch holds short tiles
+    b->order.resize(n);
+    std::iota(b->order.begin(), b->order.end(), 0);
+    std::stable_sort(b->order.begin(), b->order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    std::vector<vrc::BatchReq> ordered(n);
+    std::vector<unsigned> prefix(n + 1, 0);
+    for (int k = 0; k < n; ++k) {
+        ordered[k] = reqs[b->order[k]];
+        const unsigned long long t = (unsigned long long)ordered[k].P.tiles_x * ordered[k].P.tiles_y;
+        if (prefix[k] + t > 0xffffffffULL) {
+            release(b);
+            return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: too many ray tiles in one batch");
+        }
+        prefix[k + 1] = prefix[k] + (unsigned)t;
+    }
+    b->total_tiles = prefix[n];
+    if ((e = cudaMalloc((void**)&b->d_reqs, n * sizeof(vrc::BatchReq))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_prefix, (n + 1) * sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc((void**)&b->d_state, (3 + n) * sizeof(unsigned long long))) != cudaSuccess) {
+        release(b);
+        return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: descriptor allocation");
+    }
+    if ((e = cudaMemcpy(b->d_reqs, ordered.data(), n * sizeof(vrc::BatchReq), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(b->d_prefix, prefix.data(), (n + 1) * sizeof(unsigned), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        release(b);
+        return bfail(ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
+    }
+    // capture: state reset + start stamp, empty-space maps, one persistent march
+    cudaStream_t s = ctx->stream;
+    if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
+        release(b);
+        return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture: ") + cudaGetErrorString(e));
+    }
+    cudaError_t ce = vrc::launch_batch_begin(b->d_state, n, s);
+    for (const Occ& j : occ_jobs)
+        if (ce == cudaSuccess)
+            ce = vrc::launch_occupancy(j.mn, j.mx, j.cells, j.tf->d_prefix, j.tf->width, j.vol->desc.rwm_scale,
+                                       j.vol->desc.rwm_offset, j.tf->lo, j.tf->hi, j.map, s);
+    if (ce == cudaSuccess)
+        ce = vrc::launch_march_batch(b->d_reqs, n, b->d_prefix, b->total_tiles, b->d_state, b->compositing,
+                                     b->shading, ctx->num_sms, s);
+    e = cudaStreamEndCapture(s, &b->graph);
+    if (ce != cudaSuccess || e != cudaSuccess) {
+        release(b);
+        return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture failed: ") +
+                                            cudaGetErrorString(ce != cudaSuccess ? ce : e));
+    }
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) {
+        release(b);
+        return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: instantiate: ") + cudaGetErrorString(e));
+    }
+    *out = b;
+    return VRC_OK;
+}
+
+vrc_status vrc_batch_launch(vrc_batch* b) {
+    if (!b) return VRC_ERR_INVALID_ARG;
+    cudaError_t e = cudaGraphLaunch(b->exec, b->ctx->stream);
+    if (e != cudaSuccess) return bfail(b->ctx, VRC_ERR_CUDA, std::string("vrc_batch_launch: ") + cudaGetErrorString(e));
+    return VRC_OK;
+}
+
+vrc_status vrc_batch_stats_get(vrc_batch* b, float* latency_ms, vrc_batch_stats* st) {
+    if (!b) return VRC_ERR_INVALID_ARG;
+    cudaError_t e = cudaStreamSynchronize(b->ctx->stream);
+    std::vector<unsigned long long> h(3 + b->n);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h.data(), b->d_state, h.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return bfail(b->ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
+    std::vector<float> lat(b->n);
+    float mx = 0.f;
+    for (int k = 0; k < b->n; ++k) {
+        const unsigned long long end = h[3 + k];
+        lat[k] = end > h[1] ? float(double(end - h[1]) * 1e-6) : 0.f;
+        mx = std::max(mx, lat[k]);
+        if (latency_ms) latency_ms[b->order[k]] = lat[k];
+    }
+    if (st) {
+        std::vector<float> sorted = lat;
+        std::sort(sorted.begin(), sorted.end());
+        auto pct = [&](double q) {
+            const double pos = q * (sorted.size() - 1);
+            const size_t i = (size_t)pos;
+            const double fr = pos - i;
+            return float(i + 1 < sorted.size() ? sorted[i] * (1 - fr) + sorted[i + 1] * fr : sorted[i]);
+        };
+        st->samples = double(h[2]);
+        st->total_ms = mx;
+        st->latency_p50_ms = pct(0.5);
+        st->latency_p99_ms = pct(0.99);
+        st->latency_max_ms = mx;
+    }
+    return VRC_OK;
+}
+
+vrc_status vrc_batch_destroy(vrc_batch* b) {
+    if (!b) return VRC_ERR_INVALID_ARG;
+    cudaSetDevice(b->ctx->device);
+    cudaStreamSynchronize(b->ctx->stream);
+    release(b);
+    return VRC_OK;
+}
+
+}  // extern "C"

@@ -72,16 +72,33 @@ struct MarchParams {
     int* status;
     unsigned int* tile_counter;
     int tiles_x, tiles_y;
+    int tile_wshift;             // ray tile = (1 << tile_wshift) x (32 >> tile_wshift) pixels per warp
+};
+
+// One request of a batched launch.
+struct BatchReq {
+    MarchParams P;
+    int dtype;
+    int pad[3];
 };
 
 // Host helpers shared by the render entry points (api.cpp).
 vrc_status check_params(vrc_context* ctx, const vrc_render_params* p);
 vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P);
+// Device float4 TF table (r/255, g/255, b/255, alpha'), cached on the TF per
+// (opacity-corrected, correction exponent).
+vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float4** out);
 
 // Kernel launchers (march.cu / volume.cu). Return cudaError_t.
 cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                          cudaStream_t s);
 cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp, cudaStream_t s);
+// Batch: zero the per-launch state and stamp the start time, then one
+// persistent launch over every request's ray tiles (tile_prefix[r] = first
+// tile of request r in launch order; n + 1 entries).
+cudaError_t launch_batch_begin(unsigned long long* state, int nreq, cudaStream_t s);
+cudaError_t launch_march_batch(const BatchReq* reqs, int nreq, const unsigned* tile_prefix, unsigned total_tiles,
+                               unsigned long long* state, int compositing, int shading, int num_sms, cudaStream_t s);
 cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
                                 cudaStream_t s);

@@ -140,3 +140,40 @@ def config2(seed: int = 1, size=(512, 512, 512), image=(1920, 1080), compositing
     return Workload(f"CT-like {'shaded DVR' if compositing == DVR else 'MIP'} {size[0]}x{size[1]}x{size[2]} u16 "
                     f"{image[0]}x{image[1]}", vox, spacing, keys, 4096, domain, image[0], image[1], 2.0,
                     compositing, shading, pos, focus, near=near, far=far, light_pos=(*pos, 1.0))
+
+
+BATCH_DIMS = ((64, 64, 64), (128, 128, 128), (256, 256, 256), (384, 256, 200), (512, 512, 512))
+BATCH_IMAGES = ((256, 256), (512, 512), (1024, 1024), (1920, 1080), (2048, 2048))
+BATCH_DTYPES = (U8, U16, F32)
+
+
+def random_trapezoid_keys(rng: random.Random, n: int = 3):
+    """n trapezoids at random TF positions in [0.15, 0.95], kept apart."""
+    slots = sorted(rng.sample(range(n * 3), n))
+    centers = [0.15 + (0.8 * (sl + rng.uniform(0.3, 0.7))) / (n * 3) for sl in slots]
+    return tf_keys_trapezoids(centers, rng.randrange(1 << 30), alpha_range=(0.15, 0.7), top=(0.01, 0.03),
+                              ramp=(0.01, 0.03))
+
+
+def config3(seed: int = 1, n: int = 64, dims_set=BATCH_DIMS, images=BATCH_IMAGES, dtypes=BATCH_DTYPES):
+    """Batched requests: volume sizes from dims_set with mixed dtypes
+    (blobs or shells), image sizes from `images`, random orbit cameras and
+    random 256- or 4096-entry 3-trapezoid TFs, DVR + Phong. Volumes are
+    shared between requests of the same (size, dtype, content). Returns
+    (volumes: {key: (voxels, spacing)}, requests: [dict])."""
+    rng = random.Random(3000 + seed)
+    volumes, requests = {}, []
+    for i in range(n):
+        dims = rng.choice(dims_set)
+        dt = rng.choice(dtypes)
+        kind = rng.choice((BLOBS, SHELLS))
+        key = (dims, dt, kind)
+        if key not in volumes:
+            volumes[key] = (synth_volume(kind, dt, dims, 3000 + seed * 100 + len(volumes)), (1.0, 1.0, 1.0))
+        W, H = rng.choice(images)
+        pos, focus, near, far = orbit_camera(dims, (1.0, 1.0, 1.0), rng.uniform(0, 360), rng.uniform(-60, 60),
+                                             rng.uniform(1.1, 2.0))
+        requests.append({"volume": key, "width": W, "height": H, "camera": (pos, focus, near, far),
+                         "tf_width": rng.choice((256, 4096)), "tf_keys": random_trapezoid_keys(rng),
+                         "light": (*pos, 1.0)})
+    return volumes, requests
