@@ -208,6 +208,7 @@ typedef struct {
     float latency_p50_ms;    /* per-request completion time after the launch start: median */
     float latency_p99_ms;    /* ... 99th percentile */
     float latency_max_ms;
+    int kernels_per_launch;  /* kernel nodes in the captured graph */
 } vrc_batch_stats;
 
 /* Builds device descriptors and TF tables (allocating), orders requests

@@ -56,7 +56,8 @@ class BatchItem(C.Structure):
 
 class BatchStats(C.Structure):
     _fields_ = [("samples", C.c_double), ("total_ms", C.c_float), ("latency_p50_ms", C.c_float),
-                ("latency_p99_ms", C.c_float), ("latency_max_ms", C.c_float)]
+                ("latency_p99_ms", C.c_float), ("latency_max_ms", C.c_float),
+                ("kernels_per_launch", C.c_int)]
 
 
 class RenderStats(C.Structure):

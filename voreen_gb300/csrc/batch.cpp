@@ -21,6 +21,7 @@ struct vrc_batch {
     unsigned long long* d_state = nullptr;  // [tile counter, start ns, samples, end ns per launch position]
     std::vector<uint32_t*> occ;             // per request: fine and coarse bitmaps
     unsigned total_tiles = 0;
+    int kernels = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
 };
@@ -202,6 +203,7 @@ vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture failed: ") +
                                             cudaGetErrorString(ce != cudaSuccess ? ce : e));
     }
+    b->kernels = 2 + (int)occ_jobs.size();
     if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) {
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: instantiate: ") + cudaGetErrorString(e));
@@ -246,6 +248,7 @@ vrc_status vrc_batch_stats_get(vrc_batch* b, float* latency_ms, vrc_batch_stats*
         st->latency_p50_ms = pct(0.5);
         st->latency_p99_ms = pct(0.99);
         st->latency_max_ms = mx;
+        st->kernels_per_launch = b->kernels;
     }
     return VRC_OK;
 }
