@@ -161,6 +161,7 @@ def run_batch(args, warmup, ws, rank, local):
     """64 requests (volumes 64^3..512^3, u8/u16/f32, images 256^2..2048^2,
     DVR + Phong) in one persistent launch replayed from a CUDA graph; tile
     shape, brick size and skip cell per request class from the autotuner."""
+    import numpy as np
     import torch
 
     import voreen_gb300 as v
