@@ -184,6 +184,7 @@ def run_batch(args, warmup, ws, rank, local):
         p.camera = v.make_camera(pos, focus, near=near, far=far)
         p.light_position[:] = list(r["light"])
         p.shading = v.SHADE_PHONG
+        p.entry_exit_mode = v.EE_ANALYTIC
         best = tuner.tune(vox, sp, tf_rgba, (mn / norm, mx / norm), p, tune_bricks=r["volume"] not in brick_of)
         brick_of.setdefault(r["volume"], best["brick"])
         p.tile_width, p.skip_cell_size = best["tile_width"], min(best["skip_cell"], brick_of[r["volume"]])
