@@ -1,0 +1,62 @@
+/*
+ * vrc_nn -- kernels of the learned upsampler (no counterpart in the reference).
+ *
+ * The learned form renders a half-resolution, half-rate march and rebuilds
+ * the full-resolution frame with a 3-level BF16 U-Net (32/64/128 channels,
+ * 3x3 convolutions, FP32 accumulation on the tensor cores). These are its
+ * training and inference kernels; the network and its training loop are
+ * driven from the host (voreen_gb300/learned.py). All pointers are device
+ * pointers; tensors are NHWC; `stream` is a cudaStream_t. Return 0 on
+ * success, 1 for invalid arguments, 2 for a CUDA error, 4 for an unsupported
+ * channel count.
+ */
+#ifndef VRC_NN_H
+#define VRC_NN_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* out = conv3x3(in, w) + bias, optional ReLU. in BF16 [N][H][W][Cin]
+ * (Cin % 16 == 0), w BF16 [Cout][3][3][Cin], bias FP32 [Cout] (nullable),
+ * Cout in {16, 32, 64, 128}; out BF16 or FP32 (out_f32) [N][H][W][Cout]. */
+int vrc_nn_conv3x3_fwd(const void* in, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
+                       int relu, void* out, int out_f32, void* stream);
+/* dw[co][kh][kw][ci] += sum over pixels of dout * shifted in (FP32), and
+ * dbias[co] += sum of dout (nullable). */
+int vrc_nn_conv3x3_wgrad(const void* in, const void* dout, int N, int H, int W, int Cin, int Cout, float* dw,
+                         float* dbias, void* stream);
+/* wt[ci][kh][kw][co] = w[co][2-kh][2-kw][ci]: weights for the data gradient,
+ * which is vrc_nn_conv3x3_fwd(dout, wt). */
+int vrc_nn_flip_weights(const void* w, int Cout, int Cin, void* wt, void* stream);
+/* dy = 0 where y <= 0 (in place), BF16. */
+int vrc_nn_relu_bwd(const void* y, void* dy, long long n, void* stream);
+/* 2x2 average pool times `scale` (4: sum pool). */
+int vrc_nn_avgpool2(const void* in, int N, int H, int W, int C, float scale, void* out, void* stream);
+/* nearest 2x upsample times `scale` (0.25: backward of the average pool). */
+int vrc_nn_upsample2(const void* in, int N, int H, int W, int C, float scale, void* out, void* stream);
+/* channel concat out = [a | b] (split != 0: the reverse, out -> a, b). */
+int vrc_nn_concat(const void* a, int Ca, const void* b, int Cb, long long npix, void* out, int split, void* stream);
+/* a += b, BF16. */
+int vrc_nn_add(void* a, const void* b, long long n, void* stream);
+/* Head: 16 FP32 channels at H x W -> 2H x 2W x 4 by depth-to-space, plus the
+ * bilinear 2x upsample of the low-resolution RGBA `base` (FP32 NHWC). */
+int vrc_nn_head_fwd(const float* feat16, const float* base, int N, int H, int W, float* out, void* stream);
+int vrc_nn_head_bwd(const float* dout, int N, int H, int W, void* dfeat16, void* stream);
+/* Bilinear 2x upsample of an RGBA FP32 image (the method without the network). */
+int vrc_nn_bilinear_up2(const float* base, int N, int H, int W, float* out, void* stream);
+/* L1 + lambda * (1 - SSIM) over RGBA FP32 images ((2r+1)^2 box windows):
+ * writes dL/dx (mean normalisation) and adds [sum |x-y|, sum SSIM] to
+ * loss2. coef_scratch holds 3 floats per element. */
+int vrc_nn_loss(const float* x, const float* y, int N, int H, int W, int radius, float lambda, float* coef_scratch,
+                float* dx, float* loss2, void* stream);
+/* Adam step on FP32 master weights; refreshes the BF16 copy (nullable). */
+int vrc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long long n, float lr, float b1, float b2,
+                float eps, int step, void* stream);
+/* Network input from a low-resolution march: RGBA FP32 + aux FP32x2 (first-hit
+ * depth, gradient magnitude; nullable) -> BF16 NHWC with 16 channels. */
+int vrc_nn_pack_input(const float* rgba, const float* aux2, long long npix, void* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,131 @@
+"""Learned upsampler kernels against the FP64 numpy reference
+(oracle/unet_ref.py): 3x3 convolution forward / data gradient / weight
+gradient on the tensor cores, the L1 + SSIM loss gradient, the head, and the
+whole network's forward and parameter gradients."""
+import numpy as np
+import pytest
+
+from oracle import unet_ref as R
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def bf16(a):
+    """numpy float -> torch bf16 on the GPU and back to float64 (the values the kernels see)."""
+    t = torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(torch.bfloat16).cuda()
+    return t, t.float().cpu().numpy().astype(np.float64)
+
+
+def rel_err(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-30))
+
+
+@pytest.mark.parametrize("cin,cout,H,W", [(16, 16, 8, 16), (48, 32, 13, 21), (32, 64, 16, 40), (192, 128, 9, 17),
+                                          (96, 64, 6, 33)])
+def test_conv_forward(vrc_lib, cin, cout, H, W):
+    from voreen_gb300.learned import _call, _p, _stream
+    rng = np.random.default_rng(cin * 7 + cout)
+    x, x64 = bf16(rng.standard_normal((2, H, W, cin)))
+    w, w64 = bf16(rng.standard_normal((cout, 3, 3, cin)) / np.sqrt(9 * cin))
+    b = torch.from_numpy(rng.standard_normal(cout).astype(np.float32)).cuda()
+    ref = R.conv3x3(x64, w64, b.cpu().numpy().astype(np.float64))
+    y = torch.empty((2, H, W, cout), dtype=torch.float32, device="cuda")
+    _call("vrc_nn_conv3x3_fwd", _p(x), 2, H, W, cin, _p(w), _p(b), cout, 0, _p(y), 1, _stream())
+    torch.cuda.synchronize()
+    assert rel_err(y.cpu().numpy(), ref) < 1e-5
+    yb = torch.empty((2, H, W, cout), dtype=torch.bfloat16, device="cuda")
+    _call("vrc_nn_conv3x3_fwd", _p(x), 2, H, W, cin, _p(w), _p(b), cout, 1, _p(yb), 0, _stream())
+    torch.cuda.synchronize()
+    assert rel_err(yb.float().cpu().numpy(), np.maximum(ref, 0)) < 8e-3
+
+
+@pytest.mark.parametrize("cin,cout,H,W", [(16, 16, 8, 16), (32, 32, 13, 21), (96, 64, 16, 40), (64, 128, 9, 17)])
+def test_conv_weight_and_data_gradients(vrc_lib, cin, cout, H, W):
+    from voreen_gb300.learned import _call, _p, _stream
+    rng = np.random.default_rng(cin + cout * 3)
+    x, x64 = bf16(rng.standard_normal((2, H, W, cin)))
+    dy, dy64 = bf16(rng.standard_normal((2, H, W, cout)))
+    w, w64 = bf16(rng.standard_normal((cout, 3, 3, cin)) / np.sqrt(9 * cin))
+    dw = torch.zeros((cout, 3, 3, cin), dtype=torch.float32, device="cuda")
+    db = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    _call("vrc_nn_conv3x3_wgrad", _p(x), _p(dy), 2, H, W, cin, cout, _p(dw), _p(db), _stream())
+    wt = torch.empty((cin, 3, 3, cout), dtype=torch.bfloat16, device="cuda")
+    _call("vrc_nn_flip_weights", _p(w), cout, cin, _p(wt), _stream())
+    dx = torch.empty((2, H, W, cin), dtype=torch.float32, device="cuda")
+    if cin in (16, 32, 64, 128):
+        _call("vrc_nn_conv3x3_fwd", _p(dy), 2, H, W, cout, _p(wt), None, cin, 0, _p(dx), 1, _stream())
+    torch.cuda.synchronize()
+    rdw, rdb = R.conv3x3_wgrad(x64, dy64)
+    assert rel_err(dw.cpu().numpy(), rdw) < 1e-5
+    assert rel_err(db.cpu().numpy(), rdb) < 1e-5
+    if cin in (16, 32, 64, 128):
+        assert rel_err(dx.cpu().numpy(), R.conv3x3_dgrad(dy64, w64)) < 1e-5
+
+
+def test_loss_gradient(vrc_lib):
+    from voreen_gb300.learned import loss_and_grad
+    rng = np.random.default_rng(4)
+    y = rng.uniform(0, 1, (1, 12, 10, 4))
+    x = np.clip(y + 0.1 * rng.standard_normal(y.shape), 0, 1)
+    xt = torch.from_numpy(x.astype(np.float32)).cuda()
+    yt = torch.from_numpy(y.astype(np.float32)).cuda()
+    L, dx, _ = loss_and_grad(xt, yt, radius=2, lam=0.2)
+    x32, y32 = xt.cpu().numpy().astype(np.float64), yt.cpu().numpy().astype(np.float64)
+    assert abs(float(L) - R.loss(x32, y32)) < 1e-5
+    idx = rng.choice(x.size, 40, replace=False)
+    num = R.loss_grad_numeric(x32.copy(), y32, idx)
+    got = dx.cpu().numpy().reshape(-1)[idx].astype(np.float64)
+    assert np.abs(got - num).max() < 2e-4 * max(1.0, np.abs(num).max() * 1e3) or rel_err(got, num) < 1e-2
+
+
+def test_head_and_bilinear(vrc_lib):
+    from voreen_gb300.learned import _call, _p, _stream, bilinear_up2
+    rng = np.random.default_rng(5)
+    f = rng.standard_normal((2, 6, 10, 16)).astype(np.float32)
+    base = rng.uniform(0, 1, (2, 6, 10, 4)).astype(np.float32)
+    ft, bt = torch.from_numpy(f).cuda(), torch.from_numpy(base).cuda()
+    out = torch.empty((2, 12, 20, 4), dtype=torch.float32, device="cuda")
+    _call("vrc_nn_head_fwd", _p(ft), _p(bt), 2, 6, 10, _p(out), _stream())
+    ref = R.depth_to_space(f.astype(np.float64)) + R.bilinear_up2(base.astype(np.float64))
+    up = bilinear_up2(bt)
+    torch.cuda.synchronize()
+    assert np.abs(out.cpu().numpy() - ref).max() < 1e-5
+    assert np.abs(up.cpu().numpy() - R.bilinear_up2(base.astype(np.float64))).max() < 1e-6
+
+
+def test_network_forward_and_parameter_gradients(vrc_lib):
+    """Whole U-Net: GPU (BF16 activations, FP32 accumulation) against FP64 on
+    the same BF16 weights and input; activations are rounded to BF16 between
+    layers on the GPU, hence the percent-level bound."""
+    from voreen_gb300.learned import LAYERS, UNet
+    net = UNet(seed=3)
+    # make the head non-trivial so gradients reach every layer
+    net.w["head"].normal_(0, 0.05)
+    net.refresh()
+    rng = np.random.default_rng(6)
+    N, h, w = 2, 16, 24
+    x_np = np.zeros((N, h, w, 16))
+    x_np[..., :6] = rng.uniform(0, 1, (N, h, w, 6))
+    x0, x64 = bf16(x_np)
+    base = torch.from_numpy(rng.uniform(0, 1, (N, h, w, 4)).astype(np.float32)).cuda()
+    out = net.forward(x0, base)
+    dout_np = rng.standard_normal((N, 2 * h, 2 * w, 4)).astype(np.float32)
+    net.zero_grad()
+    net.backward(torch.from_numpy(dout_np).cuda())
+    torch.cuda.synchronize()
+    params = ({k: v.float().cpu().numpy().astype(np.float64) for k, v in net.w16.items()},
+              {k: v.cpu().numpy().astype(np.float64) for k, v in net.b.items()})
+    ref_out, acts = R.forward(params, x64, base.cpu().numpy().astype(np.float64))
+    assert rel_err(out.cpu().numpy(), ref_out) < 1e-2
+    gw, gb = R.backward(params, acts, dout_np.astype(np.float64))
+    # the GPU stores activation gradients in BF16 between layers, so the
+    # error grows with depth from the head (~1 %) to the first layer (~8 %);
+    # the direction of every gradient must still agree
+    for name, *_ in LAYERS:
+        g, r = net.gw[name].cpu().numpy().reshape(-1), gw[name].reshape(-1)
+        e = rel_err(g, r)
+        cos = float(g @ r / (np.linalg.norm(g) * np.linalg.norm(r)))
+        assert e < 0.15 and cos > 0.99, f"{name}: weight gradient relative error {e:.3g}, cosine {cos:.4f}"
+        eb = rel_err(net.gb[name].cpu().numpy(), gb[name])
+        assert eb < 0.15, f"{name}: bias gradient relative error {eb:.3g}"

@@ -30,6 +30,7 @@ SOURCES = [
     ("march.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
     ("batch.cpp", []),
+    ("nn.cu", []),
 ]
 
 
