@@ -156,7 +156,8 @@ typedef struct {
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
     int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (8), else 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
-    int reserved[6];
+    int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
+    int reserved[2];
 } vrc_render_params;
 
 /* Fills `p` with the reference's property defaults for a W x H image. */
@@ -241,6 +242,15 @@ vrc_status vrc_batch_destroy(vrc_batch* b);
 #define VRC_NOALLOC_MAX_CELLS 2097152
 vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                               const float* d_entry, const float* d_exit, void* d_out, int out_format, void* stream);
+
+/* vrc_render into device buffers plus an auxiliary per-pixel float2 image:
+ * (first-hit ray parameter / ray length, or 1 without a hit; gradient
+ * magnitude at the first hit scaled by min(spacing) / TF domain width, 0
+ * without shading). No counterpart in the reference: it feeds the learned
+ * upsampler (include/vrc_nn.h). entry/exit may be NULL in analytic mode. */
+vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                          const float* d_entry, const float* d_exit, void* d_out, int out_format, float* d_aux,
+                          vrc_render_stats* stats);
 
 /* Analytic entry/exit points (texture space) for `p->camera`, written as
  * float4 images, host or device destination. */

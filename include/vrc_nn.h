@@ -52,6 +52,11 @@ int vrc_nn_loss(const float* x, const float* y, int N, int H, int W, int radius,
 /* Adam step on FP32 master weights; refreshes the BF16 copy (nullable). */
 int vrc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long long n, float lr, float b1, float b2,
                 float eps, int step, void* stream);
+/* Probe check: adds [sum of squared error, max |a-b|] over the window
+ * (x0, y0, w, h) of two RGBA FP32 images of width W (values clamped to
+ * [0,1]) to out2 (zeroed by the caller). */
+int vrc_nn_probe_error(const float* a, const float* b, int W, int x0, int y0, int w, int h, float* out2,
+                       void* stream);
 /* Network input from a low-resolution march: RGBA FP32 + aux FP32x2 (first-hit
  * depth, gradient magnitude; nullable) -> BF16 NHWC with 16 channels. */
 int vrc_nn_pack_input(const float* rgba, const float* aux2, long long npix, void* out, void* stream);

@@ -46,7 +46,7 @@ class RenderParams(C.Structure):
                 ("material_shininess", C.c_float), ("apply_attenuation", C.c_int),
                 ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
                 ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("skip_cell_size", C.c_int),
-                ("tile_width", C.c_int), ("reserved", C.c_int * 6)]
+                ("tile_width", C.c_int), ("region", C.c_int * 4), ("reserved", C.c_int * 2)]
 
 
 class BatchItem(C.Structure):
@@ -91,12 +91,33 @@ SIGNATURES = {
     "vrc_render_params_default": (None, [P(RenderParams), C.c_int, C.c_int]),
     "vrc_render": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, C.c_int, VP, C.c_int, C.c_int, P(RenderStats)]),
     "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
+    "vrc_render_aux": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP, P(RenderStats)]),
     "vrc_batch_create": (C.c_int, [VP, P(BatchItem), C.c_int, P(VP)]),
     "vrc_batch_launch": (C.c_int, [VP]),
     "vrc_batch_stats_get": (C.c_int, [VP, VP, P(BatchStats)]),
     "vrc_batch_destroy": (C.c_int, [VP]),
     "vrc_render_noalloc": (C.c_int, [VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
+}
+
+# include/vrc_nn.h (learned upsampler kernels): all return int status
+_I, _F, _LL = C.c_int, C.c_float, C.c_longlong
+NN_SIGNATURES = {
+    "vrc_nn_conv3x3_fwd": [VP, _I, _I, _I, _I, VP, VP, _I, _I, VP, _I, VP],
+    "vrc_nn_conv3x3_wgrad": [VP, VP, _I, _I, _I, _I, _I, VP, VP, VP],
+    "vrc_nn_flip_weights": [VP, _I, _I, VP, VP],
+    "vrc_nn_relu_bwd": [VP, VP, _LL, VP],
+    "vrc_nn_avgpool2": [VP, _I, _I, _I, _I, _F, VP, VP],
+    "vrc_nn_upsample2": [VP, _I, _I, _I, _I, _F, VP, VP],
+    "vrc_nn_concat": [VP, _I, VP, _I, _LL, VP, _I, VP],
+    "vrc_nn_add": [VP, VP, _LL, VP],
+    "vrc_nn_head_fwd": [VP, VP, _I, _I, _I, VP, VP],
+    "vrc_nn_head_bwd": [VP, _I, _I, _I, VP, VP],
+    "vrc_nn_bilinear_up2": [VP, _I, _I, _I, VP, VP],
+    "vrc_nn_loss": [VP, VP, _I, _I, _I, _I, _F, VP, VP, VP, VP],
+    "vrc_nn_adam": [VP, VP, VP, VP, VP, _LL, _F, _F, _F, _F, _I, VP],
+    "vrc_nn_pack_input": [VP, VP, _LL, VP, VP],
+    "vrc_nn_probe_error": [VP, VP, _I, _I, _I, _I, _I, VP, VP],
 }
 
 _lib = None
@@ -113,6 +134,10 @@ def load(path: str = LIB_PATH):
     for name, (res, args) in SIGNATURES.items():
         fn = getattr(L, name)
         fn.restype = res
+        fn.argtypes = args
+    for name, args in NN_SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = C.c_int
         fn.argtypes = args
     _lib = L
     return L

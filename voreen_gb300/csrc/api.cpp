@@ -576,8 +576,19 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
     P.quantize = p->quantize_entry_exit;
     const int tw = p->tile_width == 0 ? 8 : p->tile_width;
     P.tile_wshift = ilog2(tw);
-    P.tiles_x = (p->width + tw - 1) / tw;
-    P.tiles_y = (p->height + (32 / tw) - 1) / (32 / tw);
+    if (p->region[2] > 0 && p->region[3] > 0) {
+        P.rx0 = std::max(0, p->region[0]);
+        P.ry0 = std::max(0, p->region[1]);
+        P.rx1 = std::min(p->width, p->region[0] + p->region[2]);
+        P.ry1 = std::min(p->height, p->region[1] + p->region[3]);
+        if (P.rx1 <= P.rx0 || P.ry1 <= P.ry0) return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: empty region");
+    } else {
+        P.rx0 = P.ry0 = 0;
+        P.rx1 = p->width;
+        P.ry1 = p->height;
+    }
+    P.tiles_x = (P.rx1 - P.rx0 + tw - 1) / tw;
+    P.tiles_y = (P.ry1 - P.ry0 + (32 / tw) - 1) / (32 / tw);
     if (p->entry_exit_mode == VRC_EE_ANALYTIC) {
         double inv[16];
         if (vrc_camera_matrices(&p->camera, &d, p->width, p->height, nullptr, nullptr, inv) != VRC_OK)
@@ -617,9 +628,13 @@ using vrc::tf_table;
 
 extern "C" {
 
-vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
-                      const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
-                      int out_on_device, vrc_render_stats* stats) {
+}  // extern "C"
+
+namespace {
+
+vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
+                       const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
+                       int out_on_device, float* aux, vrc_render_stats* stats) {
     if (!ctx) return VRC_ERR_INVALID_ARG;
     if (!vol || !tf_c) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: volume and transfer function are required");
     if (vol->ctx != ctx || tf_c->ctx != ctx) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: handle from another context");
@@ -666,6 +681,12 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
         P.out = ctx->d_out;
     }
     P.out_format = out_format;
+    if (aux) {
+        P.aux = reinterpret_cast<float2*>(aux);
+        const float dom = std::max(tf->hi - tf->lo, 1e-12f);
+        const float msp = std::min(vol->desc.spacing[0], std::min(vol->desc.spacing[1], vol->desc.spacing[2]));
+        P.aux_gscale = msp / dom;
+    }
     if (p->empty_space_skipping) {
         // skip cells: the requested edge if the volume holds that level, else the brick
         const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
@@ -725,6 +746,23 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_
         if (stats->device_status != 0) return fail(ctx, VRC_ERR_DEVICE, "vrc_render: kernel reported an error status");
     }
     return VRC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                      const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
+                      int out_on_device, vrc_render_stats* stats) {
+    return render_impl(ctx, vol, tf, p, entry, exitp, ee_on_device, out, out_format, out_on_device, nullptr, stats);
+}
+
+vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                          const float* d_entry, const float* d_exit, void* d_out, int out_format, float* d_aux,
+                          vrc_render_stats* stats) {
+    if (!d_aux) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render_aux: null aux image");
+    return render_impl(ctx, vol, tf, p, d_entry, d_exit, 1, d_out, out_format, 1, d_aux, stats);
 }
 
 vrc_status vrc_entry_exit(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, float* entry,

@@ -376,7 +376,7 @@ __device__ __forceinline__ void jump_empty_run(float& t, int& loop, float step, 
 // One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
 template <int DT, int COMP, int SHADE, int EE>
 __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
-                            int py, Counters& cnt) {
+                            int py, Counters& cnt, float2& aux) {
     using T = typename Vox<DT>::T;
     const T* __restrict__ bricks = reinterpret_cast<const T*>(P.bricks);
     const BrickLayout& L = P.L;
@@ -399,6 +399,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
     float max_int = 0.f;
     float t = 0.f;
+    float hit_t = -1.f, hit_g = 0.f;  // first sample with alpha > 0 (auxiliary output)
     bool finished = false;
     int loop = 0;
     while (!finished && loop < LOOP_CAP) {
@@ -489,11 +490,13 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
                                  a_(m_(s_(m_(sy, P.dimf[1]), 0.5f), P.spacing[1]), P.vol_offset[1]),
                                  a_(m_(s_(m_(sz, P.dimf[2]), 0.5f), P.spacing[2]), P.vol_offset[2])};
+                    if (hit_t < 0.f) hit_g = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
                     const F3 sh = phong_fast(P, g, pos, F3{c.x, c.y, c.z});
                     c.x = sh.x;
                     c.y = sh.y;
                     c.z = sh.z;
                 }
+                if (hit_t < 0.f) hit_t = t;
                 if (COMP == VRC_DVR) {
                     const float w = m_(s_(1.f, res.w), c.w);
                     res.x = a_(res.x, m_(w, c.x));
@@ -519,6 +522,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
         finished = finished || (t > tend);
     }
     cnt.samples += (unsigned long long)loop;
+    aux = hit_t < 0.f ? make_float2(1.f, 0.f) : make_float2(__fdividef(hit_t, fmaxf(tend, 1e-20f)), hit_g * P.aux_gscale);
     return res;
 }
 
@@ -541,8 +545,9 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
         if (tile >= ntiles) break;
         const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
         const int tw = 1 << P.tile_wshift;
-        const int px = tx * tw + (lane & (tw - 1)), py = ty * (32 >> P.tile_wshift) + (lane >> P.tile_wshift);
-        if (px < P.W && py < P.H) {
+        const int px = P.rx0 + tx * tw + (lane & (tw - 1));
+        const int py = P.ry0 + ty * (32 >> P.tile_wshift) + (lane >> P.tile_wshift);
+        if (px < P.rx1 && py < P.ry1) {
             const size_t pix = (size_t)py * P.W + px;
             float4 f, l;
             if (EE == VRC_EE_BUFFERS) {
@@ -554,8 +559,10 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
             const bool bg = f.x == 0.f && f.y == 0.f && f.z == 0.f && f.w == 0.f && l.x == 0.f && l.y == 0.f &&
                             l.z == 0.f && l.w == 0.f;
             float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (!bg) r = march_ray<DT, COMP, SHADE, EE>(P, s_tf, f, l, px, py, cnt);
+            float2 ax = make_float2(1.f, 0.f);
+            if (!bg) r = march_ray<DT, COMP, SHADE, EE>(P, s_tf, f, l, px, py, cnt, ax);
             write_out(P, pix, r);
+            if (P.aux) P.aux[pix] = ax;
         }
     }
     if (P.counters) {
@@ -698,21 +705,25 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS)
         const unsigned lt = tile - tile_prefix[r];
         const int tx = (int)(lt % (unsigned)P.tiles_x), ty = (int)(lt / (unsigned)P.tiles_x);
         const int tw = 1 << P.tile_wshift;
-        const int px = tx * tw + (lane & (tw - 1)), py = ty * (32 >> P.tile_wshift) + (lane >> P.tile_wshift);
-        if (px < P.W && py < P.H) {
+        const int px = P.rx0 + tx * tw + (lane & (tw - 1));
+        const int py = P.ry0 + ty * (32 >> P.tile_wshift) + (lane >> P.tile_wshift);
+        if (px < P.rx1 && py < P.ry1) {
             float4 f, l;
             analytic_entry_exit(P, px, py, f, l);
             const bool bg = f.x == 0.f && f.y == 0.f && f.z == 0.f && f.w == 0.f && l.x == 0.f && l.y == 0.f &&
                             l.z == 0.f && l.w == 0.f;
             float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
+            float2 ax = make_float2(1.f, 0.f);
             if (!bg) {
                 const int dt = s_dtype[wib];
-                if (dt == VRC_U8) res = march_ray<VRC_U8, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt);
+                if (dt == VRC_U8)
+                    res = march_ray<VRC_U8, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
                 else if (dt == VRC_U16)
-                    res = march_ray<VRC_U16, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt);
-                else res = march_ray<VRC_F32, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt);
+                    res = march_ray<VRC_U16, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
+                else res = march_ray<VRC_F32, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
             }
             write_out(P, (size_t)py * P.W + px, res);
+            if (P.aux) P.aux[(size_t)py * P.W + px] = ax;
         }
         __syncwarp();
         if (lane == 0) {

@@ -500,6 +500,27 @@ __global__ void pack_input_kernel(const float* rgba, const float* aux2, long lon
     }
 }
 
+// Probe: squared error sum and max |a - b| over a pixel window of two RGBA
+// FP32 images of width W (a: the network's frame, b: the plain render).
+__global__ void probe_error_kernel(const float* a, const float* b, int W, int x0, int y0, int w, int h, float* out2) {
+    float se = 0.f, mx = 0.f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w * h * 4; i += gridDim.x * blockDim.x) {
+        const int k = i & 3, p = i >> 2;
+        const size_t o = ((size_t)(y0 + p / w) * W + (x0 + p % w)) * 4 + k;
+        const float d = fminf(fmaxf(a[o], 0.f), 1.f) - fminf(fmaxf(b[o], 0.f), 1.f);
+        se += d * d;
+        mx = fmaxf(mx, fabsf(d));
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        se += __shfl_xor_sync(FULL, se, o);
+        mx = fmaxf(mx, __shfl_xor_sync(FULL, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out2, se);
+        atomicMax(reinterpret_cast<int*>(out2 + 1), __float_as_int(mx));  // non-negative floats order as ints
+    }
+}
+
 int ew_grid(long long n) {
     long long g = (n + 255) / 256;
     return (int)(g > 152 * 32 ? 152 * 32 : (g < 1 ? 1 : g));
@@ -613,6 +634,13 @@ int vrc_nn_adam(float* w, const float* g, float* m, float* v, void* w_bf16, long
 int vrc_nn_flip_weights(const void* w, int Cout, int Cin, void* wt, void* stream) {
     flip_weights_kernel<<<ew_grid((long long)Cout * 9 * Cin), 256, 0, static_cast<cudaStream_t>(stream)>>>(
         static_cast<const __nv_bfloat16*>(w), Cout, Cin, static_cast<__nv_bfloat16*>(wt));
+    return status_of(cudaGetLastError());
+}
+
+int vrc_nn_probe_error(const float* a, const float* b, int W, int x0, int y0, int w, int h, float* out2,
+                       void* stream) {
+    if (!a || !b || !out2 || w < 1 || h < 1) return 1;
+    probe_error_kernel<<<16, 256, 0, static_cast<cudaStream_t>(stream)>>>(a, b, W, x0, y0, w, h, out2);
     return status_of(cudaGetLastError());
 }
 

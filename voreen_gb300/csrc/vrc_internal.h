@@ -73,6 +73,9 @@ struct MarchParams {
     unsigned int* tile_counter;
     int tiles_x, tiles_y;
     int tile_wshift;             // ray tile = (1 << tile_wshift) x (32 >> tile_wshift) pixels per warp
+    int rx0, ry0, rx1, ry1;      // rendered pixel window [rx0, rx1) x [ry0, ry1) (the whole image by default)
+    float2* aux;                 // optional per pixel (first-hit depth / ray length, |gradient| there), nullptr = off
+    float aux_gscale;            // gradient magnitude scale for aux.y
 };
 
 // One request of a batched launch.

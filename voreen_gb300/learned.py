@@ -39,33 +39,8 @@ _NN = None
 
 
 def nn_lib():
-    """The library with the vrc_nn_* signatures set."""
-    global _NN
-    if _NN is None:
-        L = _abi.load()
-        VP, I, F, LL = C.c_void_p, C.c_int, C.c_float, C.c_longlong
-        sig = {
-            "vrc_nn_conv3x3_fwd": [VP, I, I, I, I, VP, VP, I, I, VP, I, VP],
-            "vrc_nn_conv3x3_wgrad": [VP, VP, I, I, I, I, I, VP, VP, VP],
-            "vrc_nn_flip_weights": [VP, I, I, VP, VP],
-            "vrc_nn_relu_bwd": [VP, VP, LL, VP],
-            "vrc_nn_avgpool2": [VP, I, I, I, I, F, VP, VP],
-            "vrc_nn_upsample2": [VP, I, I, I, I, F, VP, VP],
-            "vrc_nn_concat": [VP, I, VP, I, LL, VP, I, VP],
-            "vrc_nn_add": [VP, VP, LL, VP],
-            "vrc_nn_head_fwd": [VP, VP, I, I, I, VP, VP],
-            "vrc_nn_head_bwd": [VP, I, I, I, VP, VP],
-            "vrc_nn_bilinear_up2": [VP, I, I, I, VP, VP],
-            "vrc_nn_loss": [VP, VP, I, I, I, I, F, VP, VP, VP, VP],
-            "vrc_nn_adam": [VP, VP, VP, VP, VP, LL, F, F, F, F, I, VP],
-            "vrc_nn_pack_input": [VP, VP, LL, VP, VP],
-        }
-        for name, args in sig.items():
-            fn = getattr(L, name)
-            fn.argtypes = args
-            fn.restype = C.c_int
-        _NN = L
-    return _NN
+    """The library (signatures of include/vrc_nn.h are set by _abi.load)."""
+    return _abi.load()
 
 
 def _p(t):
@@ -308,3 +283,243 @@ def bilinear_up2(rgba):
     out = torch.empty((N, 2 * H, 2 * W, 4), dtype=torch.float32, device=rgba.device)
     _call("vrc_nn_bilinear_up2", _p(rgba.contiguous()), N, H, W, _p(out), _stream())
     return out
+
+
+# ---- the learned render path ------------------------------------------------
+def low_params(params, factor: int = 2):
+    """Half resolution, half sampling rate, analytic entry/exit."""
+    from . import EE_ANALYTIC, RenderParams
+    q = RenderParams()
+    C.memmove(C.byref(q), C.byref(params), C.sizeof(RenderParams))
+    q.width, q.height = params.width // factor, params.height // factor
+    q.sampling_rate = params.sampling_rate / factor
+    q.entry_exit_mode = EE_ANALYTIC
+    q.region[:] = [0, 0, 0, 0]
+    return q
+
+
+def march_aux(ctx, vol, tf, params):
+    """Plain march into device buffers plus the auxiliary image: returns
+    (rgba (1, h, w, 4) FP32, aux (1, h, w, 2) FP32, stats)."""
+    import torch
+    from . import OUT_RGBA32F, RenderStats, _check, lib
+    rgba = torch.empty((1, params.height, params.width, 4), dtype=torch.float32, device="cuda")
+    aux = torch.empty((1, params.height, params.width, 2), dtype=torch.float32, device="cuda")
+    st = RenderStats()
+    torch.cuda.current_stream().synchronize()
+    _check(lib().vrc_render_aux(ctx.handle, vol.handle, tf.handle, C.byref(params), None, None, _p(rgba),
+                                OUT_RGBA32F, _p(aux), C.byref(st)), ctx, "vrc_render_aux")
+    return rgba, aux, st
+
+
+def plain_frame(ctx, vol, tf, params, region=None):
+    """Full plain render (analytic entry/exit) into a device FP32 image."""
+    import torch
+    from . import EE_ANALYTIC, OUT_RGBA32F, render
+    q = low_params(params, 1)
+    q.entry_exit_mode = EE_ANALYTIC
+    if region is not None:
+        q.region[:] = list(region)
+    out = torch.zeros((params.height, params.width, 4), dtype=torch.float32, device="cuda")
+    torch.cuda.current_stream().synchronize()
+    _, st = render(ctx, vol, tf, q, None, None, OUT_RGBA32F, out)
+    return out, st
+
+
+def psnr(a, b):
+    """PSNR (peak 1) over all RGBA channels of two images clamped to [0, 1]."""
+    import torch
+    mse = torch.mean((a.clamp(0, 1) - b.clamp(0, 1)) ** 2).item()
+    return float("inf") if mse == 0 else 10.0 * math.log10(1.0 / mse)
+
+
+class LearnedRenderer:
+    """Half-resolution, half-rate march -> U-Net -> full frame, with a probe:
+    a probe x probe tile of the plain full-rate render is compared with the
+    network's frame every call; if its PSNR falls below `psnr_bound` the frame
+    is rendered by the plain kernel instead (the fallback)."""
+
+    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0):
+        import torch
+        self.ctx, self.net, self.probe, self.bound = ctx, net, probe, psnr_bound
+        self.err = torch.zeros(2, dtype=torch.float32, device="cuda")
+        self.frames = 0
+        self.fallbacks = 0
+
+    def probe_window(self, W, H):
+        """A different probe tile each frame, walking a coarse grid of the image."""
+        p = self.probe
+        nx, ny = max(1, W // p), max(1, H // p)
+        k = (self.frames * 7919) % (nx * ny)
+        return (k % nx) * p, (k // nx) * p, min(p, W), min(p, H)
+
+    def render(self, vol, tf, params):
+        """Returns (frame (H, W, 4) FP32 device tensor, info dict)."""
+        import torch
+        lp = low_params(params, 2)
+        rgba, aux, _ = march_aux(self.ctx, vol, tf, lp)
+        x0 = pack_input(rgba, aux)
+        out = self.net.forward(x0, rgba)[0]
+        x, y, w, h = self.probe_window(params.width, params.height)
+        ref, _ = plain_frame(self.ctx, vol, tf, params, region=(x, y, w, h))
+        self.err.zero_()
+        _call("vrc_nn_probe_error", _p(out), _p(ref), params.width, x, y, w, h, _p(self.err), _stream())
+        se, mx = self.err.tolist()
+        mse = se / (w * h * 4)
+        probe_psnr = float("inf") if mse == 0 else 10 * math.log10(1.0 / mse)
+        self.frames += 1
+        fallback = probe_psnr < self.bound
+        if fallback:
+            self.fallbacks += 1
+            out, _ = plain_frame(self.ctx, vol, tf, params)
+        return out, {"probe_psnr": probe_psnr, "probe_max_abs": mx, "fallback": fallback}
+
+
+# ---- training on pairs the plain raycaster renders ---------------------------
+def random_view(rng, vox, spacing, seed, width=1920, height=1080):
+    """A random orbit camera and a random 5-trapezoid TF on the shell intensities."""
+    from . import synth
+    dims = (vox.shape[2], vox.shape[1], vox.shape[0])
+    keys, domain = synth.shells_tf(vox, seed)
+    pos, focus, near, far = synth.orbit_camera(dims, spacing, rng.uniform(0, 360), rng.uniform(-60, 60),
+                                               rng.uniform(1.1, 1.8))
+    w = synth.Workload("train", vox, spacing, keys, 4096, domain, width, height, 2.0, compositing=0, shading=1,
+                       camera_pos=pos, camera_focus=focus, near=near, far=far, light_pos=(*pos, 1.0))
+    return w
+
+
+def make_pair(ctx, vol, tf, params):
+    """(x0 BF16 (1,h,w,16), low rgba (1,h,w,4), target (1,H,W,4)) for one view."""
+    lp = low_params(params, 2)
+    rgba, aux, _ = march_aux(ctx, vol, tf, lp)
+    target, _ = plain_frame(ctx, vol, tf, params)
+    return pack_input(rgba, aux), rgba, target[None]
+
+
+def crops(x0, base, target, n, size, rng):
+    """n random aligned crops (low size x size, high 2size x 2size)."""
+    import torch
+    _, h, w, _ = x0.shape
+    xs, bs, ts = [], [], []
+    for _ in range(n):
+        y = int(rng.integers(0, max(1, h - size + 1)))
+        x = int(rng.integers(0, max(1, w - size + 1)))
+        xs.append(x0[:, y:y + size, x:x + size])
+        bs.append(base[:, y:y + size, x:x + size])
+        ts.append(target[:, 2 * y:2 * y + 2 * size, 2 * x:2 * x + 2 * size])
+    return (torch.cat(xs).contiguous(), torch.cat(bs).contiguous(), torch.cat(ts).contiguous())
+
+
+def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, crop: int = 96, lr: float = 1e-3,
+          refresh_every: int = 2, log=None, width=1920, height=1080):
+    """Adam on L1 + SSIM over random crops of pairs rendered on the fly from
+    `volumes` [(Volume, voxels, spacing)] with random cameras and TFs."""
+    import random
+    import time
+
+    import numpy as np
+
+    from . import TransferFunction
+    rng = np.random.default_rng(seed)
+    prng = random.Random(seed)
+    hist = []
+    pair = None
+    t0 = time.time()
+    for it in range(steps):
+        if pair is None or it % refresh_every == 0:
+            vol, vox, sp = volumes[int(rng.integers(0, len(volumes)))]
+            w = random_view(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
+            tf = TransferFunction(ctx, TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+            pair = make_pair(ctx, vol, tf, w.params())
+            tf.close()
+        x0, base, target = crops(*pair, batch, crop, rng)
+        out = net.forward(x0, base)
+        L, dx, (l1, ss) = loss_and_grad(out, target)
+        net.zero_grad()
+        net.backward(dx)
+        cur_lr = lr * 0.5 * (1 + math.cos(math.pi * it / max(1, steps)))
+        net.adam(lr=cur_lr)
+        if log is not None and (it % 100 == 0 or it == steps - 1):
+            rec = {"step": it, "loss": float(L), "l1": float(l1), "ssim": float(ss), "lr": cur_lr,
+                   "seconds": time.time() - t0}
+            hist.append(rec)
+            log(rec)
+    return hist
+
+
+def evaluate(ctx, net, volumes, views: int, seed: int, width=1920, height=1080):
+    """PSNR of the learned frame and of the bilinear upsample of the same
+    half-resolution march (the method without the network) against the plain
+    full render, on `views` random views of `volumes`."""
+    import random
+
+    import numpy as np
+
+    from . import TransferFunction
+    prng = random.Random(seed)
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(views):
+        vol, vox, sp = volumes[int(rng.integers(0, len(volumes)))]
+        w = random_view(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
+        tf = TransferFunction(ctx, TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+        x0, base, target = make_pair(ctx, vol, tf, w.params())
+        y = net.forward(x0, base)
+        bl = bilinear_up2(base)
+        out.append({"psnr_net": psnr(y, target), "psnr_bilinear": psnr(bl, target),
+                    "max_abs_net": float((y.clamp(0, 1) - target.clamp(0, 1)).abs().max())})
+        tf.close()
+    return out
+
+
+def _main():
+    import argparse
+    import json
+    import time
+
+    import torch
+
+    from . import Context, Volume, build, synth, synth_volume
+    ap = argparse.ArgumentParser(description="train / evaluate the learned upsampler")
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--size", type=int, default=512)
+    ap.add_argument("--train-volumes", type=int, default=4)
+    ap.add_argument("--eval-views", type=int, default=8)
+    ap.add_argument("--batch", type=int, default=8)
+    ap.add_argument("--crop", type=int, default=96)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--out", default="upsampler.npz")
+    ap.add_argument("--init", default=None)
+    args = ap.parse_args()
+    build.build()
+    ctx = Context(0)
+    d = (args.size,) * 3
+
+    def vols(seeds):
+        res = []
+        for s in seeds:
+            vox = synth_volume(synth.SHELLS, 1, d, 4000 + s)
+            res.append((Volume(ctx, vox, (0.7, 0.7, 1.0)), vox, (0.7, 0.7, 1.0)))
+        return res
+
+    t0 = time.time()
+    train_vols = vols(range(args.train_volumes))
+    held_out = vols([100, 101])
+    net = UNet(seed=0)
+    if args.init:
+        net.load(args.init)
+    print(json.dumps({"volumes_ready_s": time.time() - t0}), flush=True)
+    hist = train(ctx, net, train_vols, args.steps, seed=1, batch=args.batch, crop=args.crop, lr=args.lr,
+                 log=lambda r: print(json.dumps(r), flush=True), width=args.width, height=args.height)
+    torch.cuda.synchronize()
+    net.save(args.out)
+    ev = evaluate(ctx, net, held_out, args.eval_views, seed=777, width=args.width, height=args.height)
+    print(json.dumps({"eval": ev, "mean_psnr_net": sum(e["psnr_net"] for e in ev) / len(ev),
+                      "mean_psnr_bilinear": sum(e["psnr_bilinear"] for e in ev) / len(ev),
+                      "train_seconds": hist[-1]["seconds"] if hist else 0}), flush=True)
+
+
+if __name__ == "__main__":
+    _main()
