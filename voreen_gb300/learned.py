@@ -396,14 +396,20 @@ def make_pair(ctx, vol, tf, params):
     return pack_input(rgba, aux), rgba, target[None]
 
 
-def crops(x0, base, target, n, size, rng):
-    """n random aligned crops (low size x size, high 2size x 2size)."""
+def crops(x0, base, target, n, size, rng, min_alpha: float = 0.02, tries: int = 8):
+    """n random aligned crops (low size x size, high 2size x 2size), each
+    re-drawn up to `tries` times until the target's mean alpha exceeds
+    `min_alpha` (empty background teaches nothing)."""
     import torch
     _, h, w, _ = x0.shape
+    amap = target[0, ..., 3]
     xs, bs, ts = [], [], []
     for _ in range(n):
-        y = int(rng.integers(0, max(1, h - size + 1)))
-        x = int(rng.integers(0, max(1, w - size + 1)))
+        for _t in range(tries):
+            y = int(rng.integers(0, max(1, h - size + 1)))
+            x = int(rng.integers(0, max(1, w - size + 1)))
+            if float(amap[2 * y:2 * y + 2 * size, 2 * x:2 * x + 2 * size].mean()) > min_alpha:
+                break
         xs.append(x0[:, y:y + size, x:x + size])
         bs.append(base[:, y:y + size, x:x + size])
         ts.append(target[:, 2 * y:2 * y + 2 * size, 2 * x:2 * x + 2 * size])
