@@ -62,14 +62,14 @@ class UNet:
     """Parameters (FP32 master, BF16 working copies), activations, gradients
     and Adam state of the upsampler, on one CUDA device."""
 
-    def __init__(self, seed: int = 0, device: str = "cuda"):
+    def __init__(self, seed: int = 0, device: str = "cuda", head_std: float = 1e-2):
         import torch
         self.torch = torch
         self.device = device
         g = torch.Generator().manual_seed(seed)
         self.w, self.b = {}, {}
         for name, cin, cout, _ in LAYERS:
-            std = math.sqrt(2.0 / (9 * cin)) if name != "head" else 1e-3
+            std = math.sqrt(2.0 / (9 * cin)) if name != "head" else head_std
             self.w[name] = (torch.randn((cout, 3, 3, cin), generator=g) * std).to(device)
             self.b[name] = torch.zeros(cout, device=device)
         self.step = 0
@@ -416,8 +416,8 @@ def crops(x0, base, target, n, size, rng, min_alpha: float = 0.02, tries: int = 
     return (torch.cat(xs).contiguous(), torch.cat(bs).contiguous(), torch.cat(ts).contiguous())
 
 
-def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, crop: int = 96, lr: float = 1e-3,
-          refresh_every: int = 2, log=None, width=1920, height=1080):
+def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, crop: int = 96, lr: float = 2e-4,
+          refresh_every: int = 2, log=None, width=1920, height=1080, warmup: int = 200):
     """Adam on L1 + SSIM over random crops of pairs rendered on the fly from
     `volumes` [(Volume, voxels, spacing)] with random cameras and TFs."""
     import random
@@ -443,7 +443,7 @@ def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, cr
         L, dx, (l1, ss) = loss_and_grad(out, target)
         net.zero_grad()
         net.backward(dx)
-        cur_lr = lr * 0.5 * (1 + math.cos(math.pi * it / max(1, steps)))
+        cur_lr = lr * min(1.0, (it + 1) / max(1, warmup)) * 0.5 * (1 + math.cos(math.pi * it / max(1, steps)))
         net.adam(lr=cur_lr)
         if log is not None and (it % 100 == 0 or it == steps - 1):
             rec = {"step": it, "loss": float(L), "l1": float(l1), "ssim": float(ss), "lr": cur_lr,
@@ -493,7 +493,9 @@ def _main():
     ap.add_argument("--eval-views", type=int, default=8)
     ap.add_argument("--batch", type=int, default=8)
     ap.add_argument("--crop", type=int, default=96)
-    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--lr", type=float, default=2e-4)
+    ap.add_argument("--head-std", type=float, default=1e-2)
+    ap.add_argument("--warmup", type=int, default=200)
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--out", default="upsampler.npz")
@@ -513,12 +515,13 @@ def _main():
     t0 = time.time()
     train_vols = vols(range(args.train_volumes))
     held_out = vols([100, 101])
-    net = UNet(seed=0)
+    net = UNet(seed=0, head_std=args.head_std)
     if args.init:
         net.load(args.init)
     print(json.dumps({"volumes_ready_s": time.time() - t0}), flush=True)
     hist = train(ctx, net, train_vols, args.steps, seed=1, batch=args.batch, crop=args.crop, lr=args.lr,
-                 log=lambda r: print(json.dumps(r), flush=True), width=args.width, height=args.height)
+                 log=lambda r: print(json.dumps(r), flush=True), width=args.width, height=args.height,
+                 warmup=args.warmup)
     torch.cuda.synchronize()
     net.save(args.out)
     ev = evaluate(ctx, net, held_out, args.eval_views, seed=777, width=args.width, height=args.height)
