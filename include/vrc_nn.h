@@ -16,7 +16,8 @@
 extern "C" {
 #endif
 
-/* out = conv3x3(in, w) + bias, optional ReLU. in BF16 [N][H][W][Cin]
+/* out = act(conv3x3(in, w) + bias), act: 0 none, 1 ReLU, 2 leaky ReLU
+ * (slope 0.05 below zero). in BF16 [N][H][W][Cin]
  * (Cin % 16 == 0), w BF16 [Cout][3][3][Cin], bias FP32 [Cout] (nullable),
  * Cout in {16, 32, 64, 128}; out BF16 or FP32 (out_f32) [N][H][W][Cout]. */
 int vrc_nn_conv3x3_fwd(const void* in, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
@@ -28,8 +29,9 @@ int vrc_nn_conv3x3_wgrad(const void* in, const void* dout, int N, int H, int W, 
 /* wt[ci][kh][kw][co] = w[co][2-kh][2-kw][ci]: weights for the data gradient,
  * which is vrc_nn_conv3x3_fwd(dout, wt). */
 int vrc_nn_flip_weights(const void* w, int Cout, int Cin, void* wt, void* stream);
-/* dy = 0 where y <= 0 (in place), BF16. */
-int vrc_nn_relu_bwd(const void* y, void* dy, long long n, void* stream);
+/* dy *= act'(x) read from the activation y (in place, BF16): 0 (ReLU) or
+ * 0.05 (leaky) where y <= 0. */
+int vrc_nn_relu_bwd(const void* y, void* dy, long long n, int leaky, void* stream);
 /* 2x2 average pool times `scale` (4: sum pool). */
 int vrc_nn_avgpool2(const void* in, int N, int H, int W, int C, float scale, void* out, void* stream);
 /* nearest 2x upsample times `scale` (0.25: backward of the average pool). */

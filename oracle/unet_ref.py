@@ -10,9 +10,10 @@ from __future__ import annotations
 
 import numpy as np
 
-LAYERS = [("enc1a", 16, 32, 1), ("enc1b", 32, 32, 1), ("enc2a", 32, 64, 1), ("enc2b", 64, 64, 1),
-          ("bota", 64, 128, 1), ("botb", 128, 128, 1), ("dec2a", 192, 64, 1), ("dec2b", 64, 64, 1),
-          ("dec1a", 96, 32, 1), ("dec1b", 32, 32, 1), ("head", 32, 16, 0)]
+LAYERS = [("enc1a", 16, 32, 2), ("enc1b", 32, 32, 2), ("enc2a", 32, 64, 2), ("enc2b", 64, 64, 2),
+          ("bota", 64, 128, 2), ("botb", 128, 128, 2), ("dec2a", 192, 64, 2), ("dec2b", 64, 64, 2),
+          ("dec1a", 96, 32, 2), ("dec1b", 32, 32, 2), ("head", 32, 16, 0)]
+LEAK = 0.05
 C1, C2 = 0.01 ** 2, 0.03 ** 2
 
 
@@ -90,7 +91,7 @@ def space_to_depth(d):
 def forward(params, x0, base):
     w, b = params
     a = {"x0": x0}
-    r = lambda v: np.maximum(v, 0)
+    r = lambda v: np.where(v > 0, v, LEAK * v)  # leaky ReLU
     a["e1a"] = r(conv3x3(x0, w["enc1a"], b["enc1a"]))
     a["e1"] = r(conv3x3(a["e1a"], w["enc1b"], b["enc1b"]))
     a["p1"] = avgpool(a["e1"])
@@ -113,7 +114,7 @@ def forward(params, x0, base):
 def backward(params, a, dout):
     w, _ = params
     gw, gb = {}, {}
-    m = lambda y, d: d * (y > 0)
+    m = lambda y, d: d * np.where(y > 0, 1.0, LEAK)
 
     def lay(name, x, dy):
         gw[name], gb[name] = conv3x3_wgrad(x, dy)

@@ -38,6 +38,9 @@ def test_conv_forward(vrc_lib, cin, cout, H, W):
     _call("vrc_nn_conv3x3_fwd", _p(x), 2, H, W, cin, _p(w), _p(b), cout, 1, _p(yb), 0, _stream())
     torch.cuda.synchronize()
     assert rel_err(yb.float().cpu().numpy(), np.maximum(ref, 0)) < 8e-3
+    _call("vrc_nn_conv3x3_fwd", _p(x), 2, H, W, cin, _p(w), _p(b), cout, 2, _p(yb), 0, _stream())
+    torch.cuda.synchronize()
+    assert rel_err(yb.float().cpu().numpy(), np.where(ref > 0, ref, 0.05 * ref)) < 8e-3
 
 
 @pytest.mark.parametrize("cin,cout,H,W", [(16, 16, 8, 16), (32, 32, 13, 21), (96, 64, 16, 40), (64, 128, 9, 17)])
@@ -120,7 +123,7 @@ def test_network_forward_and_parameter_gradients(vrc_lib):
     assert rel_err(out.cpu().numpy(), ref_out) < 1e-2
     gw, gb = R.backward(params, acts, dout_np.astype(np.float64))
     # the GPU stores activation gradients in BF16 between layers, so the
-    # error grows with depth from the head (~1 %) to the first layer (~8 %);
+    # error grows with depth from the head (~1 %) to the first layer;
     # the direction of every gradient must still agree
     for name, *_ in LAYERS:
         g, r = net.gw[name].cpu().numpy().reshape(-1), gw[name].reshape(-1)

@@ -106,7 +106,7 @@ NN_SIGNATURES = {
     "vrc_nn_conv3x3_fwd": [VP, _I, _I, _I, _I, VP, VP, _I, _I, VP, _I, VP],
     "vrc_nn_conv3x3_wgrad": [VP, VP, _I, _I, _I, _I, _I, VP, VP, VP],
     "vrc_nn_flip_weights": [VP, _I, _I, VP, VP],
-    "vrc_nn_relu_bwd": [VP, VP, _LL, VP],
+    "vrc_nn_relu_bwd": [VP, VP, _LL, _I, VP],
     "vrc_nn_avgpool2": [VP, _I, _I, _I, _I, _F, VP, VP],
     "vrc_nn_upsample2": [VP, _I, _I, _I, _I, _F, VP, VP],
     "vrc_nn_concat": [VP, _I, VP, _I, _LL, VP, _I, VP],

@@ -16,6 +16,7 @@
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+constexpr float LEAK = 0.05f;  // slope of the leaky ReLU for negative inputs
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -129,9 +130,12 @@ __global__ void __launch_bounds__(256) conv3x3_fwd_kernel(const __nv_bfloat16* _
                 const int x = x0 + g + 8 * h;
                 if (x >= W) continue;
                 float v0 = acc[r][j][2 * h] + b0, v1 = acc[r][j][2 * h + 1] + b1;
-                if (relu) {
+                if (relu == 1) {
                     v0 = fmaxf(v0, 0.f);
                     v1 = fmaxf(v1, 0.f);
+                } else if (relu == 2) {  // leaky ReLU
+                    v0 = v0 > 0.f ? v0 : LEAK * v0;
+                    v1 = v1 > 0.f ? v1 : LEAK * v1;
                 }
                 const size_t o = (((size_t)n * H + y) * W + x) * COUT + co;
                 if (out_f32) {
@@ -268,9 +272,11 @@ cudaError_t conv_wgrad_t(const __nv_bfloat16* in, const __nv_bfloat16* dout, int
 
 // ---------------------------------------------------------------------------
 // element-wise layers
-__global__ void relu_bwd_kernel(const __nv_bfloat16* y, __nv_bfloat16* dy, long long n) {
+// dy *= d relu / dx, read from the activation's sign (leaky: slope LEAK)
+__global__ void relu_bwd_kernel(const __nv_bfloat16* y, __nv_bfloat16* dy, long long n, int leaky) {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-        if (!(__bfloat162float(y[i]) > 0.f)) dy[i] = __float2bfloat16(0.f);
+        if (!(__bfloat162float(y[i]) > 0.f))
+            dy[i] = __float2bfloat16(leaky ? LEAK * __bfloat162float(dy[i]) : 0.f);
 }
 
 // 2x2 average pool times `scale`, NHWC (H, W even); scale 4 gives the
@@ -562,9 +568,9 @@ int vrc_nn_conv3x3_wgrad(const void* in, const void* dout, int N, int H, int W, 
     }
 }
 
-int vrc_nn_relu_bwd(const void* y, void* dy, long long n, void* stream) {
+int vrc_nn_relu_bwd(const void* y, void* dy, long long n, int leaky, void* stream) {
     relu_bwd_kernel<<<ew_grid(n), 256, 0, static_cast<cudaStream_t>(stream)>>>(
-        static_cast<const __nv_bfloat16*>(y), static_cast<__nv_bfloat16*>(dy), n);
+        static_cast<const __nv_bfloat16*>(y), static_cast<__nv_bfloat16*>(dy), n, leaky);
     return status_of(cudaGetLastError());
 }
 

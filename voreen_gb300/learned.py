@@ -7,11 +7,11 @@ only holds device buffers and orders work on its current stream.
 
 Network (input h x w, output 2h x 2w RGBA):
     x0  = [rgba, first-hit depth, |gradient|, 0...]         16 ch   h x w
-    e1  = relu(conv(relu(conv(x0, 32)), 32))                       h x w
-    e2  = relu(conv(relu(conv(avgpool(e1), 64)), 64))              h/2
-    b   = relu(conv(relu(conv(avgpool(e2), 128)), 128))            h/4
-    d2  = relu(conv(relu(conv([up(b) | e2], 64)), 64))             h/2
-    d1  = relu(conv(relu(conv([up(d2) | e1], 32)), 32))            h
+    e1  = act(conv(act(conv(x0, 32)), 32))   act: leaky ReLU                       h x w
+    e2  = act(conv(act(conv(avgpool(e1), 64)), 64))              h/2
+    b   = act(conv(act(conv(avgpool(e2), 128)), 128))            h/4
+    d2  = act(conv(act(conv([up(b) | e2], 64)), 64))             h/2
+    d1  = act(conv(act(conv([up(d2) | e1], 32)), 32))            h
     out = depth_to_space(conv(d1, 16)) + bilinear_up(rgba)         2h x 2w
 The last term makes the network learn a residual on the interpolated march.
 """
@@ -26,14 +26,15 @@ import numpy as np
 
 from . import _abi
 
-LAYERS = [  # name, Cin, Cout, relu
-    ("enc1a", 16, 32, 1), ("enc1b", 32, 32, 1),
-    ("enc2a", 32, 64, 1), ("enc2b", 64, 64, 1),
-    ("bota", 64, 128, 1), ("botb", 128, 128, 1),
-    ("dec2a", 192, 64, 1), ("dec2b", 64, 64, 1),
-    ("dec1a", 96, 32, 1), ("dec1b", 32, 32, 1),
+LAYERS = [  # name, Cin, Cout, activation (2: leaky ReLU, 0: none)
+    ("enc1a", 16, 32, 2), ("enc1b", 32, 32, 2),
+    ("enc2a", 32, 64, 2), ("enc2b", 64, 64, 2),
+    ("bota", 64, 128, 2), ("botb", 128, 128, 2),
+    ("dec2a", 192, 64, 2), ("dec2b", 64, 64, 2),
+    ("dec1a", 96, 32, 2), ("dec1b", 32, 32, 2),
     ("head", 32, 16, 0),
 ]
+LEAK = 0.05
 
 _NN = None
 
@@ -185,7 +186,7 @@ class UNet:
               _stream())
 
     def _relu_bwd(self, y, dy):
-        _call("vrc_nn_relu_bwd", _p(y), _p(dy), dy.numel(), _stream())
+        _call("vrc_nn_relu_bwd", _p(y), _p(dy), dy.numel(), 1, _stream())
 
     def backward(self, dout):
         """dout: dL/d(output) (N, 2h, 2w, 4) FP32. Accumulates into gw, gb."""
