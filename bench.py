@@ -232,6 +232,76 @@ def run_batch(args, warmup, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_learned(args, warmup, ws, rank, local):
+    """Learned form on the CT-like workload: half-resolution, half-rate march +
+    U-Net (trained weights voreen_gb300/weights/upsampler_ct.npz) + 64x64
+    probe tile, against the plain full render of the same frames; PSNR and
+    max |d| against the plain render on held-out volume seeds."""
+    import random
+
+    import torch
+
+    import voreen_gb300 as v
+    from voreen_gb300 import build as vbuild, learned, synth
+    vbuild.build()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = v.Context(dev)
+    net = learned.UNet(seed=0)
+    net.load(os.path.join(ROOT, "voreen_gb300", "weights", "upsampler_ct.npz"))
+    w = build_workload(args.small)  # held-out: generator seed differs from the training volumes
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    p = w.params(entry_exit_mode=v.EE_ANALYTIC)
+    lr = learned.LearnedRenderer(ctx, net)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        lr.render(vol, tf, p)
+        learned.plain_frame(ctx, vol, tf, p)
+    torch.cuda.synchronize()
+    steps = max(3, min(args.steps, 100))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    infos = []
+    for _ in range(steps):
+        out, info = lr.render(vol, tf, p)
+        infos.append(info)
+    end.record(stream)
+    end.synchronize()
+    ms_learned = start.elapsed_time(end) / steps
+    start.record(stream)
+    for _ in range(steps):
+        ref, _ = learned.plain_frame(ctx, vol, tf, p)
+    end.record(stream)
+    end.synchronize()
+    ms_plain = start.elapsed_time(end) / steps
+    # quality on a few held-out views of the same volume
+    prng = random.Random(4242)
+    quality = []
+    for i in range(4):
+        wv = learned.random_view(prng, w.voxels, w.spacing, 900 + i, w.width, w.height)
+        tfv = v.TransferFunction(ctx, v.TransferFunction.bake(wv.tf_keys, wv.tf_width), wv.domain)
+        pv = wv.params(entry_exit_mode=v.EE_ANALYTIC)
+        o, inf = lr.render(vol, tfv, pv)
+        r, _ = learned.plain_frame(ctx, vol, tfv, pv)
+        x0, base, _ = learned.make_pair(ctx, vol, tfv, wv.params())
+        quality.append({"psnr_learned": learned.psnr(o, r), "psnr_bilinear": learned.psnr(learned.bilinear_up2(base)[0], r),
+                        "max_abs": float((o.clamp(0, 1) - r.clamp(0, 1)).abs().max()), "fallback": inf["fallback"]})
+        tfv.close()
+    line = {"metric": "learned vs plain frames/s at the PSNR bound (40 dB), 512^3 u16 @1080p",
+            "value": 1000.0 / ms_learned, "unit": "frames/s", "n_gpus": ws, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms_learned, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "bf16 network (fp32 accumulate), f32 march", "data": "synthetic (held-out seeded volume)",
+            "config": {"workload": w.name, "input_march": [w.width // 2, w.height // 2, w.sampling_rate / 2],
+                       "network": "U-Net 32/64/128, 3x3, leaky ReLU", "probe": "64x64 plain tile per frame"},
+            "plain_frames_per_s": 1000.0 / ms_plain, "speedup_vs_plain": ms_plain / ms_learned,
+            "fallback_rate": sum(1 for i in infos if i["fallback"]) / len(infos),
+            "probe_psnr_median": statistics.median(i["probe_psnr"] for i in infos),
+            "quality_held_out": quality}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -239,7 +309,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
-    ap.add_argument("--workload", default="ct", choices=["ct", "batch"],
+    ap.add_argument("--workload", default="ct", choices=["ct", "batch", "learned"],
                     help="ct: 512^3 u16 shaded DVR 1080p (default); batch: 64 mixed requests in one launch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
@@ -265,6 +335,9 @@ def main():
     if args.workload == "batch":
         if rank == 0 or ws > 1:
             run_batch(args, warmup, ws, rank, local)
+        return
+    if args.workload == "learned":
+        run_learned(args, warmup, ws, rank, local)
         return
 
     w = build_workload(args.small)
