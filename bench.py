@@ -254,12 +254,14 @@ def run_learned(args, warmup, ws, rank, local):
     tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
     p = w.params(entry_exit_mode=v.EE_ANALYTIC)
     lr = learned.LearnedRenderer(ctx, net)
-    stream = torch.cuda.current_stream()
+    stream = lr.stream
+    ref = torch.empty((w.height, w.width, 4), dtype=torch.float32, device=f"cuda:{dev}")
     for _ in range(warmup):
         lr.render(vol, tf, p)
-        learned.plain_frame(ctx, vol, tf, p)
+        lr._render_plain(vol, tf, p, ref)
     torch.cuda.synchronize()
-    steps = max(3, min(args.steps, 100))
+    ctx.synchronize()
+    steps = max(3, min(args.steps, 200))
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     start.record(stream)
     infos = []
@@ -271,7 +273,7 @@ def run_learned(args, warmup, ws, rank, local):
     ms_learned = start.elapsed_time(end) / steps
     start.record(stream)
     for _ in range(steps):
-        ref, _ = learned.plain_frame(ctx, vol, tf, p)
+        lr._render_plain(vol, tf, p, ref)
     end.record(stream)
     end.synchronize()
     ms_plain = start.elapsed_time(end) / steps

@@ -22,6 +22,11 @@ extern "C" {
  * Cout in {16, 32, 64, 128}; out BF16 or FP32 (out_f32) [N][H][W][Cout]. */
 int vrc_nn_conv3x3_fwd(const void* in, int N, int H, int W, int Cin, const void* w, const float* bias, int Cout,
                        int relu, void* out, int out_f32, void* stream);
+/* Decoder form: the input is [nearest 2x upsample of a | b] built on load
+ * (a: [N][H/2][W/2][Ca], b: [N][H][W][Cb]; Ca, Cb multiples of 16), so the
+ * upsampled and concatenated tensor is never written. */
+int vrc_nn_conv3x3_fwd_upcat(const void* a, int Ca, const void* b, int Cb, int N, int H, int W, const void* w,
+                             const float* bias, int Cout, int relu, void* out, int out_f32, void* stream);
 /* dw[co][kh][kw][ci] += sum over pixels of dout * shifted in (FP32), and
  * dbias[co] += sum of dout (nullable). */
 int vrc_nn_conv3x3_wgrad(const void* in, const void* dout, int N, int H, int W, int Cin, int Cout, float* dw,

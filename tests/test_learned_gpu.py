@@ -132,3 +132,18 @@ def test_network_forward_and_parameter_gradients(vrc_lib):
         assert e < 0.15 and cos > 0.99, f"{name}: weight gradient relative error {e:.3g}, cosine {cos:.4f}"
         eb = rel_err(net.gb[name].cpu().numpy(), gb[name])
         assert eb < 0.15, f"{name}: bias gradient relative error {eb:.3g}"
+
+
+def test_fused_decoder_inference_equals_forward(vrc_lib):
+    """infer() (upsample + concat built on load) gives forward()'s values."""
+    from voreen_gb300.learned import UNet
+    net = UNet(seed=2)
+    net.w["head"].normal_(0, 0.05)
+    net.refresh()
+    rng = np.random.default_rng(8)
+    x0, _ = bf16(np.concatenate([rng.uniform(0, 1, (1, 24, 32, 6)), np.zeros((1, 24, 32, 10))], axis=3))
+    base = torch.from_numpy(rng.uniform(0, 1, (1, 24, 32, 4)).astype(np.float32)).cuda()
+    a = net.forward(x0, base)
+    b = net.infer(x0, base)
+    torch.cuda.synchronize()
+    assert torch.equal(a, b)

@@ -104,6 +104,7 @@ SIGNATURES = {
 _I, _F, _LL = C.c_int, C.c_float, C.c_longlong
 NN_SIGNATURES = {
     "vrc_nn_conv3x3_fwd": [VP, _I, _I, _I, _I, VP, VP, _I, _I, VP, _I, VP],
+    "vrc_nn_conv3x3_fwd_upcat": [VP, _I, VP, _I, _I, _I, _I, VP, VP, _I, _I, VP, _I, VP],
     "vrc_nn_conv3x3_wgrad": [VP, VP, _I, _I, _I, _I, _I, VP, VP, VP],
     "vrc_nn_flip_weights": [VP, _I, _I, VP, VP],
     "vrc_nn_relu_bwd": [VP, VP, _LL, _I, VP],

@@ -51,11 +51,15 @@ __device__ __forceinline__ void mma_bf16(float* d, uint32_t a0, uint32_t a1, uin
 // rows fall on distinct banks), then runs 9 taps x COUT/8 MMAs per m-tile.
 constexpr int PIX_PAD = 24;  // bf16 per staged pixel / weight row (16 used)
 
+// Optional fused input [up2(A) | B]: channels [0, Ca) come from A at half
+// resolution (nearest 2x upsample on load) and [Ca, Ca + Cb) from B; Cin =
+// Ca + Cb and `in` is A. With in_b == nullptr the input is `in` as is.
 template <int COUT, int RPW>
 __global__ void __launch_bounds__(256) conv3x3_fwd_kernel(const __nv_bfloat16* __restrict__ in, int N, int H, int W,
                                                           int Cin, const __nv_bfloat16* __restrict__ wt,
                                                           const float* __restrict__ bias, int relu, void* out,
-                                                          int out_f32) {
+                                                          int out_f32, const __nv_bfloat16* __restrict__ in_b,
+                                                          int Ca) {
     constexpr int TH = 8 * RPW;
     constexpr int NT = COUT / 8;
     extern __shared__ __align__(16) __nv_bfloat16 smem[];
@@ -76,8 +80,19 @@ __global__ void __launch_bounds__(256) conv3x3_fwd_kernel(const __nv_bfloat16* _
             const int ry = pix / 18, rx = pix % 18;
             const int gy = y0 + ry - 1, gx = x0 + rx - 1;
             uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (gy >= 0 && gy < H && gx >= 0 && gx < W)
-                v = *reinterpret_cast<const uint4*>(in + (((size_t)n * H + gy) * W + gx) * Cin + c0 + half * 8);
+            if (gy >= 0 && gy < H && gx >= 0 && gx < W) {
+                if (in_b == nullptr) {
+                    v = *reinterpret_cast<const uint4*>(in + (((size_t)n * H + gy) * W + gx) * Cin + c0 + half * 8);
+                } else if (c0 < Ca) {
+                    const int Hh = H >> 1, Wh = W >> 1;
+                    v = *reinterpret_cast<const uint4*>(in + (((size_t)n * Hh + (gy >> 1)) * Wh + (gx >> 1)) * Ca + c0 +
+                                                        half * 8);
+                } else {
+                    const int Cb = Cin - Ca;
+                    v = *reinterpret_cast<const uint4*>(in_b + (((size_t)n * H + gy) * W + gx) * Cb + (c0 - Ca) +
+                                                        half * 8);
+                }
+            }
             *reinterpret_cast<uint4*>(s_in + (ry * 18 + rx) * PIX_PAD + half * 8) = v;
         }
         // stage weights [tap][cout][16]
@@ -151,14 +166,15 @@ __global__ void __launch_bounds__(256) conv3x3_fwd_kernel(const __nv_bfloat16* _
 
 template <int COUT, int RPW>
 cudaError_t conv_fwd_t(const __nv_bfloat16* in, int N, int H, int W, int Cin, const __nv_bfloat16* w,
-                       const float* bias, int relu, void* out, int out_f32, cudaStream_t s) {
+                       const float* bias, int relu, void* out, int out_f32, cudaStream_t s,
+                       const __nv_bfloat16* in_b = nullptr, int Ca = 0) {
     constexpr int TH = 8 * RPW;
     const size_t smem = ((TH + 2) * 18 * PIX_PAD + 9 * COUT * PIX_PAD) * sizeof(__nv_bfloat16);
     auto k = conv3x3_fwd_kernel<COUT, RPW>;
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     dim3 grid((W + 15) / 16, (H + TH - 1) / TH, N);
-    k<<<grid, 256, smem, s>>>(in, N, H, W, Cin, w, bias, relu, out, out_f32);
+    k<<<grid, 256, smem, s>>>(in, N, H, W, Cin, w, bias, relu, out, out_f32, in_b, Ca);
     return cudaGetLastError();
 }
 
@@ -549,6 +565,25 @@ int vrc_nn_conv3x3_fwd(const void* in, int N, int H, int W, int Cin, const void*
         case 32: return status_of(conv_fwd_t<32, 2>(i, N, H, W, Cin, wt, bias, relu, out, out_f32, s));
         case 64: return status_of(conv_fwd_t<64, 2>(i, N, H, W, Cin, wt, bias, relu, out, out_f32, s));
         case 128: return status_of(conv_fwd_t<128, 1>(i, N, H, W, Cin, wt, bias, relu, out, out_f32, s));
+        default: return 4;
+    }
+}
+
+int vrc_nn_conv3x3_fwd_upcat(const void* a, int Ca, const void* b, int Cb, int N, int H, int W, const void* w,
+                             const float* bias, int Cout, int relu, void* out, int out_f32, void* stream) {
+    if (!a || !b || !w || !out || N < 1 || H < 2 || W < 2 || H % 2 || W % 2 || Ca < 16 || Ca % 16 || Cb < 16 ||
+        Cb % 16)
+        return 1;
+    const auto* ia = static_cast<const __nv_bfloat16*>(a);
+    const auto* ib = static_cast<const __nv_bfloat16*>(b);
+    const auto* wt = static_cast<const __nv_bfloat16*>(w);
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int Cin = Ca + Cb;
+    switch (Cout) {
+        case 16: return status_of(conv_fwd_t<16, 2>(ia, N, H, W, Cin, wt, bias, relu, out, out_f32, s, ib, Ca));
+        case 32: return status_of(conv_fwd_t<32, 2>(ia, N, H, W, Cin, wt, bias, relu, out, out_f32, s, ib, Ca));
+        case 64: return status_of(conv_fwd_t<64, 2>(ia, N, H, W, Cin, wt, bias, relu, out, out_f32, s, ib, Ca));
+        case 128: return status_of(conv_fwd_t<128, 1>(ia, N, H, W, Cin, wt, bias, relu, out, out_f32, s, ib, Ca));
         default: return 4;
     }
 }

@@ -144,9 +144,34 @@ class UNet:
         return y
 
     # -- forward / backward -----------------------------------------------------
+    def _conv_upcat(self, name, a_half, b, N, H, W):
+        """Decoder conv reading [up2(a_half) | b] on load (inference)."""
+        t = self.torch
+        _, cin, cout, relu = next(l for l in LAYERS if l[0] == name)
+        y = t.empty((N, H, W, cout), dtype=t.bfloat16, device=self.device)
+        _call("vrc_nn_conv3x3_fwd_upcat", _p(a_half), a_half.shape[3], _p(b), b.shape[3], N, H, W,
+              _p(self.w16[name]), _p(self.b[name]), cout, relu, _p(y), 0, _stream())
+        return y
+
+    def infer(self, x0, base, out=None):
+        """Forward without keeping activations; the decoder convolutions build
+        [upsample | skip] on load. Same values as forward()."""
+        t = self.torch
+        N, H, W, _ = x0.shape
+        e1 = self._conv("enc1b", self._conv("enc1a", x0, N, H, W), N, H, W)
+        e2 = self._conv("enc2b", self._conv("enc2a", self._pool(e1), N, H // 2, W // 2), N, H // 2, W // 2)
+        b2 = self._conv("botb", self._conv("bota", self._pool(e2), N, H // 4, W // 4), N, H // 4, W // 4)
+        d2 = self._conv("dec2b", self._conv_upcat("dec2a", b2, e2, N, H // 2, W // 2), N, H // 2, W // 2)
+        d1 = self._conv("dec1b", self._conv_upcat("dec1a", d2, e1, N, H, W), N, H, W)
+        f = self._conv("head", d1, N, H, W, out_f32=True)
+        if out is None:
+            out = t.empty((N, 2 * H, 2 * W, 4), dtype=t.float32, device=self.device)
+        _call("vrc_nn_head_fwd", _p(f), _p(base), N, H, W, _p(out), _stream())
+        return out
+
     def forward(self, x0, base):
         """x0: (N, h, w, 16) BF16; base: (N, h, w, 4) FP32 low-res RGBA.
-        Returns (N, 2h, 2w, 4) FP32."""
+        Returns (N, 2h, 2w, 4) FP32. Keeps the activations for backward()."""
         t = self.torch
         N, H, W, _ = x0.shape
         a = {"x0": x0, "base": base}
@@ -338,14 +363,26 @@ class LearnedRenderer:
     """Half-resolution, half-rate march -> U-Net -> full frame, with a probe:
     a probe x probe tile of the plain full-rate render is compared with the
     network's frame every call; if its PSNR falls below `psnr_bound` the frame
-    is rendered by the plain kernel instead (the fallback)."""
+    is rendered by the plain kernel instead (the fallback). Everything runs on
+    the context's stream; the only host synchronisation per frame is reading
+    the probe's error."""
 
     def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0):
         import torch
         self.ctx, self.net, self.probe, self.bound = ctx, net, probe, psnr_bound
+        self.stream = torch.cuda.ExternalStream(ctx.stream)
         self.err = torch.zeros(2, dtype=torch.float32, device="cuda")
         self.frames = 0
         self.fallbacks = 0
+        self._bufs = {}
+
+    def _buf(self, key, shape, dtype):
+        import torch
+        b = self._bufs.get(key)
+        if b is None or tuple(b.shape) != tuple(shape) or b.dtype != dtype:
+            b = torch.empty(shape, dtype=dtype, device="cuda")
+            self._bufs[key] = b
+        return b
 
     def probe_window(self, W, H):
         """A different probe tile each frame, walking a coarse grid of the image."""
@@ -354,26 +391,46 @@ class LearnedRenderer:
         k = (self.frames * 7919) % (nx * ny)
         return (k % nx) * p, (k // nx) * p, min(p, W), min(p, H)
 
+    def _render_plain(self, vol, tf, params, out, region=None):
+        from . import EE_ANALYTIC, OUT_RGBA32F, _check, lib
+        q = low_params(params, 1)
+        q.entry_exit_mode = EE_ANALYTIC
+        if region is not None:
+            q.region[:] = list(region)
+        _check(lib().vrc_render(self.ctx.handle, vol.handle, tf.handle, C.byref(q), None, None, 0, _p(out),
+                                OUT_RGBA32F, 1, None), self.ctx, "vrc_render")
+
     def render(self, vol, tf, params):
         """Returns (frame (H, W, 4) FP32 device tensor, info dict)."""
         import torch
+        from . import OUT_RGBA32F, _check, lib
         lp = low_params(params, 2)
-        rgba, aux, _ = march_aux(self.ctx, vol, tf, lp)
-        x0 = pack_input(rgba, aux)
-        out = self.net.forward(x0, rgba)[0]
-        x, y, w, h = self.probe_window(params.width, params.height)
-        ref, _ = plain_frame(self.ctx, vol, tf, params, region=(x, y, w, h))
-        self.err.zero_()
-        _call("vrc_nn_probe_error", _p(out), _p(ref), params.width, x, y, w, h, _p(self.err), _stream())
-        se, mx = self.err.tolist()
-        mse = se / (w * h * 4)
-        probe_psnr = float("inf") if mse == 0 else 10 * math.log10(1.0 / mse)
-        self.frames += 1
-        fallback = probe_psnr < self.bound
-        if fallback:
-            self.fallbacks += 1
-            out, _ = plain_frame(self.ctx, vol, tf, params)
-        return out, {"probe_psnr": probe_psnr, "probe_max_abs": mx, "fallback": fallback}
+        H, W = params.height, params.width
+        with torch.cuda.stream(self.stream):
+            rgba = self._buf("rgba", (1, lp.height, lp.width, 4), torch.float32)
+            aux = self._buf("aux", (1, lp.height, lp.width, 2), torch.float32)
+            _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None, _p(rgba),
+                                        OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
+            x0 = self._buf("x0", (1, lp.height, lp.width, 16), torch.bfloat16)
+            _call("vrc_nn_pack_input", _p(rgba), _p(aux), lp.height * lp.width, _p(x0), _stream())
+            out = self._buf("out", (1, H, W, 4), torch.float32)
+            self.net.infer(x0, rgba, out)
+            x, y, w, h = self.probe_window(W, H)
+            ref = self._buf("probe", (H, W, 4), torch.float32)
+            self._render_plain(vol, tf, params, ref, region=(x, y, w, h))
+            self.err.zero_()
+            _call("vrc_nn_probe_error", _p(out), _p(ref), W, x, y, w, h, _p(self.err), _stream())
+            se, mx = self.err.tolist()  # the one synchronisation
+            mse = se / (w * h * 4)
+            probe_psnr = float("inf") if mse == 0 else 10 * math.log10(1.0 / mse)
+            self.frames += 1
+            fallback = probe_psnr < self.bound
+            frame = out[0]
+            if fallback:
+                self.fallbacks += 1
+                frame = self._buf("fallback", (H, W, 4), torch.float32)
+                self._render_plain(vol, tf, params, frame)
+        return frame, {"probe_psnr": probe_psnr, "probe_max_abs": mx, "fallback": fallback}
 
 
 # ---- training on pairs the plain raycaster renders ---------------------------
