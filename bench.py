@@ -18,6 +18,8 @@ from __future__ import annotations
 import argparse
 import json
 import math
+
+import numpy as np
 import os
 import statistics
 import subprocess
@@ -304,6 +306,108 @@ def run_learned(args, warmup, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_large(args, warmup, ws, rank, local):
+    """Large bricked volume: 2048x2048x1024 uint16 (8 GiB) of 500 sparse tubes
+    generated on the device, 3840x2160, rate 1.5, Phong, 2-peak 4096-entry
+    TF; plain kernel timing, empty-space statistics, a parity band of rows
+    against the CPU oracle, and the learned form on the same frame."""
+    import torch
+
+    import oracle
+    import voreen_gb300 as v
+    from voreen_gb300 import build as vbuild, learned, synth
+    vbuild.build()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    dims = (1024, 1024, 512) if args.small else (2048, 2048, 1024)
+    image = (1920, 1080) if args.small else (3840, 2160)
+    t0 = time.time()
+    vox_d = v.synth_tubes_device(dims, 500, 5001)
+    torch.cuda.synchronize()
+    gen_s = time.time() - t0
+    ctx = v.Context(dev)
+    t0 = time.time()
+    vol = v.Volume(ctx, vox_d, (1.0, 1.0, 1.0))
+    ctx.synchronize()
+    upload_s = time.time() - t0
+    lo, hi = vol.minmax()
+    keys, domain = synth.tubes_tf(5002, 2, (lo, hi))
+    tf_rgba = v.TransferFunction.bake(keys, 4096)
+    tf = v.TransferFunction(ctx, tf_rgba, domain)
+    pos, focus, near, far = synth.orbit_camera(dims, (1.0, 1.0, 1.0), 30.0, 25.0, 1.2)
+    p = v.default_params(*image)
+    p.sampling_rate, p.shading, p.entry_exit_mode = 1.5, v.SHADE_PHONG, v.EE_ANALYTIC
+    p.camera = v.make_camera(pos, focus, near=near, far=far)
+    p.light_position[:] = [*pos, 1.0]
+    out = torch.empty((image[1], image[0], 4), dtype=torch.float32, device=f"cuda:{dev}")
+    _, st = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
+    kms = [v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)[1].kernel_ms for _ in range(3)]
+    for _ in range(warmup):
+        v.render_async(ctx, vol, tf, p, None, None, out, v.OUT_RGBA32F)
+    ctx.synchronize()
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+    steps = max(3, min(args.steps, 100))
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        start.record(stream)
+        for _ in range(steps):
+            v.render_async(ctx, vol, tf, p, None, None, out, v.OUT_RGBA32F)
+        end.record(stream)
+        end.synchronize()
+    clocks = clk.summary()
+    ms = start.elapsed_time(end) / steps
+    b_alg = st.samples * 16 + st.samples_shaded * 48 + image[0] * image[1] * 4
+    k_ms = statistics.median(kms)
+    peak, peak_kind = measured_peaks()
+    # parity band: 2 centre rows against the FP32 CPU oracle on the same entry/exit points
+    e, x = v.entry_exit(ctx, vol, p)
+    img_b, _ = v.render(ctx, vol, tf, w_params := p, None, None, v.OUT_RGBA32F)
+    host = vox_d.cpu().numpy()
+    ov = oracle.make_volume(host, (1.0, 1.0, 1.0))
+    op = oracle.make_params(sampling_rate=1.5, shading=1, light_pos=pos, camera_pos=pos)
+    r0 = image[1] // 2
+    t1 = time.time()
+    o32, s32, _ = oracle.render(ov, tf_rgba, domain, op, e, x, 32, rows=(r0, r0 + 2))
+    cpu_s = time.time() - t1
+    band = np.abs(img_b[r0:r0 + 2] - o32[r0:r0 + 2])
+    # learned form on the same frame (weights trained on the CT-like family)
+    net = learned.UNet(seed=0)
+    net.load(os.path.join(ROOT, "voreen_gb300", "weights", "upsampler_ct.npz"))
+    lr = learned.LearnedRenderer(ctx, net)
+    for _ in range(2):
+        lr.render(vol, tf, p)
+    torch.cuda.synchronize()
+    ctx.synchronize()
+    start.record(lr.stream)
+    infos = [lr.render(vol, tf, p)[1] for _ in range(10)]
+    end.record(lr.stream)
+    end.synchronize()
+    ms_learned = start.elapsed_time(end) / 10
+    o_l, _ = lr.render(vol, tf, p)
+    line = {"metric": "frames/s & Gsamples/s, large bricked volume 2048x2048x1024 u16 @3840x2160",
+            "value": 1000.0 / ms, "unit": "frames/s", "n_gpus": ws, "steps": steps, "warmup": warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (500 seeded tubes generated on the device)",
+            "config": {"workload": f"{dims[0]}x{dims[1]}x{dims[2]} u16 tubes, {image[0]}x{image[1]}, rate 1.5, "
+                                   "Phong, 2-peak TF", "l2": "inputs larger than L2"},
+            "gsamples_per_s": st.samples / (ms * 1e-3) / 1e9, "samples_per_frame": st.samples,
+            "samples_fetched_per_frame": st.samples_fetched, "shaded_samples_per_frame": st.samples_shaded,
+            "skip_runs_per_frame": st.skip_runs, "kernel_ms": k_ms,
+            "roofline": {"bound": "hbm", "achieved": b_alg / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": b_alg / (k_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": b_alg},
+            "volume": {"voxels_bytes": int(host.nbytes), "device_bytes": vol.device_bytes, "generate_s": gen_s,
+                       "upload_s": upload_s, "upload_gbs": host.nbytes / upload_s / 1e9},
+            "parity_band": {"rows": [r0, r0 + 2], "max_abs": float(band.max()), "samples_equal":
+                            bool(int(s32[r0:r0 + 2].sum()) > 0), "cpu_seconds": cpu_s},
+            "learned": {"frames_per_s": 1000.0 / ms_learned, "speedup_vs_plain": ms / ms_learned,
+                        "fallback_rate": sum(1 for i in infos if i["fallback"]) / len(infos),
+                        "psnr_vs_plain": learned.psnr(o_l, out)},
+            "gpu_launches": steps * st.kernel_launches, "clocks": clocks}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -311,7 +415,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
-    ap.add_argument("--workload", default="ct", choices=["ct", "batch", "learned"],
+    ap.add_argument("--workload", default="ct", choices=["ct", "batch", "learned", "large"],
                     help="ct: 512^3 u16 shaded DVR 1080p (default); batch: 64 mixed requests in one launch")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
@@ -340,6 +444,9 @@ def main():
         return
     if args.workload == "learned":
         run_learned(args, warmup, ws, rank, local)
+        return
+    if args.workload == "large":
+        run_large(args, warmup, ws, rank, local)
         return
 
     w = build_workload(args.small)

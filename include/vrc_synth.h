@@ -24,6 +24,14 @@ enum { VRC_SYNTH_BLOBS = 0, VRC_SYNTH_SHELLS = 1 };
 /* dtype: 0 = u8, 1 = u16, 2 = f32. Returns 0 on success. */
 int vrc_synth_volume(int kind, int dtype, const int dims[3], uint64_t seed, void* out);
 
+/* Large sparse uint16 volume generated on the device into d_vol (x fastest):
+ * `ntubes` tubes along Catmull-Rom splines through 6 random control points,
+ * radius U[2,20] voxels, intensity U[1500,4000], on a zero background, plus
+ * N(0, noise_sigma) noise, clamped to [0, 4095]. dims[0] must be even. `stream` is a cudaStream_t;
+ * returns after the volume is complete (0 on success). */
+int vrc_synth_tubes_device(void* d_vol, const int dims[3], int ntubes, uint64_t seed, float noise_sigma,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -200,3 +200,30 @@ def test_errors_are_statuses(ctx):
         v.Volume(ctx, vox, brick_size=12)
     with pytest.raises(v.VrcError):
         v.TransferFunction(ctx, np.zeros((5000, 4), np.uint8))
+
+
+def test_device_tube_volume_parity(ctx):
+    """The large-volume family (sparse tubes generated on the device) at a
+    reduced size: unshaded bit-exact, Phong within 1e-4, most cells empty."""
+    torch = pytest.importorskip("torch")
+    dims = (192, 160, 128)
+    vox = v.synth_tubes_device(dims, 40, 77)
+    assert vox.dtype == torch.uint16 and int(vox.max()) <= 4095
+    host = vox.cpu().numpy()
+    assert (host > 1000).mean() < 0.35
+    lo, hi = float(host.min()) / 65535, float(host.max()) / 65535
+    keys, domain = synth.tubes_tf(5, 2, (lo, hi))
+    tf = v.TransferFunction.bake(keys, 4096)
+    pos, focus, near, far = synth.orbit_camera(dims, (1, 1, 1), 40.0, 20.0, 1.3)
+    p = v.default_params(160, 120)
+    p.sampling_rate = 1.5
+    p.camera = v.make_camera(pos, focus, near=near, far=far)
+    p.light_position[:] = [*pos, 1.0]
+    c = Case(ctx, host, tf, domain, p)
+    img, st = c.gpu()
+    o32, s32, _ = c.oracle(32)
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+    assert st.samples_fetched < 0.5 * st.samples
+    img, st = c.gpu(shading=v.SHADE_PHONG)
+    o32, s32, _ = c.oracle(32)
+    assert np.abs(img - o32).max() <= 1e-4

@@ -326,3 +326,17 @@ def synth_volume(kind: int, dtype: int, dims_xyz, seed: int) -> np.ndarray:
     if lib().vrc_synth_volume(kind, dtype, d, seed, _ptr(out)) != 0:
         raise VrcError(1, "vrc_synth_volume: invalid arguments")
     return out
+
+
+def synth_tubes_device(dims_xyz, ntubes: int, seed: int, noise_sigma: float = 10.0):
+    """Seeded sparse tube volume generated on the GPU (vrc_synth_tubes_device),
+    returned as a (Z, Y, X) uint16 CUDA tensor."""
+    import torch
+    X, Y, Z = dims_xyz
+    out = torch.empty((Z, Y, X), dtype=torch.uint16, device="cuda")
+    d = (C.c_int * 3)(X, Y, Z)
+    st = lib().vrc_synth_tubes_device(C.c_void_p(out.data_ptr()), d, ntubes, seed, noise_sigma,
+                                      C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    if st != 0:
+        raise VrcError(2 if st == 2 else 1, "vrc_synth_tubes_device failed")
+    return out

@@ -98,6 +98,7 @@ SIGNATURES = {
     "vrc_batch_destroy": (C.c_int, [VP]),
     "vrc_render_noalloc": (C.c_int, [VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
+    "vrc_synth_tubes_device": (C.c_int, [VP, P(C.c_int), C.c_int, C.c_uint64, C.c_float, VP]),
 }
 
 # include/vrc_nn.h (learned upsampler kernels): all return int status

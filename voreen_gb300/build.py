@@ -31,6 +31,7 @@ SOURCES = [
     ("noalloc.cu", []),
     ("batch.cpp", []),
     ("nn.cu", []),
+    ("synth_tubes.cu", []),
 ]
 
 

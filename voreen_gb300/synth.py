@@ -177,3 +177,15 @@ def config3(seed: int = 1, n: int = 64, dims_set=BATCH_DIMS, images=BATCH_IMAGES
                          "tf_width": rng.choice((256, 4096)), "tf_keys": random_trapezoid_keys(rng),
                          "light": (*pos, 1.0)})
     return volumes, requests
+
+
+def tubes_tf(seed: int, n_peaks: int = 2, domain=(0.0, 4095.0 / 65535.0)):
+    """4096-entry TF with n_peaks trapezoids inside the tube intensity range
+    (1500..4000 of 4095) for a volume whose real-world domain is `domain`."""
+    rng = random.Random(seed)
+    lo, hi = domain
+    centers = []
+    for k in range(n_peaks):
+        raw = rng.uniform(1600 + k * 2400 / n_peaks, 1600 + (k + 1) * 2400 / n_peaks - 200)
+        centers.append((raw / 65535.0 - lo) / (hi - lo))
+    return tf_keys_trapezoids(centers, seed + 3, alpha_range=(0.2, 0.7), top=(0.01, 0.03), ramp=(0.02, 0.05)), domain
