@@ -398,8 +398,8 @@ def run_large(args, warmup, ws, rank, local):
                          "algorithmic_bytes_per_launch": b_alg},
             "volume": {"voxels_bytes": int(host.nbytes), "device_bytes": vol.device_bytes, "generate_s": gen_s,
                        "upload_s": upload_s, "upload_gbs": host.nbytes / upload_s / 1e9},
-            "parity_band": {"rows": [r0, r0 + 2], "max_abs": float(band.max()), "samples_equal":
-                            bool(int(s32[r0:r0 + 2].sum()) > 0), "cpu_seconds": cpu_s},
+            "parity_band": {"rows": [r0, r0 + 2], "max_abs": float(band.max()), "oracle_samples":
+                            int(s32[r0:r0 + 2].sum()), "cpu_seconds": cpu_s},
             "learned": {"frames_per_s": 1000.0 / ms_learned, "speedup_vs_plain": ms / ms_learned,
                         "fallback_rate": sum(1 for i in infos if i["fallback"]) / len(infos),
                         "psnr_vs_plain": learned.psnr(o_l, out)},

@@ -208,8 +208,9 @@ def test_device_tube_volume_parity(ctx):
     torch = pytest.importorskip("torch")
     dims = (192, 160, 128)
     vox = v.synth_tubes_device(dims, 40, 77)
-    assert vox.dtype == torch.uint16 and int(vox.max()) <= 4095
+    assert vox.dtype == torch.uint16
     host = vox.cpu().numpy()
+    assert host.max() <= 4095
     assert (host > 1000).mean() < 0.35
     lo, hi = float(host.min()) / 65535, float(host.max()) / 65535
     keys, domain = synth.tubes_tf(5, 2, (lo, hi))
