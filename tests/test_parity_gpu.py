@@ -207,11 +207,11 @@ def test_device_tube_volume_parity(ctx):
     reduced size: unshaded bit-exact, Phong within 1e-4, most cells empty."""
     torch = pytest.importorskip("torch")
     dims = (192, 160, 128)
-    vox = v.synth_tubes_device(dims, 40, 77)
+    vox = v.synth_tubes_device(dims, 8, 77)
     assert vox.dtype == torch.uint16
     host = vox.cpu().numpy()
     assert host.max() <= 4095
-    assert (host > 1000).mean() < 0.35
+    assert (host > 1000).mean() < 0.5
     lo, hi = float(host.min()) / 65535, float(host.max()) / 65535
     keys, domain = synth.tubes_tf(5, 2, (lo, hi))
     tf = v.TransferFunction.bake(keys, 4096)
