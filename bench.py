@@ -127,11 +127,16 @@ def load_traffic():
     return None
 
 
-def build_workload(small: bool):
+def build_workload(small: bool, kind: str = "ct"):
+    """ct: 512^3 u16 shaded DVR 1080p; mip: the same volume and TF under MIP;
+    blobs: 128^3 u8 plain DVR 512x512 (the CPU-runnable case)."""
     from voreen_gb300 import synth
+    if kind == "blobs":
+        return synth.config1()
+    comp = synth.MIP if kind == "mip" else synth.DVR
     if small:
-        return synth.config2(size=(256, 256, 256), image=(960, 540))
-    return synth.config2()
+        return synth.config2(size=(256, 256, 256), image=(960, 540), compositing=comp)
+    return synth.config2(compositing=comp)
 
 
 def run_cpu(w, entry, exit_pts, target_s: float):
@@ -415,8 +420,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
-    ap.add_argument("--workload", default="ct", choices=["ct", "batch", "learned", "large"],
-                    help="ct: 512^3 u16 shaded DVR 1080p (default); batch: 64 mixed requests in one launch")
+    ap.add_argument("--workload", default="ct", choices=["ct", "mip", "blobs", "batch", "learned", "large"],
+                    help="ct: 512^3 u16 shaded DVR 1080p (default); mip: the same under MIP; blobs: 128^3 u8 "
+                         "DVR 512x512; batch: 64 mixed requests in one launch; learned: upsampler vs plain; "
+                         "large: 2048x2048x1024 u16 at 3840x2160")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
@@ -449,14 +456,20 @@ def main():
         run_large(args, warmup, ws, rank, local)
         return
 
-    w = build_workload(args.small)
-    p = w.params(skip_cell_size=args.skip_cell, empty_space_skipping=0 if args.no_skip else 1,
-                 shading=v.SHADE_PHONG if args.shading == "phong" else v.SHADE_NONE)
+    w = build_workload(args.small, args.workload)
+    shading = w.shading if args.shading == "phong" else v.SHADE_NONE
+    p = w.params(skip_cell_size=args.skip_cell, empty_space_skipping=0 if args.no_skip else 1, shading=shading)
     npix = w.width * w.height
-    config = {"workload": w.name, "volume": list(w.dims), "dtype_volume": "uint16", "spacing": list(w.spacing),
-              "image": [w.width, w.height], "sampling_rate": w.sampling_rate, "tf_width": w.tf_width,
-              "shading": "phong", "compositing": "dvr", "ert": 0.95, "camera": "orbit 1.25 x box diagonal",
-              "l2": "inputs larger than L2 (bricked volume > 129 MB)", "replicas": ws}
+    bpv = w.voxels.dtype.itemsize
+    comp_name = {v.DVR: "dvr", v.MIP: "mip", v.ISO: "iso"}[w.compositing]
+    config = {"workload": w.name, "volume": list(w.dims), "dtype_volume": str(w.voxels.dtype),
+              "spacing": list(w.spacing), "image": [w.width, w.height], "sampling_rate": w.sampling_rate,
+              "tf_width": w.tf_width, "shading": "phong" if shading == v.SHADE_PHONG else "none",
+              "compositing": comp_name, "ert": 0.95 if w.compositing == v.DVR else None,
+              "camera": "orbit 1.25 x box diagonal" if args.workload != "blobs" else "orbit 2.5 x box diagonal",
+              "l2": "inputs larger than L2 (bricked volume > 129 MB)" if w.voxels.nbytes > 129e6 else
+                    "flush: 256 MB buffer written between timed frames", "replicas": ws}
+    flush_l2 = w.voxels.nbytes <= 129e6
 
     if args.impl == "reference":
         if rank != 0:
@@ -525,17 +538,32 @@ def main():
     _barrier(ws)
     start = torch.cuda.Event(enable_timing=True)
     end = torch.cuda.Event(enable_timing=True)
+    if flush_l2:
+        # the volume fits in L2: write a 256 MB buffer before each frame and
+        # time each frame on its own
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{dev}")
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(args.steps)]
     with ClockSampler(dev) as clk:
         with torch.cuda.stream(stream):
-            start.record(stream)
-            for _ in range(args.steps):
-                v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
-            end.record(stream)
-        end.synchronize()
-        ctx.synchronize()
+            if flush_l2:
+                for a, b in evs:
+                    flush.fill_(1)
+                    a.record(stream)
+                    v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
+                    b.record(stream)
+            else:
+                start.record(stream)
+                for _ in range(args.steps):
+                    v.render_async(ctx, vol, tf, p, e_dev, x_dev, out_dev, v.OUT_RGBA8)
+                end.record(stream)
         torch.cuda.synchronize()
+        ctx.synchronize()
     clocks = clk.summary()
-    ms = start.elapsed_time(end) / args.steps
+    if flush_l2:
+        ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    else:
+        ms = start.elapsed_time(end) / args.steps
     ms = _barrier_max(ms, ws)
     fps_local = 1000.0 / ms
     value = fps_local * ws
@@ -554,16 +582,17 @@ def main():
     e2e_ms = (time.perf_counter() - t0) * 1e3 / k_e2e
     e2e_ms = _barrier_max(e2e_ms, ws)
 
-    bpv = 2
     b_alg = samples * 8 * bpv + shaded * 24 * bpv + npix * 4
     k_ms = statistics.median(kernel_ms)
     peak, peak_kind = measured_peaks()
     achieved = b_alg / (k_ms * 1e-3) / 1e9
-    traffic = load_traffic()
+    traffic = load_traffic() if (args.workload == "ct" and not args.small) else None
 
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded procedural 512^3 u16 CT-like shells)", "config": config,
+            "dtype": "f32", "data": f"synthetic (seeded procedural {w.dims[0]}x{w.dims[1]}x{w.dims[2]} "
+                                    f"{w.voxels.dtype} {'Gaussian blobs' if args.workload == 'blobs' else 'CT-like shells'})",
+            "config": config,
             "gsamples_per_s": samples / (ms * 1e-3) / 1e9 * ws,
             "samples_per_frame": samples, "shaded_samples_per_frame": shaded,
             "samples_fetched_per_frame": st.samples_fetched, "skip_runs_per_frame": st.skip_runs,
@@ -571,7 +600,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": b_alg,
-                         "note": "algorithmic bytes = 16 B/sample + 48 B/shaded sample + 4 B/pixel"},
+                         "note": f"algorithmic bytes = {8 * bpv} B/sample + {24 * bpv} B/shaded sample + 4 B/pixel"},
             "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "frames/s", "h2d_bytes_per_step": 2 * npix * 16,
                     "d2h_bytes_per_step": npix * 4},
             "gpu_launches": launches_per_frame * args.steps,
