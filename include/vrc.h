@@ -30,6 +30,13 @@
  *                       modules/base/processors/proxygeometry/optimizedproxygeometry.cpp:420-448
  *   vrc_camera_matrices tgt::Camera::getViewMatrix / getProjectionMatrix
  *                       ext/tgt/camera.cpp:133-216, ext/tgt/matrix.h:1196-1248
+ *   vrc_preint_*        PreIntegrationTable::computeTable / classify and the
+ *                       table map's resolution rule
+ *                       src/core/datastructures/transfunc/1d/preintegrationtable.cpp:67-204, 256-279,
+ *                       src/core/datastructures/transfunc/1d/preintegrationtablemap.cpp:59-69
+ *   vrc_tf_set_preintegration  TransFunc1D::getPreIntegrationTable as CPURaycaster
+ *                       calls it, transfunc1d.cpp:121-128, cpuraycaster.cpp:112-123
+ *   vrc_sampling_step   VolumeRaycaster::getSamplingStepSize / cpuraycaster.cpp:104
  *
  * Conventions: images are row-major with row 0 at the bottom (OpenGL window
  * coordinates); entry/exit points are texture-space float4 (w = 1 on hit, the
@@ -59,7 +66,25 @@ typedef enum {
 } vrc_status;
 
 typedef enum { VRC_U8 = 0, VRC_U16 = 1, VRC_F32 = 2 } vrc_dtype;
-typedef enum { VRC_DVR = 0, VRC_MIP = 1, VRC_ISO = 2 } vrc_compositing;
+/* Compositing ("compositing"): dvr, mip, iso as both CPURaycaster and the GLSL
+ * raycaster do them; mop (maximum opacity), mida (maximum intensity difference
+ * accumulation, "gammaValue"), fhp (first-hit position) and fhn (first-hit
+ * normal) as mod_compositing.frag:97-214 does them. mip, mop and mida run
+ * without early ray termination (volumeraycaster.cpp:226-228). */
+typedef enum {
+    VRC_DVR = 0,
+    VRC_MIP = 1,
+    VRC_ISO = 2,
+    VRC_MOP = 3,
+    VRC_MIDA = 4,
+    VRC_FHP = 5,
+    VRC_FHN = 6
+} vrc_compositing;
+/* Classification ("classification"): the 1D TF table, or the pre-integration
+ * table attached to the TF (vrc_tf_set_preintegration) -- CPURaycaster's
+ * "pre-integrated-cpu" / "pre-integrated-approximation" (cpuraycaster.cpp:112-123,
+ * 255-261); DVR compositing only. */
+typedef enum { VRC_CLASSIFY_TF = 0, VRC_CLASSIFY_PREINTEGRATED = 1 } vrc_classification;
 typedef enum { VRC_SHADE_NONE = 0, VRC_SHADE_PHONG = 1 } vrc_shading;
 typedef enum { VRC_OUT_RGBA8 = 0, VRC_OUT_RGBA32F = 1, VRC_OUT_RGBA16 = 2 } vrc_out_format;
 typedef enum { VRC_EE_BUFFERS = 0, VRC_EE_ANALYTIC = 1 } vrc_entry_exit_mode;
@@ -122,6 +147,37 @@ vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float
                          vrc_tf** out);
 vrc_status vrc_tf_destroy(vrc_tf* tf);
 
+/* ---- pre-integrated classification --------------------------------------
+ * PreIntegrationTable (src/core/datastructures/transfunc/1d/preintegrationtable.cpp):
+ * an res x res RGBA table, entry [back * res + front] = the TF integrated
+ * between the previous sample's TF coordinate (front) and the current one
+ * (back) over one sampling step. */
+typedef struct vrc_preint vrc_preint;
+
+/* Table resolution: `requested` if > 0, else min(TF width, 1024)
+ * (PreIntegrationTableMap::getPreIntegrationTable, preintegrationtablemap.cpp:64-69). */
+int vrc_preint_resolution(int tf_width, int requested);
+/* Host-only: the TF sampled at `res` entries as PreIntegrationTable::computeTable
+ * does (preintegrationtable.cpp:71-104): entry i = the keys' RGBA8 mapping at
+ * gamma(i / (res - 1)), zero for i < iround(threshold_lo * res) and for
+ * i >= iround(threshold_hi * res). */
+vrc_status vrc_preint_bake_source(const vrc_tf_key* keys, int nkeys, int res, float gamma, float threshold_lo,
+                                  float threshold_hi, uint8_t* out_rgba);
+/* Builds the table for sampling step `step` (vrc_sampling_step) on the
+ * device from the res x RGBA8 source. use_integral = 0: the exact table
+ * (composited entry by entry, O(res^3), built by a CUDA kernel); 1: the
+ * integral-function approximation (O(res^2), built on the host). 2 <= res <= 4096. */
+vrc_status vrc_preint_create(vrc_context* ctx, const uint8_t* source_rgba, int res, float step, int use_integral,
+                             vrc_preint** out);
+/* Copies the table to the host: res * res * 4 floats, entry [back * res + front]. */
+vrc_status vrc_preint_download(const vrc_preint* t, float* out_rgba);
+vrc_status vrc_preint_destroy(vrc_preint* t);
+/* Attaches `t` to `tf` for renders with classification VRC_CLASSIFY_PREINTEGRATED
+ * (NULL detaches). The table must outlive its use by the TF. */
+vrc_status vrc_tf_set_preintegration(vrc_tf* tf, const vrc_preint* t);
+/* samplingStepSize = 1 / (max(dim) * samplingRate) (cpuraycaster.cpp:104), as the march uses it. */
+float vrc_sampling_step(const vrc_volume* vol, float sampling_rate);
+
 /* ---- camera ------------------------------------------------------------ */
 typedef struct {
     float position[3], focus[3], up[3];  /* world coordinates */
@@ -157,7 +213,8 @@ typedef struct {
     int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (8), else 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
     int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
-    int reserved[2];
+    int classification;         /* vrc_classification, default VRC_CLASSIFY_TF */
+    float mida_gamma;           /* "gammaValue" for VRC_MIDA, in [-1, 1], default 0 */
 } vrc_render_params;
 
 /* Fills `p` with the reference's property defaults for a W x H image. */

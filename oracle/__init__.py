@@ -22,7 +22,7 @@ import numpy as np
 from . import build as _build
 
 U8, U16, F32 = 0, 1, 2
-DVR, MIP, ISO = 0, 1, 2
+DVR, MIP, ISO, MOP, MIDA, FHP, FHN = 0, 1, 2, 3, 4, 5, 6
 SHADE_NONE, SHADE_PHONG = 0, 1
 _DT = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
 
@@ -41,7 +41,8 @@ class OrcParams(C.Structure):
                 ("iso_value", C.c_float), ("ert_threshold", C.c_float), ("light_pos_phys", C.c_float * 3),
                 ("camera_pos_phys", C.c_float * 3), ("light_ambient", C.c_float * 3),
                 ("light_diffuse", C.c_float * 3), ("light_specular", C.c_float * 3), ("shininess", C.c_float),
-                ("apply_attenuation", C.c_int), ("attenuation", C.c_float * 3)]
+                ("apply_attenuation", C.c_int), ("attenuation", C.c_float * 3), ("mida_gamma", C.c_float),
+                ("preint", C.c_void_p), ("preint_res", C.c_int)]
 
 
 class OrcTFKey(C.Structure):
@@ -58,6 +59,9 @@ def lib():
         L = C.CDLL(path)
         P = C.POINTER
         L.oracle_bake_tf_keys.argtypes = [P(OrcTFKey), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_void_p]
+        L.oracle_preint_source.argtypes = [P(OrcTFKey), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                           C.c_void_p]
+        L.oracle_preint_table.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_void_p]
         L.oracle_entry_exit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         for name in ("oracle_render_f32", "oracle_render_f64"):
             getattr(L, name).argtypes = [P(OrcVolume), P(OrcTF), P(OrcParams), C.c_void_p, C.c_void_p, C.c_int,
@@ -88,8 +92,18 @@ def make_volume(vox: np.ndarray, spacing=(1, 1, 1), offset=(0, 0, 0), rwm=(1.0, 
 
 def make_params(sampling_rate=2.0, compositing=DVR, shading=SHADE_NONE, iso_value=0.5, ert=0.95,
                 light_pos=(2.3, 1.5, 1.5), camera_pos=(0, 0, 3), ambient=(0.4,) * 3, diffuse=(0.8,) * 3,
-                specular=(0.6,) * 3, shininess=60.0, attenuation=None) -> OrcParams:
+                specular=(0.6,) * 3, shininess=60.0, attenuation=None, mida_gamma=0.0,
+                preint_table: np.ndarray | None = None) -> OrcParams:
+    """preint_table: (res, res, 4) float32 pre-integration table ([back, front]),
+    None = classification by the TF."""
     p = OrcParams()
+    p.mida_gamma = mida_gamma
+    if preint_table is not None:
+        t = np.ascontiguousarray(preint_table, dtype=np.float32)
+        assert t.ndim == 3 and t.shape[0] == t.shape[1] and t.shape[2] == 4
+        p.preint = t.ctypes.data
+        p.preint_res = t.shape[0]
+        p._keep = t
     p.sampling_rate = sampling_rate
     p.compositing = compositing
     p.shading = shading
@@ -115,6 +129,31 @@ def bake_tf(keys, width, gamma=1.0, threshold=(0.0, 1.0)) -> np.ndarray:
         arr[i].color_r[:] = list(k[2] if len(k) > 2 else k[1])
     out = np.zeros((width, 4), np.uint8)
     lib().oracle_bake_tf_keys(arr, len(keys), width, gamma, threshold[0], threshold[1], _ptr(out))
+    return out
+
+
+def _keys(keys):
+    arr = (OrcTFKey * max(1, len(keys)))()
+    for i, k in enumerate(keys):
+        arr[i].intensity = k[0]
+        arr[i].color_l[:] = list(k[1])
+        arr[i].color_r[:] = list(k[2] if len(k) > 2 else k[1])
+    return arr
+
+
+def preint_source(keys, res, gamma=1.0, threshold=(0.0, 1.0)) -> np.ndarray:
+    """The TF sampled at `res` entries as the pre-integration table build does."""
+    out = np.zeros((res, 4), np.uint8)
+    lib().oracle_preint_source(_keys(keys), len(keys), res, gamma, threshold[0], threshold[1], _ptr(out))
+    return out
+
+
+def preint_table(source_rgba: np.ndarray, step: float, use_integral: bool = False) -> np.ndarray:
+    """(res, res, 4) float32 table, [back, front] (PreIntegrationTable::computeTable)."""
+    src = np.ascontiguousarray(source_rgba, dtype=np.uint8)
+    res = src.shape[0]
+    out = np.zeros((res, res, 4), np.float32)
+    lib().oracle_preint_table(_ptr(src), res, step, 1 if use_integral else 0, _ptr(out))
     return out
 
 

@@ -25,6 +25,11 @@
  * and the GLSL-only rules of SingleVolumeRaycaster:
  *   rayTraversal                          modules/base/glsl/rc_singlevolume.frag:116-312
  *   compositeDVR / MIP / ISO              modules/core/glsl/modules/mod_compositing.frag:47-59, 85-95, 156-166
+ *   compositeMOP / MIDA / FHP / FHN       mod_compositing.frag:97-146, 168-196; no early ray
+ *                                         termination for mip/mop/mida (volumeraycaster.cpp:226-228)
+ *   pre-integrated classification         cpuraycaster.cpp:255-261 (classify(last, cur), no opacity
+ *                                         correction), PreIntegrationTable::computeTable / classify
+ *                                         src/core/datastructures/transfunc/1d/preintegrationtable.cpp:67-204, 256-279
  *   calcGradientA / fixClipBorderGradient modules/core/glsl/modules/mod_gradients.frag:202-214, 39-46
  *   phongShading and its terms            modules/core/glsl/modules/mod_shading.frag:52-151
  *   texToPhysical                         modules/core/glsl/modules/mod_sampler3d.frag:179-181
@@ -251,7 +256,12 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
         dir = v3<R>(dir.x * rl, dir.y * rl, dir.z * rl);
     }
     const R ert = R(p->ert_threshold);
-    const bool use_ert = p->compositing != ORC_MIP;  /* MIP runs without ERT */
+    const int comp = p->compositing;
+    /* no early ray termination for mip / mop / mida (volumeraycaster.cpp:226-228) */
+    const bool use_ert = comp != ORC_MIP && comp != ORC_MOP && comp != ORC_MIDA;
+    const bool preint = p->preint != nullptr;
+    const int pres = p->preint_res;
+    R last_int = R(0);  /* lastIntensity, cpuraycaster.cpp:235 */
     const R lo = R(tf->domain_lo), hi = R(tf->domain_hi);
     const R rs = R(v->rwm_scale), ro = R(v->rwm_offset);
     const R kcorr = step * R(200);  /* SAMPLING_BASE_INTERVAL_RCP */
@@ -264,12 +274,24 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
         const V3<R> s = v3<R>(first.x + t * dir.x, first.y + t * dir.y, first.z + t * dir.z);
         const R intensity = sample_tex<R>(v, s.x, s.y, s.z);
         const R rw = intensity * rs + ro;
-        const int idx = tf_index<R>(rw_to_tf<R>(rw, lo, hi), tf->width);
-        const uint8_t* e = tf->rgba + 4 * idx;
-        R col[4] = {R(e[0]) / R(255), R(e[1]) / R(255), R(e[2]) / R(255), R(e[3]) / R(255)};
+        R col[4];
+        if (preint) {
+            /* PreIntegrationTable::classify(last, cur) (preintegrationtable.cpp:256-279) */
+            const R cur = rw_to_tf<R>(rw, lo, hi);
+            const int i1 = tf_index<R>(last_int, pres), i2 = tf_index<R>(cur, pres);
+            const float* e = p->preint + 4 * (size_t(i2) * size_t(pres) + size_t(i1));
+            for (int k = 0; k < 4; ++k) col[k] = R(e[k]);
+            last_int = cur;
+        } else {
+            const int idx = tf_index<R>(rw_to_tf<R>(rw, lo, hi), tf->width);
+            const uint8_t* e = tf->rgba + 4 * idx;
+            for (int k = 0; k < 4; ++k) col[k] = R(e[k]) / R(255);
+        }
         if (col[3] > R(0)) {
+            V3<R> g = v3<R>(0, 0, 0);
+            if (p->shading == ORC_SHADE_PHONG || comp == ORC_FHN)
+                g = (t == R(0)) ? clip_border_gradient<R>(c, s, dir, px, py) : calc_gradient<R>(c, s.x, s.y, s.z);
             if (p->shading == ORC_SHADE_PHONG) {
-                const V3<R> g = (t == R(0)) ? clip_border_gradient<R>(c, s, dir, px, py) : calc_gradient<R>(c, s.x, s.y, s.z);
                 /* texToPhysical (mod_sampler3d.frag:179-181) */
                 const V3<R> pos = v3<R>((s.x * c.dimf[0] - R(0.5)) * R(v->spacing[0]) + R(v->offset[0]),
                                         (s.y * c.dimf[1] - R(0.5)) * R(v->spacing[1]) + R(v->offset[1]),
@@ -277,9 +299,10 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
                 const V3<R> sh = phong<R>(c, g, pos, v3<R>(col[0], col[1], col[2]));
                 col[0] = sh.x; col[1] = sh.y; col[2] = sh.z;
             }
-            if (p->compositing == ORC_DVR) {
-                /* opacity correction, then front-to-back (cpuraycaster.cpp:291-303) */
-                col[3] = R(1) - rpow<R>(R(1) - col[3], kcorr);
+            if (comp == ORC_DVR) {
+                /* opacity correction (none for a pre-integrated colour), then
+                 * front-to-back (cpuraycaster.cpp:291-303) */
+                if (!preint) col[3] = R(1) - rpow<R>(R(1) - col[3], kcorr);
                 if (col[3] > R(0)) {
                     const R w = (R(1) - res[3]) * col[3];
                     res[0] = res[0] + w * col[0];
@@ -288,17 +311,68 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
                     res[3] = res[3] + (R(1) - res[3]) * col[3];
                 }
                 if (depth_t < R(0) && res[3] > R(0)) depth_t = t;
-            } else if (p->compositing == ORC_MIP) {
+            } else if (comp == ORC_MIP) {
                 if (rw > max_int) {
                     res[0] = col[0]; res[1] = col[1]; res[2] = col[2]; res[3] = col[3];
                     max_int = rw;
                     depth_t = t;
                 }
-            } else {  /* ISO */
+            } else if (comp == ORC_ISO) {
                 const R iso = R(p->iso_value), eps = R(0.02);
                 if (col[3] >= iso - eps && col[3] <= iso + eps) {
                     res[0] = col[0]; res[1] = col[1]; res[2] = col[2]; res[3] = R(1);
                     depth_t = t;
+                }
+            } else if (comp == ORC_MOP) {
+                /* compositeMOP (mod_compositing.frag:97-107) */
+                if (col[3] > res[3]) {
+                    res[0] = col[0]; res[1] = col[1]; res[2] = col[2]; res[3] = col[3];
+                    depth_t = t;
+                }
+            } else if (comp == ORC_MIDA) {
+                /* compositeMIDA / compositeMIDAhelper (mod_compositing.frag:109-146).
+                 * As there, the helper never raises maxIntensity: with gamma <= 0
+                 * it stays at its initial 0, with gamma > 0 only the MIP half
+                 * raises it (before the helper reads it). */
+                col[3] = R(1) - rpow<R>(R(1) - col[3], kcorr);
+                const R gamma = R(p->mida_gamma);
+                auto helper = [&](const R* in, R maxi, R gm, R* o) {
+                    R delta = R(0);
+                    if (rw > maxi) delta = rw - maxi;
+                    const R beta = R(1) - delta * (R(1) + gm);
+                    for (int k = 0; k < 3; ++k) o[k] = beta * in[k] + (R(1) - beta * in[3]) * col[3] * col[k];
+                    o[3] = beta * in[3] + (R(1) - beta * in[3]) * col[3];
+                };
+                if (gamma <= R(0)) {
+                    R o[4];
+                    helper(res, max_int, gamma, o);
+                    for (int k = 0; k < 4; ++k) res[k] = o[k];
+                } else {
+                    R mip[4] = {res[0], res[1], res[2], res[3]};
+                    if (rw > max_int) {
+                        for (int k = 0; k < 4; ++k) mip[k] = col[k];
+                        max_int = rw;
+                        depth_t = t;
+                    }
+                    R mida[4];
+                    helper(res, max_int, R(0), mida);
+                    for (int k = 0; k < 4; ++k) res[k] = gamma * mip[k] + (R(1) - gamma) * mida[k];
+                }
+                if (depth_t < R(0)) depth_t = t;
+            } else if (comp == ORC_FHP) {
+                /* compositeFHP (mod_compositing.frag:168-181): texture-space position */
+                if (res[0] == R(0) && res[1] == R(0) && res[2] == R(0)) {
+                    res[0] = s.x; res[1] = s.y; res[2] = s.z; res[3] = R(1);
+                    if (depth_t < R(0)) depth_t = t;
+                }
+            } else if (comp == ORC_FHN) {
+                /* compositeFHN (mod_compositing.frag:183-196): normalize(gradient)/2 + 0.5;
+                 * a zero gradient (undefined in GLSL) gives 0.5 */
+                if (res[0] == R(0) && res[1] == R(0) && res[2] == R(0)) {
+                    const V3<R> n = normalize3(g);
+                    res[0] = n.x / R(2) + R(0.5); res[1] = n.y / R(2) + R(0.5); res[2] = n.z / R(2) + R(0.5);
+                    res[3] = R(1);
+                    if (depth_t < R(0)) depth_t = t;
                 }
             }
         }
@@ -394,6 +468,100 @@ void oracle_bake_tf_keys(const OrcTFKey* keys, int nkeys, int width, float gamma
                 const float diff = float(int(Rk.color_l[ch]) - int(L.color_r[ch]));
                 const float sum = float(L.color_r[ch]) + diff * fraction;
                 o[ch] = static_cast<uint8_t>(sum);
+            }
+        }
+    }
+}
+
+void oracle_preint_source(const OrcTFKey* keys, int nkeys, int res, float gamma, float threshold_lo,
+                          float threshold_hi, uint8_t* out) {
+    /* PreIntegrationTable::computeTable's TF buffer (preintegrationtable.cpp:71-104):
+     * the same key mapping as the texture, sampled at `res` entries, but
+     * zeroed from back_start on (the texture keeps entry back_start). */
+    const int front_end = static_cast<int>(std::floor(threshold_lo * float(res) + 0.5f));
+    const int back_start = static_cast<int>(std::floor(threshold_hi * float(res) + 0.5f));
+    oracle_bake_tf_keys(keys, nkeys, res, gamma, 0.f, 1.f, out);
+    for (int i = 0; i < res; ++i)
+        if (i < front_end || i >= back_start) std::memset(out + 4 * i, 0, 4);
+}
+
+void oracle_preint_table(const uint8_t* src, int res, float d, int use_integral, float* out) {
+    /* PreIntegrationTable::computeTable (preintegrationtable.cpp:67-204), FP32 */
+    struct F4 {
+        float r, g, b, a;
+    };
+    std::vector<F4> tb(res);
+    for (int i = 0; i < res; ++i)  /* tgt::vec4(ubyte) / 255.f */
+        tb[i] = F4{float(src[4 * i]) / 255.f, float(src[4 * i + 1]) / 255.f, float(src[4 * i + 2]) / 255.f,
+                   float(src[4 * i + 3]) / 255.f};
+    auto clamp01 = [](float x) { return std::min(std::max(x, 0.f), 1.f); };
+    auto store = [&](size_t idx, F4 c) {
+        out[4 * idx] = clamp01(c.r);
+        out[4 * idx + 1] = clamp01(c.g);
+        out[4 * idx + 2] = clamp01(c.b);
+        out[4 * idx + 3] = clamp01(c.a);
+    };
+    const float k200 = d * 200.0f;
+    if (!use_integral) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic)
+#endif
+        for (int sb = 0; sb < res; ++sb) {
+            for (int sf = 0; sf < res; ++sf) {
+                const size_t idx = size_t(sb) * res + sf;
+                if (sb != sf) {
+                    const float scale = 1.0f / (std::fabs(static_cast<float>(sb - sf)) + 1);
+                    const int incr = sb < sf ? -1 : 1;
+                    F4 r{0.f, 0.f, 0.f, 0.f};
+                    for (int s = sf; (incr == 1 ? s <= sb : s >= sb) && (r.a < 0.95f); s += incr) {
+                        F4 c = tb[s];
+                        if (c.a > 0.0f) {
+                            c.a = 1.f - std::pow(1.f - c.a, k200 * scale);
+                            const float w = (1.0f - r.a) * c.a;
+                            const float nr = r.r + w * c.r, ng = r.g + w * c.g, nb = r.b + w * c.b;
+                            r.a = r.a + (1.0f - r.a) * c.a;
+                            r.r = nr; r.g = ng; r.b = nb;
+                        }
+                    }
+                    const float m = std::max(r.a, 0.001f);
+                    r.r /= m; r.g /= m; r.b /= m;
+                    store(idx, r);
+                } else {
+                    F4 r{clamp01(tb[sf].r), clamp01(tb[sf].g), clamp01(tb[sf].b), clamp01(tb[sf].a)};
+                    r.a = 1.f - std::pow(1.f - r.a, k200);
+                    store(idx, r);
+                }
+            }
+        }
+    } else {
+        /* integral functions (Real-Time Volume Graphics p. 96) */
+        std::vector<F4> I(res);
+        F4 acc{0.f, 0.f, 0.f, 0.f};
+        for (int i = 0; i < res; ++i) {
+            const F4 c = tb[i];
+            if (c.a > 0.0f) {
+                acc.r += c.r * c.a; acc.g += c.g * c.a; acc.b += c.b * c.a;
+                acc.a += c.a;
+            }
+            I[i] = acc;
+        }
+        for (int sb = 0; sb < res; ++sb) {
+            for (int sf = 0; sf < res; ++sf) {
+                const int smin = std::min(sb, sf), smax = std::max(sb, sf);
+                F4 col;
+                if (smax != smin) {
+                    const float factor = k200 / static_cast<float>(smax - smin);
+                    col.r = (I[smax].r - I[smin].r) * factor;
+                    col.g = (I[smax].g - I[smin].g) * factor;
+                    col.b = (I[smax].b - I[smin].b) * factor;
+                    col.a = 1.f - std::exp(-(I[smax].a - I[smin].a) * factor);
+                    const float m = std::max(col.a, 0.001f);
+                    col.r /= m; col.g /= m; col.b /= m;
+                } else {
+                    col = tb[smin];
+                    col.a = 1.f - std::pow(1.f - col.a, k200);
+                }
+                store(size_t(sb) * res + sf, col);
             }
         }
     }

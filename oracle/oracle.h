@@ -30,7 +30,7 @@ extern "C" {
 #endif
 
 enum { ORC_U8 = 0, ORC_U16 = 1, ORC_F32 = 2 };
-enum { ORC_DVR = 0, ORC_MIP = 1, ORC_ISO = 2 };
+enum { ORC_DVR = 0, ORC_MIP = 1, ORC_ISO = 2, ORC_MOP = 3, ORC_MIDA = 4, ORC_FHP = 5, ORC_FHN = 6 };
 enum { ORC_SHADE_NONE = 0, ORC_SHADE_PHONG = 1 };
 
 typedef struct {
@@ -60,6 +60,9 @@ typedef struct {
     float shininess;
     int apply_attenuation;
     float attenuation[3];
+    float mida_gamma;           /* "gammaValue" (ORC_MIDA) */
+    const float* preint;        /* pre-integration table (res*res RGBA, [back*res + front]), NULL = TF */
+    int preint_res;
 } OrcParams;
 
 /* One TF key as TransFuncMappingKey holds it: intensity in [0,1], left/right
@@ -73,6 +76,17 @@ typedef struct {
 /* TransFunc1D::createTextureData + TransFunc1DKeys::getMappingForValueUByte. */
 void oracle_bake_tf_keys(const OrcTFKey* keys, int nkeys, int width, float gamma,
                          float threshold_lo, float threshold_hi, uint8_t* out_rgba);
+
+/* PreIntegrationTable::computeTable's TF buffer (preintegrationtable.cpp:71-104):
+ * entry i = the keys' mapping at gamma(i/(res-1)), zero below
+ * iround(threshold_lo*res) and from iround(threshold_hi*res) on. */
+void oracle_preint_source(const OrcTFKey* keys, int nkeys, int res, float gamma, float threshold_lo,
+                          float threshold_hi, uint8_t* out_rgba);
+
+/* PreIntegrationTable::computeTable (preintegrationtable.cpp:67-204): the
+ * exact table (use_integral 0) or the integral-function approximation (1),
+ * FP32, out[4 * (back * res + front) + c]. */
+void oracle_preint_table(const uint8_t* source_rgba, int res, float step, int use_integral, float* out);
 
 /* Texture-space entry/exit points of the unit-cube proxy for a perspective
  * camera, in FP64 (MeshEntryExitPoints rendering processCube's cube).

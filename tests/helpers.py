@@ -10,9 +10,10 @@ import voreen_gb300 as v
 TOL = 1.0 / 255.0  # spec bound per RGBA channel against the FP64 oracle
 
 
-def oracle_params(w_params, light=None, cam=None):
+def oracle_params(w_params, light=None, cam=None, preint_table=None):
     p = w_params
     return oracle.make_params(sampling_rate=p.sampling_rate, compositing=p.compositing, shading=p.shading,
+                              mida_gamma=p.mida_gamma, preint_table=preint_table,
                               iso_value=p.iso_value, ert=p.ert_threshold,
                               light_pos=list(p.light_position)[:3] if light is None else light,
                               camera_pos=list(p.camera.position) if cam is None else cam,
@@ -54,10 +55,11 @@ class Case:
     def step(self):
         return 1.0 / (max(self.vol.dims) * self.params.sampling_rate)
 
-    def oracle(self, precision=32, rows=None, entry=None, exit_pts=None):
+    def oracle(self, precision=32, rows=None, entry=None, exit_pts=None, preint_table=None):
         e = self.entry if entry is None else entry
         x = self.exit if exit_pts is None else exit_pts
-        return oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params), e, x, precision, rows)
+        return oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params, preint_table=preint_table),
+                             e, x, precision, rows)
 
 
 def sample_index(first_hit, step):

@@ -52,3 +52,49 @@ def test_process_renders_like_the_oracle(ctx):
     ref, _, _ = oracle.render(oracle.make_volume(w.voxels, w.spacing), tf, (lo, hi), oracle_params(p), e, x, 32)
     np.testing.assert_array_equal(img.view(np.uint32), ref.view(np.uint32))
     r.deinitialize()
+
+
+def test_preintegrated_gpu_falls_back_with_an_error(vrc_lib):
+    """cpuraycaster.cpp:123-129: pre-integrated-gpu logs an error, selects
+    pre-integrated-cpu and renders nothing this call."""
+    r = CudaRaycaster()
+    r._ctx = object()
+    w = synth.config1(size=(8, 8, 8), image=(4, 4))
+    r.volumeInport.setData(VolumeData(w.voxels))
+    r.entryPort.setData(np.zeros((4, 4, 4), np.float32))
+    r.exitPort.setData(np.zeros((4, 4, 4), np.float32))
+    r.classification = "pre-integrated-gpu"
+    r.process()
+    assert "Falling back to CPU" in r.lastError and r.classification == "pre-integrated-cpu"
+    assert not r.outport.hasData()
+    assert r.preIntegrationTableSize == 0 and r.gammaValue == 0.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("classification", ["pre-integrated-cpu", "pre-integrated-approximation"])
+def test_process_preintegrated_like_the_oracle(ctx, classification):
+    import oracle
+    from helpers import oracle_entry_exit, oracle_params
+    w = synth.config1(size=(48, 40, 44), image=(80, 64))
+    r = CudaRaycaster()
+    r.volumeInport.setData(VolumeData(w.voxels, w.spacing))
+    r.transferFunction.keys = w.tf_keys
+    r.classification = classification
+    p = w.params()
+    r.camera = p.camera
+    desc = v.make_desc(v.U8, w.dims, w.spacing)
+    e, x = oracle_entry_exit(desc, p)
+    r.entryPort.setData(e)
+    r.exitPort.setData(x)
+    r.process()
+    assert r.lastError == ""
+    img = r.outport.getData()
+    lo, hi = r.transferFunction.domain
+    step = float(np.float32(1) / (np.float32(48) * np.float32(2)))
+    src = oracle.preint_source(w.tf_keys, 256)
+    table = oracle.preint_table(src, step, classification.endswith("approximation"))
+    tf = v.TransferFunction.bake(w.tf_keys, 256)
+    ref, _, _ = oracle.render(oracle.make_volume(w.voxels, w.spacing), tf, (lo, hi),
+                              oracle_params(p, preint_table=table), e, x, 32)
+    np.testing.assert_array_equal(img.view(np.uint32), ref.view(np.uint32))
+    r.deinitialize()

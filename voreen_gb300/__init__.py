@@ -19,11 +19,13 @@ import ctypes as C
 import numpy as np
 
 from . import _abi
-from ._abi import (DVR, EE_ANALYTIC, EE_BUFFERS, F32, ISO, MIP, NOALLOC_MAX_CELLS, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE,
-                   SHADE_PHONG, U8, U16, Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
+from ._abi import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, F32, FHN, FHP, ISO, MIDA, MIP,
+                   MOP, NOALLOC_MAX_CELLS, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, U8, U16,
+                   Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
 
-__all__ = ["VrcError", "Context", "Volume", "TransferFunction", "render", "entry_exit", "default_params",
-           "camera_matrices", "lib", "DVR", "MIP", "ISO", "SHADE_NONE", "SHADE_PHONG", "U8", "U16", "F32",
+__all__ = ["VrcError", "Context", "Volume", "TransferFunction", "PreIntegrationTable", "render", "entry_exit",
+           "default_params", "sampling_step", "camera_matrices", "lib", "DVR", "MIP", "ISO", "MOP", "MIDA", "FHP",
+           "FHN", "CLASSIFY_TF", "CLASSIFY_PREINTEGRATED", "SHADE_NONE", "SHADE_PHONG", "U8", "U16", "F32",
            "OUT_RGBA8", "OUT_RGBA16", "OUT_RGBA32F", "EE_BUFFERS", "EE_ANALYTIC", "Camera", "RenderParams",
            "RenderStats", "VolumeDesc", "TFKey"]
 
@@ -194,6 +196,13 @@ class TransferFunction:
     def table_width(dtype: int) -> int:
         return int(lib().vrc_tf_table_width(dtype))
 
+    def set_preintegration(self, table: "PreIntegrationTable | None"):
+        """Attach (or with None detach) the table used by renders with
+        classification CLASSIFY_PREINTEGRATED."""
+        _check(lib().vrc_tf_set_preintegration(self.handle, table.handle if table is not None else None), self.ctx,
+               "vrc_tf_set_preintegration")
+        self._preint = table
+
     def close(self):
         if self.handle:
             lib().vrc_tf_destroy(self.handle)
@@ -204,6 +213,64 @@ class TransferFunction:
             self.close()
         except Exception:
             pass
+
+
+def _tf_keys(keys):
+    arr = (TFKey * max(1, len(keys)))()
+    for i, k in enumerate(keys):
+        arr[i].intensity = float(k[0])
+        arr[i].color_l[:] = [int(v) for v in k[1]]
+        arr[i].color_r[:] = [int(v) for v in (k[2] if len(k) > 2 else k[1])]
+    return arr
+
+
+class PreIntegrationTable:
+    """Pre-integrated classification table on the device (vrc_preint,
+    PreIntegrationTable): res x res RGBA, entry [back, front], for one
+    sampling step size."""
+
+    def __init__(self, ctx: Context, source_rgba: np.ndarray, step: float, use_integral: bool = False):
+        self.ctx = ctx
+        self.source = np.ascontiguousarray(source_rgba, dtype=np.uint8).reshape(-1, 4)
+        self.res = self.source.shape[0]
+        self.step = float(np.float32(step))
+        self.use_integral = bool(use_integral)
+        self.handle = C.c_void_p()
+        _check(lib().vrc_preint_create(ctx.handle, _ptr(self.source), self.res, self.step, 1 if use_integral else 0,
+                                       C.byref(self.handle)), ctx, "vrc_preint_create")
+
+    @staticmethod
+    def resolution(tf_width: int, requested: int = 0) -> int:
+        return int(lib().vrc_preint_resolution(tf_width, requested))
+
+    @staticmethod
+    def bake_source(keys, res: int, gamma: float = 1.0, threshold=(0.0, 1.0)) -> np.ndarray:
+        """The TF keys sampled at `res` entries as the table build samples them."""
+        out = np.zeros((res, 4), np.uint8)
+        _check(lib().vrc_preint_bake_source(_tf_keys(keys), len(keys), res, gamma, threshold[0], threshold[1],
+                                            _ptr(out)), None, "vrc_preint_bake_source")
+        return out
+
+    def download(self) -> np.ndarray:
+        out = np.zeros((self.res, self.res, 4), np.float32)
+        _check(lib().vrc_preint_download(self.handle, _ptr(out)), self.ctx, "vrc_preint_download")
+        return out
+
+    def close(self):
+        if self.handle:
+            lib().vrc_preint_destroy(self.handle)
+            self.handle = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def sampling_step(vol: "Volume", sampling_rate: float) -> float:
+    """The march's step size 1 / (max(dim) * samplingRate) in FP32."""
+    return float(lib().vrc_sampling_step(vol.handle, sampling_rate))
 
 
 def default_params(width: int, height: int) -> RenderParams:

@@ -16,7 +16,8 @@ STATUS_NAMES = {0: "VRC_OK", 1: "VRC_ERR_INVALID_ARG", 2: "VRC_ERR_CUDA", 3: "VR
                 4: "VRC_ERR_UNSUPPORTED", 5: "VRC_ERR_TIMEOUT", 6: "VRC_ERR_NOT_READY", 7: "VRC_ERR_DEVICE",
                 8: "VRC_ERR_SCRATCH_LIMIT"}
 U8, U16, F32 = 0, 1, 2
-DVR, MIP, ISO = 0, 1, 2
+DVR, MIP, ISO, MOP, MIDA, FHP, FHN = 0, 1, 2, 3, 4, 5, 6
+CLASSIFY_TF, CLASSIFY_PREINTEGRATED = 0, 1
 SHADE_NONE, SHADE_PHONG = 0, 1
 OUT_RGBA8, OUT_RGBA32F, OUT_RGBA16 = 0, 1, 2
 EE_BUFFERS, EE_ANALYTIC = 0, 1
@@ -46,7 +47,8 @@ class RenderParams(C.Structure):
                 ("material_shininess", C.c_float), ("apply_attenuation", C.c_int),
                 ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
                 ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("skip_cell_size", C.c_int),
-                ("tile_width", C.c_int), ("region", C.c_int * 4), ("reserved", C.c_int * 2)]
+                ("tile_width", C.c_int), ("region", C.c_int * 4), ("classification", C.c_int),
+                ("mida_gamma", C.c_float)]
 
 
 class BatchItem(C.Structure):
@@ -97,6 +99,13 @@ SIGNATURES = {
     "vrc_batch_stats_get": (C.c_int, [VP, VP, P(BatchStats)]),
     "vrc_batch_destroy": (C.c_int, [VP]),
     "vrc_render_noalloc": (C.c_int, [VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP]),
+    "vrc_preint_resolution": (C.c_int, [C.c_int, C.c_int]),
+    "vrc_preint_bake_source": (C.c_int, [P(TFKey), C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, VP]),
+    "vrc_preint_create": (C.c_int, [VP, VP, C.c_int, C.c_float, C.c_int, P(VP)]),
+    "vrc_preint_download": (C.c_int, [VP, VP]),
+    "vrc_preint_destroy": (C.c_int, [VP]),
+    "vrc_tf_set_preintegration": (C.c_int, [VP, VP]),
+    "vrc_sampling_step": (C.c_float, [VP, C.c_float]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
     "vrc_synth_tubes_device": (C.c_int, [VP, P(C.c_int), C.c_int, C.c_uint64, C.c_float, VP]),
 }

@@ -28,6 +28,11 @@ SOURCES = [
     ("synth.cpp", []),
     ("volume.cu", []),
     ("march.cu", ["-fmad=false"]),
+    ("march_dvr.cu", ["-fmad=false"]),
+    ("march_mip_iso.cu", ["-fmad=false"]),
+    ("march_mop_mida.cu", ["-fmad=false"]),
+    ("march_first_hit.cu", ["-fmad=false"]),
+    ("preint.cu", ["-fmad=false"]),
     ("noalloc.cu", []),
     ("batch.cpp", []),
     ("nn.cu", []),
@@ -72,7 +77,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         obj = os.path.join(BUILD, src.replace(".", "_") + ".o")
         objs.append(obj)
         tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS", "VRC_MARCH_ROUND")
-                if src == "march.cu" and os.environ.get(k)]
+                if src.startswith("march") and os.environ.get(k)]
         extra = extra + tune
         force_this = bool(tune)
         if force or force_this or _stale(obj, [path] + hdrs):

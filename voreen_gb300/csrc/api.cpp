@@ -497,6 +497,15 @@ void vrc_render_params_default(vrc_render_params* p, int W, int H) {
     p->entry_exit_mode = VRC_EE_BUFFERS;
     p->quantize_entry_exit = 0;
     p->empty_space_skipping = 1;
+    p->classification = VRC_CLASSIFY_TF;
+    p->mida_gamma = 0.f;                 // volumeraycaster.cpp:66 ("gammaValue")
+}
+
+float vrc_sampling_step(const vrc_volume* vol, float sampling_rate) {
+    if (!vol || !(sampling_rate > 0.f)) return 0.f;
+    const int* d = vol->desc.dims;
+    const int maxdim = std::max(d[0], std::max(d[1], d[2]));
+    return 1.f / (float(maxdim) * sampling_rate);
 }
 
 }  // extern "C"
@@ -570,6 +579,7 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
     P.iso = p->iso_value;
     P.shininess = p->material_shininess;
     P.atten_on = p->apply_attenuation;
+    P.mida_gamma = p->mida_gamma;
     P.W = p->width;
     P.H = p->height;
     P.ee_mode = p->entry_exit_mode;
@@ -604,8 +614,14 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: image size out of range");
     if (!(p->sampling_rate > 0.f) || !std::isfinite(p->sampling_rate))
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: sampling_rate must be > 0");
-    if (p->compositing < VRC_DVR || p->compositing > VRC_ISO)
+    if (p->compositing < VRC_DVR || p->compositing > VRC_FHN)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown compositing mode");
+    if (p->classification != VRC_CLASSIFY_TF && p->classification != VRC_CLASSIFY_PREINTEGRATED)
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown classification mode");
+    if (p->classification == VRC_CLASSIFY_PREINTEGRATED && p->compositing != VRC_DVR)
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: pre-integrated classification needs DVR compositing");
+    if (!std::isfinite(p->mida_gamma))
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: mida_gamma must be finite");
     if (p->shading < VRC_SHADE_NONE || p->shading > VRC_SHADE_PHONG)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown shading mode");
     if (p->entry_exit_mode != VRC_EE_BUFFERS && p->entry_exit_mode != VRC_EE_ANALYTIC)
@@ -649,12 +665,28 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     VRC_CUDA(ctx, cudaSetDevice(ctx->device));
     MarchParams P;
     if ((st = fill_params(ctx, vol, p, P)) != VRC_OK) return st;
-    const bool dvr = p->compositing == VRC_DVR;
     const float kcorr = P.step * 200.f;  // SAMPLING_BASE_INTERVAL_RCP
-    float4* table = nullptr;
-    if ((st = tf_table(ctx, tf, dvr, kcorr, &table)) != VRC_OK) return st;
-    P.tf_table = table;
-    P.tf_width = tf->width;
+    const int* occ_prefix = tf->d_prefix;
+    int occ_width = tf->width;
+    if (p->classification == VRC_CLASSIFY_PREINTEGRATED) {
+        const vrc_preint* pi = tf->preint;
+        if (!pi) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: no pre-integration table attached to the TF");
+        if (pi->step != P.step)
+            return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: the pre-integration table was built for another step size");
+        P.pi_table = pi->d_table;
+        P.pi_res = pi->res;
+        P.tf_table = nullptr;
+        P.tf_width = 0;  // the TF table is not read
+        occ_prefix = pi->d_prefix;
+        occ_width = pi->res;
+    } else {
+        float4* table = nullptr;
+        if ((st = tf_table(ctx, tf, vrc::alpha_corrected(p->compositing, p->classification), kcorr, &table)) !=
+            VRC_OK)
+            return st;
+        P.tf_table = table;
+        P.tf_width = tf->width;
+    }
     P.tf_lo = tf->lo;
     P.tf_hi = tf->hi;
     const size_t npix = (size_t)p->width * p->height;
@@ -703,7 +735,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             }
         const long long n = (long long)nc[0] * nc[1] * nc[2];
         VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, vrc::occupancy_bytes(n)));
-        VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, tf->d_prefix, tf->width, vol->desc.rwm_scale,
+        VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, occ_prefix, occ_width, vol->desc.rwm_scale,
                                             vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
         P.occupancy = ctx->d_occ;
         P.cshift = ilog2(C);
@@ -714,7 +746,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             // coarse level: whole bricks, tested first
             const long long nb = vol->L.nbricks();
             VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes, vrc::occupancy_bytes(nb)));
-            VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, tf->d_prefix, tf->width,
+            VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width,
                                                 vol->desc.rwm_scale, vol->desc.rwm_offset, tf->lo, tf->hi,
                                                 ctx->d_occ_coarse, s));
             P.occ_coarse = ctx->d_occ_coarse;

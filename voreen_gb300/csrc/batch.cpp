@@ -74,6 +74,9 @@ vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n
         if (st != VRC_OK) return st;
         if (it.params.entry_exit_mode != VRC_EE_ANALYTIC)
             return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: batched requests use analytic entry/exit");
+        if (it.params.compositing > VRC_ISO || it.params.classification != VRC_CLASSIFY_TF)
+            return bfail(ctx, VRC_ERR_UNSUPPORTED,
+                         "vrc_batch_create: batches take dvr / mip / iso compositing with TF classification");
         if (it.params.compositing != items[0].params.compositing || it.params.shading != items[0].params.shading)
             return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: all requests must share compositing and shading");
         if (it.out_format < VRC_OUT_RGBA8 || it.out_format > VRC_OUT_RGBA16)

@@ -1,586 +1,11 @@
-// The ray-march kernel: a GB300 restatement of CPURaycaster::directRendering
-// (modules/base/processors/render/cpuraycaster.cpp:210-326) with the GLSL-only
-// compositing and shading rules of rc_singlevolume.frag:116-312.
-//
-// Design:
-//  * persistent grid (a few CTAs per SM); each warp pulls 8x4 ray tiles from
-//    a global counter, so a warp's 32 rays are adjacent on screen and walk
-//    the same bricks;
-//  * the transfer function sits in shared memory as float4 (r, g, b, alpha')
-//    where alpha' already carries the opacity correction 1-(1-a)^(step*200)
-//    (computed on the host with the same powf the CPU path calls);
-//  * voxels come from the bricked layout (32^3 core + apron), so a stencil
-//    never crosses a brick; empty bricks (per-brick min/max against the TF)
-//    are skipped without reading voxels while t still advances sample by
-//    sample, which keeps results identical to the unskipped march;
-//  * every operation on the sample path is an explicitly rounded FP32
-//    intrinsic in the reference's order (no FMA contraction), so positions,
-//    trilinear values, TF indices, compositing and the t > tend stop match
-//    the FP32 CPU path bit for bit. Voxel normalisation v/255 and v/65535 is
-//    computed as q0 = v*r, q = fma(fma(-q0, d, v), r, q0), which equals the
-//    correctly rounded quotient for every 8- and 16-bit value;
-//  * gradients (central differences, mod_gradients.frag:202-214) are six
-//    lookups at +-1/dim in texture space, clamped like the intensity sample
-//    and read from the centre's brick apron (another brick only when rounding
-//    puts a tap two voxels away); they interpolate raw voxel values with FMA
-//    lerps. Phong (mod_shading.frag:134-151) runs in registers with fast
-//    reciprocal square roots and __powf. Shading only colours samples whose
-//    alpha is already decided, so it changes no discrete decision; its
-//    colours differ from the CPU path by ~1e-6.
-#include <cstdint>
-
-#include "vrc_internal.h"
+// Frame-level launch dispatch of the ray march (one translation unit per
+// compositing family: march_dvr.cu, march_mip_iso.cu, march_mop_mida.cu,
+// march_first_hit.cu), the analytic entry/exit kernel and the batched
+// persistent render.
+#include "march_core.cuh"
 
 namespace vrc {
 namespace {
-
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int LOOP_CAP = 255 * 255;  // cpuraycaster.cpp:239
-
-__device__ __forceinline__ float m_(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ float a_(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ float s_(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); }
-
-template <int DT> struct Vox;
-template <> struct Vox<VRC_U8> {
-    using T = uint8_t;
-    static __device__ __forceinline__ float norm(T v) {
-        const float x = (float)v, r = 1.f / 255.f;
-        const float q0 = __fmul_rn(x, r);
-        return __fmaf_rn(__fmaf_rn(-q0, 255.f, x), r, q0);
-    }
-};
-template <> struct Vox<VRC_U16> {
-    using T = uint16_t;
-    static __device__ __forceinline__ float norm(T v) {
-        const float x = (float)v, r = 1.f / 65535.f;
-        const float q0 = __fmul_rn(x, r);
-        return __fmaf_rn(__fmaf_rn(-q0, 65535.f, x), r, q0);
-    }
-};
-template <> struct Vox<VRC_F32> {
-    using T = float;
-    static __device__ __forceinline__ float norm(T v) { return v; }
-};
-
-struct F3 {
-    float x, y, z;
-};
-
-// VolumeRAM::getVoxelNormalizedLinear summation order (volumeram.cpp:89-96).
-__device__ __forceinline__ float tri8(float v000, float v100, float v110, float v010, float v001, float v101,
-                                      float v111, float v011, float fx, float fy, float fz) {
-    const float ox = s_(1.f, fx), oy = s_(1.f, fy), oz = s_(1.f, fz);
-    float s = m_(m_(m_(v000, ox), oy), oz);
-    s = a_(s, m_(m_(m_(v100, fx), oy), oz));
-    s = a_(s, m_(m_(m_(v110, fx), fy), oz));
-    s = a_(s, m_(m_(m_(v010, ox), fy), oz));
-    s = a_(s, m_(m_(m_(v001, ox), oy), fz));
-    s = a_(s, m_(m_(m_(v101, fx), oy), fz));
-    s = a_(s, m_(m_(m_(v111, fx), fy), fz));
-    s = a_(s, m_(m_(m_(v011, ox), fy), fz));
-    return s;
-}
-
-template <int DT>
-__device__ __forceinline__ float tri_at(const typename Vox<DT>::T* __restrict__ b, int o, int S, int S2, float fx,
-                                        float fy, float fz) {
-    using V = Vox<DT>;
-    return tri8(V::norm(__ldg(b + o)), V::norm(__ldg(b + o + 1)), V::norm(__ldg(b + o + S + 1)),
-                V::norm(__ldg(b + o + S)), V::norm(__ldg(b + o + S2)), V::norm(__ldg(b + o + S2 + 1)),
-                V::norm(__ldg(b + o + S2 + S + 1)), V::norm(__ldg(b + o + S2 + S)), fx, fy, fz);
-}
-
-__device__ __forceinline__ float clampf_(float x, float lo, float hi) {
-    x = x > lo ? x : lo;
-    return x < hi ? x : hi;
-}
-
-__device__ __forceinline__ float rw_to_tf(float rw, float lo, float hi) {
-    if (rw < lo) return 0.f;
-    if (rw > hi) return 1.f;
-    if (lo == hi) return 0.f;
-    return d_(s_(rw, lo), s_(hi, lo));
-}
-
-__device__ __forceinline__ int tf_index(float x, int w) {
-    const float f = m_(x, (float)(w - 1));
-    const int i = (int)floorf(a_(f, 0.5f));
-    return i < 0 ? 0 : (i > w - 1 ? w - 1 : i);
-}
-
-__device__ __forceinline__ float len3(float x, float y, float z) {
-    float s = m_(x, x);
-    s = a_(s, m_(y, y));
-    s = a_(s, m_(z, z));
-    return __fsqrt_rn(s);
-}
-
-__device__ __forceinline__ F3 normalize3(F3 v) {
-    const float l = len3(v.x, v.y, v.z);
-    if (l == 0.f) return F3{0.f, 0.f, 0.f};
-    const float r = d_(1.f, l);
-    return F3{m_(v.x, r), m_(v.y, r), m_(v.z, r)};
-}
-
-__device__ __forceinline__ float dot3(F3 a, F3 b) {
-    float s = m_(a.x, b.x);
-    s = a_(s, m_(a.y, b.y));
-    s = a_(s, m_(a.z, b.z));
-    return s;
-}
-
-// ---- shading path ----------------------------------------------------
-// Shading feeds only the colour of samples with alpha > 0; it has no
-// discrete decision and its pow is not correctly rounded on any platform, so
-// it uses fused multiply-adds, fast reciprocal square roots and __powf. The
-// resulting colour differs from the CPU path by ~1e-6 relative.
-__device__ __forceinline__ F3 fnormalize(F3 v) {
-    const float l2 = __fmaf_rn(v.x, v.x, __fmaf_rn(v.y, v.y, __fmul_rn(v.z, v.z)));
-    if (l2 == 0.f) return F3{0.f, 0.f, 0.f};
-    const float r = rsqrtf(l2);
-    return F3{v.x * r, v.y * r, v.z * r};
-}
-__device__ __forceinline__ float fdot(F3 a, F3 b) { return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, __fmul_rn(a.z, b.z))); }
-
-// Trilinear interpolation of raw voxel values with FMA lerps (gradient taps).
-template <int DT>
-__device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__ b, int o, int S, int S2, float fx,
-                                         float fy, float fz) {
-    const float v000 = (float)__ldg(b + o), v100 = (float)__ldg(b + o + 1);
-    const float v010 = (float)__ldg(b + o + S), v110 = (float)__ldg(b + o + S + 1);
-    const float v001 = (float)__ldg(b + o + S2), v101 = (float)__ldg(b + o + S2 + 1);
-    const float v011 = (float)__ldg(b + o + S2 + S), v111 = (float)__ldg(b + o + S2 + S + 1);
-    const float x00 = __fmaf_rn(fx, v100 - v000, v000), x10 = __fmaf_rn(fx, v110 - v010, v010);
-    const float x01 = __fmaf_rn(fx, v101 - v001, v001), x11 = __fmaf_rn(fx, v111 - v011, v011);
-    const float y0 = __fmaf_rn(fy, x10 - x00, x00), y1 = __fmaf_rn(fy, x11 - x01, x01);
-    return __fmaf_rn(fz, y1 - y0, y0);
-}
-
-// Raw trilinear value at a clamped voxel position from the brick holding it.
-template <int DT>
-__device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
-                                                float vx, float vy, float vz) {
-    const BrickLayout& L = P.L;
-    const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
-    const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
-    const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
-    const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
-    const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
-                  (ix - (bx << L.shift) + APRON_LO);
-    return tri_raw<DT>(bricks + brick * L.brick_stride, o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
-}
-
-// One central-difference lookup displaced along one axis: tap position `vt`
-// (clamped voxel coordinate on that axis, as calcGradientA's texture lookup
-// gives it) with the centre's coordinates on the other axes. Reads from the
-// centre's brick when the stencil fits in its apron.
-template <int DT, int AXIS>
-__device__ __forceinline__ float grad_tap(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
-                                          const typename Vox<DT>::T* __restrict__ b, int o, int lc, int ic, float vt,
-                                          float vx, float vy, float vz, float fx, float fy, float fz) {
-    const float fl = floorf(vt);
-    const int it = (int)fl;
-    const int lt = lc + (it - ic);
-    const int S = P.L.S, S2 = P.L.S * P.L.S;
-    if (lt >= 0 && lt <= P.L.B + 1) {
-        const int stride = AXIS == 0 ? 1 : (AXIS == 1 ? S : S2);
-        const float ft = vt - fl;
-        return tri_raw<DT>(b, o + (it - ic) * stride, S, S2, AXIS == 0 ? ft : fx, AXIS == 1 ? ft : fy,
-                           AXIS == 2 ? ft : fz);
-    }
-    return tap_raw_any_brick<DT>(P, bricks, AXIS == 0 ? vt : vx, AXIS == 1 ? vt : vy, AXIS == 2 ? vt : vz);
-}
-
-// phongShading (mod_shading.frag:134-151), ka = kd = TF colour, ks = 1.
-__device__ __forceinline__ F3 phong_fast(const MarchParams& P, F3 n, F3 pos, F3 col) {
-    const F3 N = fnormalize(n);
-    F3 L{P.light_phys[0] - pos.x, P.light_phys[1] - pos.y, P.light_phys[2] - pos.z};
-    const F3 V = fnormalize(F3{P.cam_phys[0] - pos.x, P.cam_phys[1] - pos.y, P.cam_phys[2] - pos.z});
-    const float d2 = fdot(L, L);
-    const float rd = d2 > 0.f ? rsqrtf(d2) : 0.f;
-    const float d = d2 * rd;
-    L = F3{L.x * rd, L.y * rd, L.z * rd};
-    const float ndl = fmaxf(fdot(N, L), 0.f);
-    const F3 Hh = fnormalize(F3{V.x + L.x, V.y + L.y, V.z + L.z});
-    const float ndh = fmaxf(fdot(N, Hh), 0.f);
-    const float spec = __powf(ndh, P.shininess);
-    F3 out{__fmaf_rn(col.x * P.dif[0], ndl, __fmaf_rn(P.spec[0], spec, col.x * P.amb[0])),
-           __fmaf_rn(col.y * P.dif[1], ndl, __fmaf_rn(P.spec[1], spec, col.y * P.amb[1])),
-           __fmaf_rn(col.z * P.dif[2], ndl, __fmaf_rn(P.spec[2], spec, col.z * P.amb[2]))};
-    if (P.atten_on) {
-        const float att = fminf(__fdividef(1.f, __fmaf_rn(P.att[2] * d, d, __fmaf_rn(P.att[1], d, P.att[0]))), 1.f);
-        out = F3{out.x * att, out.y * att, out.z * att};
-    }
-    return out;
-}
-
-// Analytic entry/exit for pixel (px, py): the pixel-centre ray through the
-// unit texture cube, clipped to the near/far planes. Returns false for
-// background.
-__device__ bool analytic_entry_exit(const MarchParams& P, int px, int py, float4& e, float4& l) {
-    const float nx = s_(d_(m_(2.f, a_((float)px, 0.5f)), (float)P.W), 1.f);
-    const float ny = s_(d_(m_(2.f, a_((float)py, 0.5f)), (float)P.H), 1.f);
-    float pn[4], pf[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        const float* M = P.inv_mvp + 4 * r;
-        const float base = a_(m_(M[0], nx), m_(M[1], ny));
-        pn[r] = a_(s_(base, M[2]), M[3]);
-        pf[r] = a_(a_(base, M[2]), M[3]);
-    }
-    float o[3], d[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        o[i] = d_(pn[i], pn[3]);
-        d[i] = s_(d_(pf[i], pf[3]), o[i]);
-    }
-    float s0 = 0.f, s1 = 1.f;
-    bool hit = true;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        if (d[i] == 0.f) {
-            if (o[i] < 0.f || o[i] > 1.f) hit = false;
-        } else {
-            float a = d_(s_(0.f, o[i]), d[i]), b = d_(s_(1.f, o[i]), d[i]);
-            if (a > b) {
-                const float t = a;
-                a = b;
-                b = t;
-            }
-            s0 = fmaxf(s0, a);
-            s1 = fminf(s1, b);
-        }
-    }
-    if (!hit || !(s0 < s1)) {
-        e = make_float4(0.f, 0.f, 0.f, 0.f);
-        l = e;
-        return false;
-    }
-    float en[3], ex[3];
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        float a = clampf_(a_(o[i], m_(s0, d[i])), 0.f, 1.f);
-        float b = clampf_(a_(o[i], m_(s1, d[i])), 0.f, 1.f);
-        if (P.quantize) {
-            a = d_(floorf(a_(m_(a, 65535.f), 0.5f)), 65535.f);
-            b = d_(floorf(a_(m_(b, 65535.f), 0.5f)), 65535.f);
-        }
-        en[i] = a;
-        ex[i] = b;
-    }
-    e = make_float4(en[0], en[1], en[2], 1.f);
-    l = make_float4(ex[0], ex[1], ex[2], 1.f);
-    return true;
-}
-
-template <int EE> __device__ __forceinline__ F3 entry_point_at(const MarchParams& P, int x, int y) {
-    x = min(max(x, 0), P.W - 1);
-    y = min(max(y, 0), P.H - 1);
-    float4 e, l;
-    if (EE == VRC_EE_BUFFERS) {
-        e = P.entry[(size_t)y * P.W + x];
-    } else {
-        analytic_entry_exit(P, x, y, e, l);
-    }
-    return F3{e.x, e.y, e.z};
-}
-
-// fixClipBorderGradient (mod_gradients.frag:39-46)
-template <int EE> __device__ F3 clip_border_gradient(const MarchParams& P, F3 s, F3 dir, int px, int py) {
-    const F3 a = entry_point_at<EE>(P, px + 2, py), b = entry_point_at<EE>(P, px, py + 2);
-    const F3 v0 = normalize3(F3{s_(a.x, s.x), s_(a.y, s.y), s_(a.z, s.z)});
-    const F3 v1 = normalize3(F3{s_(b.x, s.x), s_(b.y, s.y), s_(b.z, s.z)});
-    F3 g{s_(m_(v0.y, v1.z), m_(v0.z, v1.y)), s_(m_(v0.z, v1.x), m_(v0.x, v1.z)), s_(m_(v0.x, v1.y), m_(v0.y, v1.x))};
-    if (!(dot3(g, dir) < 0.f)) g = F3{-g.x, -g.y, -g.z};
-    return g;
-}
-
-__device__ __forceinline__ void write_out(const MarchParams& P, size_t pix, float4 r) {
-    if (P.out_format == VRC_OUT_RGBA32F) {
-        reinterpret_cast<float4*>(P.out)[pix] = r;
-    } else if (P.out_format == VRC_OUT_RGBA8) {
-        auto q = [](float v) -> unsigned {
-            v = fminf(fmaxf(v, 0.f), 1.f);
-            return (unsigned)floorf(v * 255.f + 0.5f);
-        };
-        reinterpret_cast<uchar4*>(P.out)[pix] = make_uchar4(q(r.x), q(r.y), q(r.z), q(r.w));
-    } else {
-        auto q = [](float v) -> unsigned {
-            v = fminf(fmaxf(v, 0.f), 1.f);
-            return (unsigned)floorf(v * 65535.f + 0.5f);
-        };
-        reinterpret_cast<ushort4*>(P.out)[pix] = make_ushort4(q(r.x), q(r.y), q(r.z), q(r.w));
-    }
-}
-
-struct Counters {
-    unsigned long long samples = 0, fetched = 0, shaded = 0, runs = 0;
-};
-
-// Largest ray parameter up to which every sample's floor voxel stays in skip
-// cell (cx, cy, cz): per axis, where the unclamped voxel coordinate
-// dim * (first + t * dir) - 0.5 reaches the cell face it moves toward, pulled
-// in by skip_margin voxels to absorb rounding (the margin exceeds the error of
-// the sample-position arithmetic and of the fast division here by orders of
-// magnitude). Cells on the volume border have no face on their outer side:
-// clamping keeps samples there.
-__device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, float dx, float dy, float dz, int cx,
-                                             int cy, int cz, int shift, const int* nc) {
-    const int C = 1 << shift;
-    const float fo[3] = {f.x, f.y, f.z}, di[3] = {dx, dy, dz};
-    const int ci[3] = {cx, cy, cz};
-    float tmax = INFINITY;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const float a = P.dimf[i] * fo[i] - 0.5f, b = P.dimf[i] * di[i];
-        if (b > 0.f && ci[i] < nc[i] - 1) {
-            tmax = fminf(tmax, __fdividef((float)((ci[i] + 1) * C) - P.skip_margin - a, b));
-        } else if (b < 0.f && ci[i] > 0) {
-            tmax = fminf(tmax, __fdividef((float)(ci[i] * C) + P.skip_margin - a, b));
-        }
-    }
-    return tmax;
-}
-
-// Advances (t, loop) over the samples of an empty run in closed form: every
-// sample with t <= lim is processed (and changes nothing). The FP32 sum
-// t + step, for t on the grid of its binade [2^(e-1), 2^e) with spacing u,
-// is exactly t + q with q = round(step / u) * u unless step / u ends in .5
-// (a rounding tie, left to the caller's exact loop). So n steps inside the
-// binade give exactly t + n * q, the value the reference's one-at-a-time
-// accumulation t += samplingStepSize produces. Stops short of the binade end
-// and of LOOP_CAP; the caller finishes with exact single steps.
-__device__ __forceinline__ void jump_empty_run(float& t, int& loop, float step, float lim) {
-    const int bits = __float_as_int(t);
-    const int ex = (bits >> 23) & 0xff;  // biased exponent, t normal and > 0
-    if (ex < 24 || ex > 250) return;
-    const float u = __int_as_float((ex - 23) << 23);     // ulp of t: 2^(ex - 127 - 23)
-    const float top = __int_as_float((ex + 1) << 23);    // 2^(ex - 127 + 1): end of t's binade
-    const float k = __fmul_rn(step, __int_as_float((127 + 150 - ex) << 23));  // step / u, exact
-    const float kf = floorf(k);
-    if (__fsub_rn(k, kf) == 0.5f) return;
-    const float q = __fmul_rn(rintf(k), u);
-    if (q <= 0.f) return;
-    float nf = floorf(__fdividef(__fsub_rn(lim, t), q)) + 1.f;
-    nf = fminf(nf, floorf(__fdividef(__fsub_rn(top, t), q)));
-    nf = fminf(nf, (float)(LOOP_CAP - loop));
-    int n = nf > 0.f ? (int)nf : 0;
-    while (n > 0 && (__fadd_rn(t, __fmul_rn((float)(n - 1), q)) > lim || __fadd_rn(t, __fmul_rn((float)n, q)) >= top))
-        --n;
-    t = __fadd_rn(t, __fmul_rn((float)n, q));
-    loop += n;
-}
-
-// One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
-template <int DT, int COMP, int SHADE, int EE>
-__device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
-                            int py, Counters& cnt, float2& aux) {
-    using T = typename Vox<DT>::T;
-    const T* __restrict__ bricks = reinterpret_cast<const T*>(P.bricks);
-    const BrickLayout& L = P.L;
-    const int S = L.S, S2 = L.S * L.S;
-    const float step = P.step;
-    float dx = s_(l.x, f.x), dy = s_(l.y, f.y), dz = s_(l.z, f.z);
-    const bool dir0 = dx == 0.f && dy == 0.f && dz == 0.f;
-    const bool last0 = l.x == 0.f && l.y == 0.f && l.z == 0.f;
-    const bool first0 = f.x == 0.f && f.y == 0.f && f.z == 0.f;
-    float tend;
-    if (dir0 && !last0 && !first0) {
-        tend = d_(step, 2.f);
-    } else {
-        tend = len3(dx, dy, dz);
-        const float rl = d_(1.f, tend);
-        dx = m_(dx, rl);
-        dy = m_(dy, rl);
-        dz = m_(dz, rl);
-    }
-    float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
-    float max_int = 0.f;
-    float t = 0.f;
-    float hit_t = -1.f, hit_g = 0.f;  // first sample with alpha > 0 (auxiliary output)
-    bool finished = false;
-    int loop = 0;
-    while (!finished && loop < LOOP_CAP) {
-        const float sx = a_(f.x, m_(t, dx)), sy = a_(f.y, m_(t, dy)), sz = a_(f.z, m_(t, dz));
-        const float vx = clampf_(s_(m_(P.dimf[0], sx), 0.5f), 0.f, P.dim_m1[0]);
-        const float vy = clampf_(s_(m_(P.dimf[1], sy), 0.5f), 0.f, P.dim_m1[1]);
-        const float vz = clampf_(s_(m_(P.dimf[2], sz), 0.5f), 0.f, P.dim_m1[2]);
-        const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
-        const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
-        if (P.occupancy) {
-            // Two skip levels: a whole empty brick-sized cell first, else an
-            // empty fine cell (8^3 by default).
-            float tsafe = 0.f;
-            bool empty = false;
-            if (P.occ_coarse) {
-                const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
-                const long long c = ((long long)cz * P.ncc[1] + cy) * P.ncc[0] + cx;
-                if (((__ldg(P.occ_coarse + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
-                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift_coarse, P.ncc);
-                    empty = true;
-                }
-            }
-            if (!empty) {
-                const int cx = ix >> P.cshift, cy = iy >> P.cshift, cz = iz >> P.cshift;
-                const long long c = ((long long)cz * P.nc[1] + cy) * P.nc[0] + cx;
-                if (((__ldg(P.occupancy + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
-                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift, P.nc);
-                    empty = true;
-                }
-            }
-            if (empty) {
-                // This sample lies in a cell where every reachable TF entry has
-                // alpha 0: it changes nothing. So do all following samples that
-                // provably stay in the cell; only t and the count advance.
-                ++cnt.runs;
-                t = a_(t, step);
-                ++loop;
-                // samples are processed while t <= tend and t <= tsafe: jump to
-                // the end of t's binade in closed form, step across the binade
-                // edge (or a rounding tie) singly, repeat
-                const float lim = fminf(tsafe, tend);
-                while (t <= lim && loop < LOOP_CAP) {
-                    jump_empty_run(t, loop, step, lim);
-                    if (t <= lim && loop < LOOP_CAP) {
-                        t = a_(t, step);
-                        ++loop;
-                    }
-                }
-                finished = t > tend;
-                continue;
-            }
-        }
-        {
-            const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
-            const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
-            ++cnt.fetched;
-            const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
-            const T* __restrict__ b = bricks + brick * L.brick_stride;
-            const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
-                      lz = iz - (bz << L.shift) + APRON_LO;
-            const int o = (lz * S + ly) * S + lx;
-            const float intensity = tri_at<DT>(b, o, S, S2, fx, fy, fz);
-            const float rw = a_(m_(intensity, P.rwm_scale), P.rwm_offset);
-            float4 c = s_tf[tf_index(rw_to_tf(rw, P.tf_lo, P.tf_hi), P.tf_width)];
-            if (c.w > 0.f) {
-                if (SHADE == VRC_SHADE_PHONG) {
-                    ++cnt.shaded;
-                    F3 g;
-                    if (t == 0.f) {
-                        g = clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py);
-                    } else {
-                        // calcGradientA: six lookups at +-1/dim in texture space, each
-                        // clamped like the intensity sample; interpolated on raw values
-                        const float vxp = clampf_(s_(m_(P.dimf[0], a_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
-                        const float vyp = clampf_(s_(m_(P.dimf[1], a_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
-                        const float vzp = clampf_(s_(m_(P.dimf[2], a_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
-                        const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
-                        const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float v0 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
-                        const float v1 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
-                        const float v2 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
-                        const float v3 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
-                        const float v4 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
-                        const float v5 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
-                        g = F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
-                    }
-                    const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
-                                 a_(m_(s_(m_(sy, P.dimf[1]), 0.5f), P.spacing[1]), P.vol_offset[1]),
-                                 a_(m_(s_(m_(sz, P.dimf[2]), 0.5f), P.spacing[2]), P.vol_offset[2])};
-                    if (hit_t < 0.f) hit_g = sqrtf(g.x * g.x + g.y * g.y + g.z * g.z);
-                    const F3 sh = phong_fast(P, g, pos, F3{c.x, c.y, c.z});
-                    c.x = sh.x;
-                    c.y = sh.y;
-                    c.z = sh.z;
-                }
-                if (hit_t < 0.f) hit_t = t;
-                if (COMP == VRC_DVR) {
-                    const float w = m_(s_(1.f, res.w), c.w);
-                    res.x = a_(res.x, m_(w, c.x));
-                    res.y = a_(res.y, m_(w, c.y));
-                    res.z = a_(res.z, m_(w, c.z));
-                    res.w = a_(res.w, m_(s_(1.f, res.w), c.w));
-                } else if (COMP == VRC_MIP) {
-                    if (rw > max_int) {
-                        res = c;
-                        max_int = rw;
-                    }
-                } else {
-                    if (c.w >= s_(P.iso, 0.02f) && c.w <= a_(P.iso, 0.02f)) res = make_float4(c.x, c.y, c.z, 1.f);
-                }
-            }
-        }
-        if (COMP != VRC_MIP && res.w >= P.ert) {
-            res.w = 1.f;
-            finished = true;
-        }
-        t = a_(t, step);
-        ++loop;
-        finished = finished || (t > tend);
-    }
-    cnt.samples += (unsigned long long)loop;
-    aux = hit_t < 0.f ? make_float2(1.f, 0.f) : make_float2(__fdividef(hit_t, fmaxf(tend, 1e-20f)), hit_g * P.aux_gscale);
-    return res;
-}
-
-#ifndef VRC_MARCH_MIN_BLOCKS
-#define VRC_MARCH_MIN_BLOCKS 3
-#endif
-
-template <int DT, int COMP, int SHADE, int EE>
-__global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchParams P) {
-    extern __shared__ float4 s_tf[];
-    for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_table[i];
-    __syncthreads();
-    const int lane = threadIdx.x & 31;
-    const int ntiles = P.tiles_x * P.tiles_y;
-    Counters cnt;
-    for (;;) {
-        int tile = 0;
-        if (lane == 0) tile = (int)atomicAdd(P.tile_counter, 1u);
-        tile = __shfl_sync(FULL, tile, 0);
-        if (tile >= ntiles) break;
-        const int tx = tile % P.tiles_x, ty = tile / P.tiles_x;
-        const int tw = 1 << P.tile_wshift;
-        const int px = P.rx0 + tx * tw + (lane & (tw - 1));
-        const int py = P.ry0 + ty * (32 >> P.tile_wshift) + (lane >> P.tile_wshift);
-        if (px < P.rx1 && py < P.ry1) {
-            const size_t pix = (size_t)py * P.W + px;
-            float4 f, l;
-            if (EE == VRC_EE_BUFFERS) {
-                f = P.entry[pix];
-                l = P.exitp[pix];
-            } else {
-                analytic_entry_exit(P, px, py, f, l);
-            }
-            const bool bg = f.x == 0.f && f.y == 0.f && f.z == 0.f && f.w == 0.f && l.x == 0.f && l.y == 0.f &&
-                            l.z == 0.f && l.w == 0.f;
-            float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
-            float2 ax = make_float2(1.f, 0.f);
-            if (!bg) r = march_ray<DT, COMP, SHADE, EE>(P, s_tf, f, l, px, py, cnt, ax);
-            write_out(P, pix, r);
-            if (P.aux) P.aux[pix] = ax;
-        }
-    }
-    if (P.counters) {
-        unsigned long long a = cnt.samples, b = cnt.fetched, c = cnt.shaded, d = cnt.runs;
-        for (int o = 16; o > 0; o >>= 1) {
-            a += __shfl_xor_sync(FULL, a, o);
-            b += __shfl_xor_sync(FULL, b, o);
-            c += __shfl_xor_sync(FULL, c, o);
-            d += __shfl_xor_sync(FULL, d, o);
-        }
-        if (lane == 0) {
-            atomicAdd(P.counters + 0, a);
-            atomicAdd(P.counters + 1, b);
-            atomicAdd(P.counters + 2, c);
-            atomicAdd(P.counters + 3, d);
-        }
-    }
-}
 
 __global__ void entry_exit_kernel(MarchParams P, float4* entry, float4* exitp) {
     const int px = blockIdx.x * blockDim.x + threadIdx.x, py = blockIdx.y;
@@ -591,52 +16,18 @@ __global__ void entry_exit_kernel(MarchParams P, float4* entry, float4* exitp) {
     exitp[(size_t)py * P.W + px] = l;
 }
 
-template <int DT, int COMP, int SHADE, int EE>
-cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
-    auto k = march_kernel<DT, COMP, SHADE, EE>;
-    const size_t smem = (size_t)p.tf_width * sizeof(float4);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
-    const long long tiles = (long long)p.tiles_x * p.tiles_y;
-    long long grid = (long long)num_sms * per_sm;
-    const long long need = (tiles + 7) / 8;  // 8 warps per CTA
-    if (grid > need) grid = need < 1 ? 1 : need;
-    k<<<(unsigned)grid, 256, smem, s>>>(p);
-    return cudaGetLastError();
-}
-
-template <int DT, int COMP, int SHADE>
-cudaError_t launch_ee(const MarchParams& p, int num_sms, cudaStream_t s) {
-    return p.ee_mode == VRC_EE_ANALYTIC ? launch_t<DT, COMP, SHADE, VRC_EE_ANALYTIC>(p, num_sms, s)
-                                        : launch_t<DT, COMP, SHADE, VRC_EE_BUFFERS>(p, num_sms, s);
-}
-
-template <int DT, int COMP>
-cudaError_t launch_sh(const MarchParams& p, int shading, int num_sms, cudaStream_t s) {
-    return shading == VRC_SHADE_PHONG ? launch_ee<DT, COMP, VRC_SHADE_PHONG>(p, num_sms, s)
-                                      : launch_ee<DT, COMP, VRC_SHADE_NONE>(p, num_sms, s);
-}
-
-template <int DT> cudaError_t launch_comp(const MarchParams& p, int comp, int shading, int num_sms, cudaStream_t s) {
-    switch (comp) {
-        case VRC_MIP: return launch_sh<DT, VRC_MIP>(p, shading, num_sms, s);
-        case VRC_ISO: return launch_sh<DT, VRC_ISO>(p, shading, num_sms, s);
-        default: return launch_sh<DT, VRC_DVR>(p, shading, num_sms, s);
-    }
-}
-
 }  // namespace
 
 cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                          cudaStream_t s) {
-    switch (dtype) {
-        case VRC_U8: return launch_comp<VRC_U8>(p, compositing, shading, num_sms, s);
-        case VRC_U16: return launch_comp<VRC_U16>(p, compositing, shading, num_sms, s);
-        default: return launch_comp<VRC_F32>(p, compositing, shading, num_sms, s);
+    switch (compositing) {
+        case VRC_MIP:
+        case VRC_ISO: return launch_march_mip_iso(p, dtype, compositing, shading, num_sms, s);
+        case VRC_MOP:
+        case VRC_MIDA: return launch_march_mop_mida(p, dtype, compositing, shading, num_sms, s);
+        case VRC_FHP:
+        case VRC_FHN: return launch_march_first_hit(p, dtype, compositing, num_sms, s);
+        default: return launch_march_dvr(p, dtype, shading, num_sms, s);
     }
 }
 

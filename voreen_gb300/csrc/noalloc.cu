@@ -70,6 +70,7 @@ extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf
     if (out_format < VRC_OUT_RGBA8 || out_format > VRC_OUT_RGBA16) return VRC_ERR_INVALID_ARG;
     if (p->entry_exit_mode == VRC_EE_BUFFERS && (!d_entry || !d_exit)) return VRC_ERR_NOT_READY;
     if (tf->width > 4096) return VRC_ERR_SCRATCH_LIMIT;
+    if (p->classification != VRC_CLASSIFY_TF) return VRC_ERR_UNSUPPORTED;  // TF classification only
 
     // empty-space cells: the requested level, else the brick grid (as vrc_render)
     const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
@@ -100,12 +101,12 @@ extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf
 
     // TF table (r/255, g/255, b/255, alpha') into the scratch array; the same
     // host arithmetic as vrc_render's table, so results match it exactly
-    const bool dvr = p->compositing == VRC_DVR;
+    const bool corrected = vrc::alpha_corrected(p->compositing, p->classification);
     const float kcorr = P.step * 200.f;
     for (int i = 0; i < tf->width; ++i) {
         const uint8_t* c = tf->h_rgba + 4 * i;
         float a = float(c[3]) / 255.f;
-        if (dvr) a = 1.f - powf(1.f - a, kcorr);
+        if (corrected) a = 1.f - powf(1.f - a, kcorr);
         t_tf_host[i] = make_float4(float(c[0]) / 255.f, float(c[1]) / 255.f, float(c[2]) / 255.f, a);
     }
     float4* d_tf = reinterpret_cast<float4*>(scratch + COUNTER_BYTES);

@@ -76,7 +76,21 @@ struct MarchParams {
     int rx0, ry0, rx1, ry1;      // rendered pixel window [rx0, rx1) x [ry0, ry1) (the whole image by default)
     float2* aux;                 // optional per pixel (first-hit depth / ray length, |gradient| there), nullptr = off
     float aux_gscale;            // gradient magnitude scale for aux.y
+    const float4* pi_table;      // pre-integration table [back * pi_res + front]; nullptr = classify by the TF
+    int pi_res;
+    float mida_gamma;            // "gammaValue" of MIDA compositing
 };
+
+// Internal compositing code of the march kernels: DVR with pre-integrated
+// classification (no opacity correction, classify(previous, current)).
+constexpr int COMP_DVR_PREINT = 16;
+
+// Whether the TF table carries the opacity correction 1-(1-a)^(step*200):
+// DVR with TF classification (cpuraycaster.cpp:291) and MIDA
+// (mod_compositing.frag:134); MIP / ISO / MOP / FHP / FHN use the TF alpha.
+inline bool alpha_corrected(int compositing, int classification) {
+    return (compositing == VRC_DVR && classification == VRC_CLASSIFY_TF) || compositing == VRC_MIDA;
+}
 
 // One request of a batched launch.
 struct BatchReq {
@@ -95,6 +109,18 @@ vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, f
 // Kernel launchers (march.cu / volume.cu). Return cudaError_t.
 cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                          cudaStream_t s);
+// Per compositing family (one translation unit each, compiled in parallel).
+cudaError_t launch_march_dvr(const MarchParams& p, int dtype, int shading, int num_sms, cudaStream_t s);
+cudaError_t launch_march_mip_iso(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
+                                 cudaStream_t s);
+cudaError_t launch_march_mop_mida(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
+                                  cudaStream_t s);
+cudaError_t launch_march_first_hit(const MarchParams& p, int dtype, int compositing, int num_sms, cudaStream_t s);
+// Exact pre-integration table: one thread per (back, front) entry.
+// tb: res float4 TF entries; a8: their alpha bytes; corr[k * 256 + a] =
+// 1 - (1 - a/255)^(step * 200 / (k + 1)).
+cudaError_t launch_preint_exact(const float4* tb, const uint8_t* a8, const float* corr, int res, float4* out,
+                                cudaStream_t s);
 cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp, cudaStream_t s);
 // Batch: zero the per-launch state and stamp the start time, then one
 // persistent launch over every request's ray tiles (tile_prefix[r] = first
@@ -167,4 +193,14 @@ struct vrc_tf {
     // device float4 tables keyed by (opacity-corrected?, correction exponent bits)
     std::map<std::pair<int, uint32_t>, float4*> tables;
     int* d_prefix = nullptr;  // prefix count of entries with alpha > 0 (width + 1 ints)
+    const vrc_preint* preint = nullptr;  // attached pre-integration table (not owned)
+};
+
+struct vrc_preint {
+    vrc_context* ctx = nullptr;
+    int res = 0;
+    float step = 0.f;
+    int use_integral = 0;
+    float4* d_table = nullptr;  // res * res entries, [back * res + front]
+    int* d_prefix = nullptr;    // prefix count of source entries with alpha > 0 (res + 1 ints)
 };

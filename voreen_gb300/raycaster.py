@@ -6,8 +6,13 @@ reference so tests read like its processor code:
   ports       volumehandle.volumehandle, image.entrypoints, image.exitpoints,
               image.output                       (volumeraycaster.cpp:44-47)
   properties  samplingRate (2.0, 0.01..20), isoValue (0.5), compositing
-              (dvr/mip/iso), shading (none/phong), gradient
-              (central-differences), classification (transfer-function),
+              (dvr/mip/iso/mop/mida/fhp/fhn), gammaValue (MIDA, 0, -1..1),
+              shading (none/phong), gradient (central-differences),
+              classification (transfer-function / pre-integrated-cpu /
+              pre-integrated-approximation; pre-integrated-gpu falls back to
+              pre-integrated-cpu with an error, cpuraycaster.cpp:123-129),
+              preIntegrationTableSize (deriveFromBitDepth = 0 / 256 / 512 /
+              1024, cpuraycaster.cpp:51-74),
               transferFunction (keys + domain + gamma + thresholds),
               lightPosition, lightAmbient, lightDiffuse, lightSpecular,
               materialShininess, applyLightAttenuation, lightAttenuation,
@@ -20,6 +25,9 @@ reference so tests read like its processor code:
               inport changes, renders into image.output. On a failure it logs
               an error and returns without output, as CPURaycaster::process does
               (cpuraycaster.cpp:125-146); `lastError` keeps the message.
+              Pre-integration tables are cached per (step, size, mode), one
+              at a time, like PreIntegrationTableMap's default size 1
+              (preintegrationtablemap.cpp:59-95).
 """
 from __future__ import annotations
 
@@ -28,12 +36,15 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import (DVR, EE_ANALYTIC, EE_BUFFERS, ISO, MIP, OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, Context,
-               TransferFunction, Volume, VrcError, default_params, make_camera, render)
+from . import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, FHN, FHP, ISO, MIDA, MIP, MOP,
+               OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, Context, PreIntegrationTable, TransferFunction, Volume, VrcError,
+               default_params, make_camera, render, sampling_step)
 
 log = logging.getLogger("voreen.CudaRaycaster")
 
-COMPOSITING = {"dvr": DVR, "mip": MIP, "iso": ISO}
+COMPOSITING = {"dvr": DVR, "mip": MIP, "iso": ISO, "mop": MOP, "mida": MIDA, "fhp": FHP, "fhn": FHN}
+CLASSIFICATION = ("transfer-function", "pre-integrated-gpu", "pre-integrated-cpu", "pre-integrated-approximation")
+PREINT_TABLE_SIZES = (0, 256, 512, 1024)
 SHADING = {"none": SHADE_NONE, "phong": SHADE_PHONG}
 
 
@@ -90,6 +101,8 @@ class CudaRaycaster:
         self.shading = "none"
         self.gradient = "central-differences"
         self.classification = "transfer-function"
+        self.preIntegrationTableSize = 0
+        self.gammaValue = 0.0
         self.transferFunction = TransFunc1DKeys()
         self.lightPosition = (2.3, 1.5, 1.5, 1.0)
         self.lightAmbient = (0.4, 0.4, 0.4, 1.0)
@@ -104,12 +117,16 @@ class CudaRaycaster:
         self._ctx = None
         self._vol = None
         self._vol_src = None
+        self._preint = None       # (key, PreIntegrationTable): the cached table
 
     # Processor lifecycle ---------------------------------------------------
     def initialize(self):
         self._ctx = Context(self._device)
 
     def deinitialize(self):
+        if self._preint is not None:
+            self._preint[1].close()
+        self._preint = None
         if self._vol is not None:
             self._vol.close()
         self._vol = None
@@ -134,6 +151,18 @@ class CudaRaycaster:
             tf.domain = (lo * s + o, hi * s + o)
             tf.domain_fitted = True
 
+    def _preint_table(self, step: float) -> PreIntegrationTable:
+        t = self.transferFunction
+        res = PreIntegrationTable.resolution(t.width, self.preIntegrationTableSize)
+        integral = self.classification == "pre-integrated-approximation"
+        key = (step, res, integral, repr(t.keys), t.gamma, tuple(t.threshold))
+        if self._preint is None or self._preint[0] != key:
+            if self._preint is not None:
+                self._preint[1].close()
+            src = PreIntegrationTable.bake_source(t.keys, res, t.gamma, t.threshold)
+            self._preint = (key, PreIntegrationTable(self._ctx, src, step, integral))
+        return self._preint[1]
+
     def process(self, analytic_entry_exit: bool = False):
         if self._ctx is None:
             self.initialize()
@@ -142,6 +171,14 @@ class CudaRaycaster:
             return
         if self.compositing not in COMPOSITING or self.shading not in SHADING:
             self._error(f"unsupported compositing/shading: {self.compositing}/{self.shading}")
+            return
+        if self.classification not in CLASSIFICATION or self.preIntegrationTableSize not in PREINT_TABLE_SIZES:
+            self._error(f"unsupported classification: {self.classification}/{self.preIntegrationTableSize}")
+            return
+        if self.classification == "pre-integrated-gpu":
+            self._error("CPU raycaster does not support computing the pre-integration table on the GPU. "
+                        "Falling back to CPU.")
+            self.classification = "pre-integrated-cpu"
             return
         if not (0.01 <= self.samplingRate <= 20.0):
             self._error(f"samplingRate {self.samplingRate} outside [0.01, 20]")
@@ -168,6 +205,10 @@ class CudaRaycaster:
             p.compositing = COMPOSITING[self.compositing]
             p.shading = SHADING[self.shading]
             p.iso_value = self.isoValue
+            p.mida_gamma = self.gammaValue
+            if self.classification.startswith("pre-integrated"):
+                p.classification = CLASSIFY_PREINTEGRATED
+                tf.set_preintegration(self._preint_table(sampling_step(self._vol, self.samplingRate)))
             p.light_position[:] = list(self.lightPosition)
             p.light_ambient[:] = list(self.lightAmbient)[:3]
             p.light_diffuse[:] = list(self.lightDiffuse)[:3]
