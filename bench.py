@@ -239,6 +239,83 @@ def run_batch(args, warmup, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_preint(args, warmup, ws, rank, local):
+    """Pre-integrated classification on the CT-like workload (DVR + Phong,
+    512^3 u16, 1080p): the exact table (1024 x 1024, the largest size the
+    reference derives) built on the GPU against the same build by the CPU
+    restatement on all host cores, and frames/s of the pre-integrated march
+    against the TF march."""
+    import torch
+
+    import oracle
+    import voreen_gb300 as v
+    from voreen_gb300 import build as vbuild
+    vbuild.build()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = v.Context(dev)
+    w = build_workload(args.small)
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    p = w.params(entry_exit_mode=v.EE_ANALYTIC)
+    res = v.PreIntegrationTable.resolution(w.tf_width)
+    step = v.sampling_step(vol, p.sampling_rate)
+    src = v.PreIntegrationTable.bake_source(w.tf_keys, res)
+    builds = {}
+    exact = None
+    for integral in (False, True):
+        t_gpu = []
+        for k in range(3):
+            t0 = time.perf_counter()
+            tbl = v.PreIntegrationTable(ctx, src, step, integral)
+            t_gpu.append(time.perf_counter() - t0)
+            if k < 2:
+                tbl.close()
+        t0 = time.perf_counter()
+        ref = oracle.preint_table(src, tbl.step, integral)
+        t_cpu = time.perf_counter() - t0
+        equal = bool(np.array_equal(tbl.download().view(np.uint32), ref.view(np.uint32)))
+        builds["integral" if integral else "exact"] = {"gpu_ms": 1e3 * statistics.median(t_gpu),
+                                                        "cpu_ms": 1e3 * t_cpu, "cpu_threads": os.cpu_count(),
+                                                        "equal_to_cpu_build": equal}
+        if integral:
+            tbl.close()
+        else:
+            exact = tbl
+    tf.set_preintegration(exact)
+    out = torch.empty((w.height, w.width, 4), dtype=torch.uint8, device=f"cuda:{dev}")
+    stream = torch.cuda.ExternalStream(ctx.stream, device=f"cuda:{dev}")
+
+    def frames(q):
+        for _ in range(warmup):
+            v.render_async(ctx, vol, tf, q, None, None, out, v.OUT_RGBA8)
+        ctx.synchronize()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.steps):
+            v.render_async(ctx, vol, tf, q, None, None, out, v.OUT_RGBA8)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b) / args.steps
+
+    with ClockSampler(dev) as clk:
+        ms_tf = frames(p)
+        p.classification = v.CLASSIFY_PREINTEGRATED
+        ms_pi = frames(p)
+    _, st = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA8, out)
+    line = {"metric": "pre-integrated DVR frames/s, 512^3 u16 @1080p; table build ms (GPU vs CPU)",
+            "value": 1000.0 / ms_pi, "unit": "frames/s", "n_gpus": ws, "steps": args.steps, "warmup": warmup,
+            "ms_per_step": ms_pi, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded procedural CT-like shells)",
+            "config": {"workload": w.name + " pre-integrated", "table": [res, res], "classification":
+                       "pre-integrated-cpu (exact table)", "l2": "inputs larger than L2"},
+            "tf_classification_frames_per_s": 1000.0 / ms_tf, "samples_per_frame": st.samples,
+            "samples_fetched_per_frame": st.samples_fetched, "table_build": builds,
+            "gpu_launches": args.steps * st.kernel_launches, "clocks": clk.summary()}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def run_learned(args, warmup, ws, rank, local):
     """Learned form on the CT-like workload: half-resolution, half-rate march +
     U-Net (trained weights voreen_gb300/weights/upsampler_ct.npz) + 64x64
@@ -420,10 +497,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
-    ap.add_argument("--workload", default="ct", choices=["ct", "mip", "blobs", "batch", "learned", "large"],
+    ap.add_argument("--workload", default="ct", choices=["ct", "mip", "blobs", "batch", "learned", "large", "preint"],
                     help="ct: 512^3 u16 shaded DVR 1080p (default); mip: the same under MIP; blobs: 128^3 u8 "
                          "DVR 512x512; batch: 64 mixed requests in one launch; learned: upsampler vs plain; "
-                         "large: 2048x2048x1024 u16 at 3840x2160")
+                         "large: 2048x2048x1024 u16 at 3840x2160; preint: pre-integrated classification")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
@@ -454,6 +531,9 @@ def main():
         return
     if args.workload == "large":
         run_large(args, warmup, ws, rank, local)
+        return
+    if args.workload == "preint":
+        run_preint(args, warmup, ws, rank, local)
         return
 
     w = build_workload(args.small, args.workload)
