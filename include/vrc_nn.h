@@ -68,6 +68,28 @@ int vrc_nn_probe_error(const float* a, const float* b, int W, int x0, int y0, in
  * depth, gradient magnitude; nullable) -> BF16 NHWC with 16 channels. */
 int vrc_nn_pack_input(const float* rgba, const float* aux2, long long npix, void* out, void* stream);
 
+/* Mean alpha of each tile x tile block of an RGBA FP32 H x W image into
+ * out[ny][nx] (the learned path's content map for choosing its probe tile). */
+int vrc_nn_tile_alpha(const float* rgba, int H, int W, int tile, int ny, int nx, float* out, void* stream);
+
+/* ---- inference on the 5th-generation tensor cores ------------------------ */
+
+/* out = act(conv3x3([in0 | in1]) + bias) with tcgen05.mma on operands that
+ * TMA stages in shared memory: input channels [0, C0) from in0, [C0, C0 + C1)
+ * from in1 (C1 = 0: in0 only), both NHWC BF16 at N x H x W; C0, C1 multiples
+ * of 16. wtc: the weights rearranged by vrc_nn_weights_tc with the same C0,
+ * C1 and n_split (Cout / n_split output channels per CTA, a multiple of 16, at
+ * most 128). out_mode 0: BF16 NHWC with act (0 none, 1 ReLU, 2 leaky); 1:
+ * FP32 NHWC (act applied likewise). d_err (nullable): set non-zero by a CTA
+ * whose bounded wait gave up (the output is then incomplete). */
+int vrc_nn_conv3x3_tc(const void* in0, int C0, const void* in1, int C1, int N, int H, int W, const void* wtc,
+                      const float* bias, int Cout, int n_split, int act, void* out, int out_mode, int* d_err,
+                      void* stream);
+/* w BF16 [Cout][3][3][C0 + C1] -> the shared-memory operand image that
+ * vrc_nn_conv3x3_tc loads (same size): per output-channel slice, tap and
+ * channel chunk, a block of rows swizzled as the tensor cores read them. */
+int vrc_nn_weights_tc(const void* w, int Cout, int C0, int C1, int n_split, void* wtc, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -147,3 +147,71 @@ def test_fused_decoder_inference_equals_forward(vrc_lib):
     b = net.infer(x0, base)
     torch.cuda.synchronize()
     assert torch.equal(a, b)
+
+
+# ---- tcgen05 inference path ---------------------------------------------------
+@pytest.mark.parametrize("c0,c1,cout,H,W,split,out_f32", [
+    (16, 0, 32, 6, 200, 1, False),     # 32-byte swizzle; two tiles per row, the second partial
+    (32, 0, 64, 13, 131, 1, False),    # 64-byte swizzle
+    (64, 0, 128, 9, 40, 2, False),     # 128-byte swizzle
+    (128, 0, 128, 5, 260, 4, False),   # three tiles per row
+    (128, 64, 64, 7, 96, 2, False),    # two inputs (decoder: upsampled | skip)
+    (64, 32, 32, 8, 130, 1, False),
+    (32, 0, 16, 10, 150, 1, True),     # head: FP32 out
+])
+def test_conv_tc_matches_fp64(vrc_lib, c0, c1, cout, H, W, split, out_f32):
+    """tcgen05 convolution (TMA-staged swizzled operands, tensor-memory
+    accumulators) against FP64 on the same BF16 inputs and weights."""
+    from voreen_gb300.learned import _call, _p, _stream
+    rng = np.random.default_rng(c0 * 3 + c1 + cout + W)
+    cin = c0 + c1
+    x, x64 = bf16(rng.standard_normal((2, H, W, cin)))
+    w, w64 = bf16(rng.standard_normal((cout, 3, 3, cin)) / np.sqrt(9 * cin))
+    b = torch.from_numpy(rng.standard_normal(cout).astype(np.float32)).cuda()
+    ref = R.conv3x3(x64, w64, b.cpu().numpy().astype(np.float64))
+    x0 = x[..., :c0].contiguous()
+    x1 = x[..., c0:].contiguous() if c1 else None
+    wtc = torch.empty_like(w)
+    _call("vrc_nn_weights_tc", _p(w), cout, c0, c1, split, _p(wtc), _stream())
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for act in ((0,) if out_f32 else (0, 2)):
+        y = torch.empty((2, H, W, cout), dtype=torch.float32 if out_f32 else torch.bfloat16, device="cuda")
+        _call("vrc_nn_conv3x3_tc", _p(x0), c0, _p(x1) if c1 else None, c1, 2, H, W, _p(wtc), _p(b), cout,
+              split, act, _p(y), 1 if out_f32 else 0, _p(err), _stream())
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        r = ref if act == 0 else np.where(ref > 0, ref, 0.05 * ref)
+        assert rel_err(y.float().cpu().numpy(), r) < (1e-5 if out_f32 else 8e-3)
+
+
+def test_tile_alpha(vrc_lib):
+    from voreen_gb300.learned import _call, _p, _stream
+    rgba = torch.rand((1, 6, 10, 4), device="cuda")
+    scores = torch.empty((2, 3), dtype=torch.float32, device="cuda")
+    _call("vrc_nn_tile_alpha", _p(rgba), 6, 10, 4, 2, 3, _p(scores), _stream())
+    a = rgba[0, ..., 3].cpu().numpy()
+    ref = [[a[4 * j:4 * j + 4, 4 * i:4 * i + 4].sum() / 16 for i in range(3)] for j in range(2)]
+    np.testing.assert_allclose(scores.cpu().numpy(), ref, rtol=1e-5)
+
+
+def test_infer_tc_matches_infer(vrc_lib):
+    """The whole network on tcgen05 against the mma.sync path: the same BF16
+    weights and inputs; FP32 sums run in another order, so an activation can
+    round to a neighbouring BF16 value."""
+    from voreen_gb300.learned import UNet
+    net = UNet(seed=4)
+    net.w["head"].normal_(0, 0.05)
+    net.refresh()
+    rng = np.random.default_rng(10)
+    N, h, w = 1, 36, 260
+    x_np = np.zeros((N, h, w, 16))
+    x_np[..., :6] = rng.uniform(0, 1, (N, h, w, 6))
+    x0, _ = bf16(x_np)
+    base = torch.from_numpy(rng.uniform(0, 1, (N, h, w, 4)).astype(np.float32)).cuda()
+    a = net.infer(x0, base)
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    b = net.infer_tc(x0, base, err=err)
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    assert rel_err(b.cpu().numpy(), a.cpu().numpy()) < 1e-2
+    assert float((a - b).abs().max()) < 5e-2

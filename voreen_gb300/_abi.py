@@ -129,6 +129,9 @@ NN_SIGNATURES = {
     "vrc_nn_adam": [VP, VP, VP, VP, VP, _LL, _F, _F, _F, _F, _I, VP],
     "vrc_nn_pack_input": [VP, VP, _LL, VP, VP],
     "vrc_nn_probe_error": [VP, VP, _I, _I, _I, _I, _I, VP, VP],
+    "vrc_nn_tile_alpha": [VP, _I, _I, _I, _I, _I, VP, VP],
+    "vrc_nn_conv3x3_tc": [VP, _I, VP, _I, _I, _I, _I, VP, VP, _I, _I, _I, VP, _I, VP, VP],
+    "vrc_nn_weights_tc": [VP, _I, _I, _I, _I, VP, VP],
 }
 
 _lib = None

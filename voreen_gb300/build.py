@@ -36,6 +36,7 @@ SOURCES = [
     ("noalloc.cu", []),
     ("batch.cpp", []),
     ("nn.cu", []),
+    ("nn_tc.cu", []),
     ("synth_tubes.cu", []),
 ]
 

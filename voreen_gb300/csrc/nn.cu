@@ -522,6 +522,26 @@ __global__ void pack_input_kernel(const float* rgba, const float* aux2, long lon
     }
 }
 
+// Mean alpha of each tile x tile block of an RGBA FP32 image (the content
+// map that picks the probe tile); one CTA per block, ny x nx blocks.
+__global__ void tile_alpha_kernel(const float* rgba, int H, int W, int tile, int nx, float* out) {
+    const int bx = blockIdx.x % nx, by = blockIdx.x / nx;
+    float s = 0.f;
+    for (int i = threadIdx.x; i < tile * tile; i += blockDim.x) {
+        const int x = bx * tile + i % tile, y = by * tile + i / tile;
+        if (x < W && y < H) s += rgba[((size_t)y * W + x) * 4 + 3];
+    }
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(FULL, s, o);
+    __shared__ float part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float t = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+        out[blockIdx.x] = t / float(tile * tile);
+    }
+}
+
 // Probe: squared error sum and max |a - b| over a pixel window of two RGBA
 // FP32 images of width W (a: the network's frame, b: the plain render).
 __global__ void probe_error_kernel(const float* a, const float* b, int W, int x0, int y0, int w, int h, float* out2) {
@@ -689,6 +709,12 @@ int vrc_nn_pack_input(const float* rgba, const float* aux2, long long npix, void
     pack_input_kernel<<<ew_grid(npix), 256, 0, static_cast<cudaStream_t>(stream)>>>(rgba, aux2, npix,
                                                                                    static_cast<__nv_bfloat16*>(out));
     return status_of(cudaGetLastError());
+}
+
+int vrc_nn_tile_alpha(const float* rgba, int H, int W, int tile, int ny, int nx, float* out, void* stream) {
+    if (!rgba || !out || tile < 1 || ny < 1 || nx < 1) return 1;
+    tile_alpha_kernel<<<ny * nx, 256, 0, static_cast<cudaStream_t>(stream)>>>(rgba, H, W, tile, nx, out);
+    return cudaGetLastError() == cudaSuccess ? 0 : 2;
 }
 
 }  // extern "C"

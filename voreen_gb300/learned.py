@@ -35,6 +35,18 @@ LAYERS = [  # name, Cin, Cout, activation (2: leaky ReLU, 0: none)
     ("head", 32, 16, 0),
 ]
 LEAK = 0.05
+# Inference layers run on the tcgen05 convolution where it is faster than the
+# mma.sync one on a GB300 at 960 x 540 (measured per layer, microseconds,
+# tcgen05 / mma.sync): enc2a 23 / 25, enc2b 33 / 41, bota 15 / 29, botb 31 / 50,
+# dec2b 33 / 41. With 32 or fewer output channels an MMA of N <= 32 costs
+# about as much as one of N = 64, so the full-resolution layers (enc1a/b,
+# dec1b, head: 40-54 / 25-39) and the decoder inputs [upsample | skip]
+# (fused on load by the mma.sync form) stay on mma.sync.
+TC_LAYERS = ("enc2a", "enc2b", "bota", "botb", "dec2b")
+# Output-channel slices per CTA of the tcgen05 convolution, chosen so each
+# slice's weights (9 x Cin x Cout / split BF16) stay in shared memory beside
+# the operand stages.
+TC_SPLIT = {"botb": 2}
 
 _NN = None
 
@@ -90,11 +102,13 @@ class UNet:
         self.vb = {k: t.zeros_like(v) for k, v in self.b.items()}
 
     def refresh(self):
-        """BF16 copies and the flipped data-gradient weights from the masters."""
+        """BF16 copies and the flipped data-gradient weights from the masters
+        (the tcgen05 inference weights follow on the next infer_tc)."""
         for name, cin, cout, _ in LAYERS:
             self.w16[name].copy_(self.w[name].to(self.torch.bfloat16))
             self.wt16[name] = self.torch.empty((cin, 3, 3, cout), dtype=self.torch.bfloat16, device=self.device)
             _call("vrc_nn_flip_weights", _p(self.w16[name]), cout, cin, _p(self.wt16[name]), _stream())
+        self._wtc_step = None
 
     def state_dict(self):
         return {"step": self.step, "w": {k: v.cpu().numpy() for k, v in self.w.items()},
@@ -152,6 +166,66 @@ class UNet:
         _call("vrc_nn_conv3x3_fwd_upcat", _p(a_half), a_half.shape[3], _p(b), b.shape[3], N, H, W,
               _p(self.w16[name]), _p(self.b[name]), cout, relu, _p(y), 0, _stream())
         return y
+
+    # -- inference on the tcgen05 tensor cores ---------------------------------
+    def _tbuf(self, key, shape, dtype):
+        bufs = self.__dict__.setdefault("_tc_bufs", {})
+        b = bufs.get(key)
+        if b is None or tuple(b.shape) != tuple(shape) or b.dtype != dtype:
+            b = self.torch.empty(shape, dtype=dtype, device=self.device)
+            bufs[key] = b
+        return b
+
+    def _conv_tc(self, name, x, x1, N, H, W, err, out_f32=False):
+        t = self.torch
+        _, cin, cout, act = next(l for l in LAYERS if l[0] == name)
+        c0 = x.shape[3]
+        c1 = x1.shape[3] if x1 is not None else 0
+        assert cin == c0 + c1
+        y = self._tbuf(name, (N, H, W, cout), t.float32 if out_f32 else t.bfloat16)
+        _call("vrc_nn_conv3x3_tc", _p(x), c0, _p(x1) if x1 is not None else None, c1, N, H, W, _p(self.wtc[name]),
+              _p(self.b[name]), cout, TC_SPLIT.get(name, 1), act, _p(y), 1 if out_f32 else 0,
+              _p(err) if err is not None else None, _stream())
+        return y
+
+    def _pool_tc(self, key, x):
+        N, H, W, Cc = x.shape
+        y = self._tbuf(key, (N, H // 2, W // 2, Cc), self.torch.bfloat16)
+        _call("vrc_nn_avgpool2", _p(x), N, H, W, Cc, 1.0, _p(y), _stream())
+        return y
+
+    def infer_tc(self, x0, base, out=None, err=None):
+        """infer() with the layers of TC_LAYERS on the tcgen05 convolution:
+        x0 (N, h, w, 16) BF16 NHWC (h, w multiples of 4), base (N, h, w, 4)
+        FP32. err: optional 4-byte device word the tcgen05 convolutions set
+        when a bounded wait gives up."""
+        t = self.torch
+        if getattr(self, "_wtc_step", None) != self.step:  # weights changed since the last rearrangement
+            self.wtc = {}
+            for name, cin, cout, _ in LAYERS:
+                if name in TC_LAYERS:
+                    self.wtc[name] = t.empty_like(self.w16[name])
+                    _call("vrc_nn_weights_tc", _p(self.w16[name]), cout, cin, 0, TC_SPLIT.get(name, 1),
+                          _p(self.wtc[name]), _stream())
+            self._wtc_step = self.step
+
+        def conv(name, x, N, H, W, out_f32=False):
+            if name in TC_LAYERS:
+                return self._conv_tc(name, x, None, N, H, W, err, out_f32)
+            return self._conv(name, x, N, H, W, out_f32)
+
+        N, H, W, _ = x0.shape
+        H2, W2, H4, W4 = H // 2, W // 2, H // 4, W // 4
+        e1 = conv("enc1b", conv("enc1a", x0, N, H, W), N, H, W)
+        e2 = conv("enc2b", conv("enc2a", self._pool_tc("p1", e1), N, H2, W2), N, H2, W2)
+        b2 = conv("botb", conv("bota", self._pool_tc("p2", e2), N, H4, W4), N, H4, W4)
+        d2 = conv("dec2b", self._conv_upcat("dec2a", b2, e2, N, H2, W2), N, H2, W2)
+        d1 = conv("dec1b", self._conv_upcat("dec1a", d2, e1, N, H, W), N, H, W)
+        f = conv("head", d1, N, H, W, out_f32=True)
+        if out is None:
+            out = t.empty((N, 2 * H, 2 * W, 4), dtype=t.float32, device=self.device)
+        _call("vrc_nn_head_fwd", _p(f), _p(base), N, H, W, _p(out), _stream())
+        return out
 
     def infer(self, x0, base, out=None):
         """Forward without keeping activations; the decoder convolutions build
@@ -361,20 +435,26 @@ def psnr(a, b):
 
 class LearnedRenderer:
     """Half-resolution, half-rate march -> U-Net -> full frame, with a probe:
-    a probe x probe tile of the plain full-rate render is compared with the
-    network's frame every call; if its PSNR falls below `psnr_bound` the frame
-    is rendered by the plain kernel instead (the fallback). Everything runs on
-    the context's stream; the only host synchronisation per frame is reading
-    the probe's error."""
+    a probe x probe tile with content (picked from the previous frame's
+    low-resolution alpha) of the plain full-rate render is compared with the
+    network's frame every call; the frame PSNR is estimated as the tile's
+    error spread over the frame's content tiles, and below `psnr_bound` the
+    frame is rendered by the plain kernel instead (the fallback). The network
+    runs on the tcgen05 convolutions (tensor_cores=True) or the mma.sync ones.
+    Everything runs on the context's stream; the only host synchronisation
+    per frame reads the probe's error words and the content map."""
 
-    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0):
+    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0, tensor_cores: bool = True):
         import torch
         self.ctx, self.net, self.probe, self.bound = ctx, net, probe, psnr_bound
+        self.tensor_cores = tensor_cores
         self.stream = torch.cuda.ExternalStream(ctx.stream)
-        self.err = torch.zeros(2, dtype=torch.float32, device="cuda")
+        # [probe squared error, probe max |d|, convolution timeout word, unused]
+        self.err = torch.zeros(4, dtype=torch.float32, device="cuda")
         self.frames = 0
         self.fallbacks = 0
         self._bufs = {}
+        self._scores = None   # per probe-tile mean alpha of the previous frame (host)
 
     def _buf(self, key, shape, dtype):
         import torch
@@ -385,11 +465,19 @@ class LearnedRenderer:
         return b
 
     def probe_window(self, W, H):
-        """A different probe tile each frame, walking a coarse grid of the image."""
+        """The probe tile: one with content (mean alpha > 0.02 in the previous
+        frame's low-resolution march), a different one each frame; without
+        that map, a walk over a coarse grid. Returns (x, y, w, h, content
+        fraction of the frame or None)."""
         p = self.probe
         nx, ny = max(1, W // p), max(1, H // p)
+        if self._scores is not None and self._scores.shape == (ny, nx):
+            idx = np.flatnonzero(self._scores.reshape(-1) > 0.02)
+            if len(idx):
+                k = int(idx[(self.frames * 7919) % len(idx)])
+                return (k % nx) * p, (k // nx) * p, min(p, W), min(p, H), len(idx) / (nx * ny)
         k = (self.frames * 7919) % (nx * ny)
-        return (k % nx) * p, (k // nx) * p, min(p, W), min(p, H)
+        return (k % nx) * p, (k // nx) * p, min(p, W), min(p, H), None
 
     def _render_plain(self, vol, tf, params, out, region=None):
         from . import EE_ANALYTIC, OUT_RGBA32F, _check, lib
@@ -411,26 +499,42 @@ class LearnedRenderer:
             aux = self._buf("aux", (1, lp.height, lp.width, 2), torch.float32)
             _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None, _p(rgba),
                                         OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
+            out = self._buf("out", (1, H, W, 4), torch.float32)
+            self.err.zero_()
             x0 = self._buf("x0", (1, lp.height, lp.width, 16), torch.bfloat16)
             _call("vrc_nn_pack_input", _p(rgba), _p(aux), lp.height * lp.width, _p(x0), _stream())
-            out = self._buf("out", (1, H, W, 4), torch.float32)
-            self.net.infer(x0, rgba, out)
-            x, y, w, h = self.probe_window(W, H)
+            if self.tensor_cores and lp.height % 4 == 0 and lp.width % 4 == 0:
+                self.net.infer_tc(x0, rgba, out, err=self.err[2:3])
+            else:
+                self.net.infer(x0, rgba, out)
+            # content map of this frame (for the next frame's probe), read back with the error words
+            ny, nx = max(1, H // self.probe), max(1, W // self.probe)
+            scores = self._buf("scores", (ny, nx), torch.float32)
+            _call("vrc_nn_tile_alpha", _p(rgba), lp.height, lp.width, self.probe // 2, ny, nx, _p(scores), _stream())
+            x, y, w, h, content = self.probe_window(W, H)
             ref = self._buf("probe", (H, W, 4), torch.float32)
             self._render_plain(vol, tf, params, ref, region=(x, y, w, h))
-            self.err.zero_()
             _call("vrc_nn_probe_error", _p(out), _p(ref), W, x, y, w, h, _p(self.err), _stream())
-            se, mx = self.err.tolist()  # the one synchronisation
+            host = torch.cat([self.err, scores.reshape(-1)]).cpu()  # the one synchronisation
+            se, mx = float(host[0]), float(host[1])
+            tc_err = int(host[2:3].view(torch.int32)[0])
+            if tc_err:
+                raise RuntimeError(f"tcgen05 convolution gave up waiting (code {tc_err})")
+            self._scores = host[4:].numpy().reshape(ny, nx)
             mse = se / (w * h * 4)
             probe_psnr = float("inf") if mse == 0 else 10 * math.log10(1.0 / mse)
+            # frame estimate: the content tile's error spread over the frame's content
+            est = mse * content if content is not None else mse
+            frame_psnr = float("inf") if est == 0 else 10 * math.log10(1.0 / est)
             self.frames += 1
-            fallback = probe_psnr < self.bound
+            fallback = frame_psnr < self.bound
             frame = out[0]
             if fallback:
                 self.fallbacks += 1
                 frame = self._buf("fallback", (H, W, 4), torch.float32)
                 self._render_plain(vol, tf, params, frame)
-        return frame, {"probe_psnr": probe_psnr, "probe_max_abs": mx, "fallback": fallback}
+        return frame, {"probe_psnr": probe_psnr, "frame_psnr_estimate": frame_psnr, "probe_max_abs": mx,
+                       "fallback": fallback, "probe": (x, y, w, h)}
 
 
 # ---- training on pairs the plain raycaster renders ---------------------------
