@@ -316,6 +316,81 @@ def run_preint(args, warmup, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_upsampler_layers(args, warmup, ws, rank, local):
+    """Every 3x3 convolution of the upsampler at 960 x 540 (random BF16
+    weights and inputs), timed with CUDA events on the tcgen05 kernel (each
+    output-channel split it supports) and on the mma.sync kernel (the decoder
+    inputs fused on load); one JSON line with per-layer microseconds."""
+    import ctypes as C
+
+    import torch
+
+    import voreen_gb300 as v
+    from voreen_gb300 import build as vbuild
+    vbuild.build()
+    torch.cuda.set_device(local if ws > 1 else 0)
+    L = v.lib()
+    H0, W0 = 540, 960
+    layers = [("enc1a", 16, 0, 32, 0, [1]), ("enc1b", 32, 0, 32, 0, [1]), ("enc2a", 32, 0, 64, 1, [1]),
+              ("enc2b", 64, 0, 64, 1, [1]), ("bota", 64, 0, 128, 2, [1, 2]), ("botb", 128, 0, 128, 2, [2, 4]),
+              ("dec2a", 128, 64, 64, 1, [2]), ("dec2b", 64, 0, 64, 1, [1]), ("dec1a", 64, 32, 32, 0, [1]),
+              ("dec1b", 32, 0, 32, 0, [1]), ("head", 32, 0, 16, 0, [1])]
+    steps = max(3, args.steps)
+
+    def timeit(fn):
+        for _ in range(warmup):
+            fn()
+        torch.cuda.synchronize()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(steps):
+            fn()
+        e.record()
+        e.synchronize()
+        return round(a.elapsed_time(e) / steps * 1e3, 1)
+
+    def P(t):
+        return C.c_void_p(t.data_ptr()) if t is not None else None
+
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    result, flops = {}, {}
+    for name, c0, c1, cout, lvl, splits in layers:
+        H, W = H0 >> lvl, W0 >> lvl
+        cin = c0 + c1
+        x0 = (torch.randn((1, H, W, c0), device="cuda", generator=gen) * 0.5).to(torch.bfloat16)
+        x1 = (torch.randn((1, H, W, c1), device="cuda", generator=gen) * 0.5).to(torch.bfloat16) if c1 else None
+        xh = (torch.randn((1, H // 2, W // 2, c0), device="cuda", generator=gen) * 0.5).to(torch.bfloat16) if c1 else None
+        w = (torch.randn((cout, 3, 3, cin), device="cuda", generator=gen) * 0.05).to(torch.bfloat16)
+        b = torch.zeros(cout, device="cuda")
+        of = 1 if name == "head" else 0
+        act = 0 if of else 2
+        y = torch.empty((1, H, W, cout), dtype=torch.float32 if of else torch.bfloat16, device="cuda")
+        r = {}
+        for sp in splits:
+            wtc = torch.empty_like(w)
+            L.vrc_nn_weights_tc(P(w), cout, c0, c1, sp, P(wtc), None)
+            r[f"tcgen05_split{sp}"] = timeit(lambda: L.vrc_nn_conv3x3_tc(P(x0), c0, P(x1), c1, 1, H, W, P(wtc), P(b),
+                                                                         cout, sp, act, P(y), of, None, None))
+        if c1:
+            r["mma_sync_upcat"] = timeit(lambda: L.vrc_nn_conv3x3_fwd_upcat(P(xh), c0, P(x1), c1, 1, H, W, P(w), P(b),
+                                                                            cout, act, P(y), of, None))
+            r["upsample_for_tcgen05"] = timeit(lambda: L.vrc_nn_upsample2(P(xh), 1, H // 2, W // 2, c0, 1.0, P(x0),
+                                                                          None))
+        else:
+            r["mma_sync"] = timeit(lambda: L.vrc_nn_conv3x3_fwd(P(x0), 1, H, W, cin, P(w), P(b), cout, act, P(y), of,
+                                                               None))
+        result[name] = r
+        flops[name] = 2 * H * W * cout * 9 * cin
+    best = {k: min(t for n, t in r.items() if not n.startswith("upsample")) for k, r in result.items()}
+    line = {"metric": "upsampler convolution microseconds per layer at 960x540 (tcgen05 vs mma.sync)",
+            "value": sum(best.values()), "unit": "us (sum of the faster form per layer)", "n_gpus": 1,
+            "steps": steps, "warmup": warmup, "higher_is_better": False, "dtype": "bf16 (fp32 accumulate)",
+            "data": "synthetic (random BF16)", "config": {"workload": "U-Net 32/64/128 layers, 960x540"},
+            "layers_us": result, "tflops_best": {k: round(flops[k] / (best[k] * 1e-6) / 1e12, 1) for k in best}}
+    if rank == 0:
+        print(json.dumps(line))
+
+
 def run_learned(args, warmup, ws, rank, local):
     """Learned form on the CT-like workload: half-resolution, half-rate march +
     U-Net (trained weights voreen_gb300/weights/upsampler_ct.npz) + 64x64
@@ -497,10 +572,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
-    ap.add_argument("--workload", default="ct", choices=["ct", "mip", "blobs", "batch", "learned", "large", "preint"],
+    ap.add_argument("--workload", default="ct",
+                    choices=["ct", "mip", "blobs", "batch", "learned", "large", "preint", "upsampler_layers"],
                     help="ct: 512^3 u16 shaded DVR 1080p (default); mip: the same under MIP; blobs: 128^3 u8 "
                          "DVR 512x512; batch: 64 mixed requests in one launch; learned: upsampler vs plain; "
-                         "large: 2048x2048x1024 u16 at 3840x2160; preint: pre-integrated classification")
+                         "large: 2048x2048x1024 u16 at 3840x2160; preint: pre-integrated classification; "
+                         "upsampler_layers: the learned path's convolutions, tcgen05 vs mma.sync")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
@@ -534,6 +611,9 @@ def main():
         return
     if args.workload == "preint":
         run_preint(args, warmup, ws, rank, local)
+        return
+    if args.workload == "upsampler_layers":
+        run_upsampler_layers(args, warmup, ws, rank, local)
         return
 
     w = build_workload(args.small, args.workload)

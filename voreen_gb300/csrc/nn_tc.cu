@@ -82,13 +82,18 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
 }
 
 // Wait for the phase of parity `parity` to complete; false after WAIT_NS or
-// once another role has given up (abort flag in shared memory).
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+// once another role has given up (abort flag in shared memory). sleep_ns > 0
+// backs off between polls, leaving issue slots to the warps sharing the
+// scheduler (the epilogue warps share theirs with the producer and the MMA
+// issuer).
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, unsigned sleep_ns = 0) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = gtime();
     for (;;) {
-        for (int i = 0; i < 32; ++i)
+        for (int i = 0; i < 32; ++i) {
             if (mbar_try(bar, parity)) return true;
+            if (sleep_ns) __nanosleep(sleep_ns);
+        }
         if (abort_flag && *abort_flag) return false;
         if (gtime() - t0 > WAIT_NS) return false;
     }
@@ -323,7 +328,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int tl = 0;
         for (int t = cta; t < p.pix_tiles; t += ncta, ++tl) {
             const int acc = tl & 1;
-            if (!mbar_wait(tfull0 + 8 * acc, (tl >> 1) & 1, s_abort)) {
+            if (!mbar_wait(tfull0 + 8 * acc, (tl >> 1) & 1, s_abort, 256)) {
                 record_error(p.err, s_abort, 5);
                 break;
             }
