@@ -37,6 +37,9 @@
  *   vrc_tf_set_preintegration  TransFunc1D::getPreIntegrationTable as CPURaycaster
  *                       calls it, transfunc1d.cpp:121-128, cpuraycaster.cpp:112-123
  *   vrc_sampling_step   VolumeRaycaster::getSamplingStepSize / cpuraycaster.cpp:104
+ *   vrc_image_rescale   VolumeRaycaster::rescaleRendering
+ *                       src/core/processors/volumeraycaster.cpp:348-375 (interaction
+ *                       coarseness, singlevolumeraycaster.cpp:253-256)
  *
  * Conventions: images are row-major with row 0 at the bottom (OpenGL window
  * coordinates); entry/exit points are texture-space float4 (w = 1 on hit, the
@@ -241,6 +244,13 @@ typedef struct {
 vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                       const float* entry, const float* exit_pts, int ee_on_device, void* out, int out_format,
                       int out_on_device, vrc_render_stats* stats);
+
+/* Bilinear rescale of a device RGBA image (w x h) to W x H on the context
+ * stream: VolumeRaycaster::rescaleRendering (GL_LINEAR, clamp to edge) as
+ * SingleVolumeRaycaster applies it after an interaction-coarseness render.
+ * format: VRC_OUT_RGBA8 or VRC_OUT_RGBA32F (same for both images). */
+vrc_status vrc_image_rescale(vrc_context* ctx, const void* d_src, int w, int h, void* d_dst, int W, int H,
+                             int format);
 
 /* ---- batched persistent render ----------------------------------------------
  * No counterpart in the reference (it renders one request per processor

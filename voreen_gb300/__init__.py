@@ -24,7 +24,7 @@ from ._abi import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUF
                    Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
 
 __all__ = ["VrcError", "Context", "Volume", "TransferFunction", "PreIntegrationTable", "render", "entry_exit",
-           "default_params", "sampling_step", "camera_matrices", "lib", "DVR", "MIP", "ISO", "MOP", "MIDA", "FHP",
+           "default_params", "sampling_step", "image_rescale", "camera_matrices", "lib", "DVR", "MIP", "ISO", "MOP", "MIDA", "FHP",
            "FHN", "CLASSIFY_TF", "CLASSIFY_PREINTEGRATED", "SHADE_NONE", "SHADE_PHONG", "U8", "U16", "F32",
            "OUT_RGBA8", "OUT_RGBA16", "OUT_RGBA32F", "EE_BUFFERS", "EE_ANALYTIC", "Camera", "RenderParams",
            "RenderStats", "VolumeDesc", "TFKey"]
@@ -266,6 +266,15 @@ class PreIntegrationTable:
             self.close()
         except Exception:
             pass
+
+
+def image_rescale(ctx: Context, src, dst, out_format: int = OUT_RGBA32F):
+    """Bilinear rescale (GL_LINEAR, clamp to edge) of the device RGBA image
+    `src` (h, w, 4) into `dst` (H, W, 4), on the context stream."""
+    h, w = src.shape[0], src.shape[1]
+    H, W = dst.shape[0], dst.shape[1]
+    _check(lib().vrc_image_rescale(ctx.handle, _ptr(src), w, h, _ptr(dst), W, H, out_format), ctx,
+           "vrc_image_rescale")
 
 
 def sampling_step(vol: "Volume", sampling_rate: float) -> float:

@@ -106,6 +106,7 @@ SIGNATURES = {
     "vrc_preint_destroy": (C.c_int, [VP]),
     "vrc_tf_set_preintegration": (C.c_int, [VP, VP]),
     "vrc_sampling_step": (C.c_float, [VP, C.c_float]),
+    "vrc_image_rescale": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, C.c_int]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
     "vrc_synth_tubes_device": (C.c_int, [VP, P(C.c_int), C.c_int, C.c_uint64, C.c_float, VP]),
 }

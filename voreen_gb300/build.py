@@ -33,6 +33,7 @@ SOURCES = [
     ("march_mop_mida.cu", ["-fmad=false"]),
     ("march_first_hit.cu", ["-fmad=false"]),
     ("preint.cu", ["-fmad=false"]),
+    ("image.cu", []),
     ("noalloc.cu", []),
     ("batch.cpp", []),
     ("nn.cu", []),

@@ -12,7 +12,9 @@ reference so tests read like its processor code:
               pre-integrated-approximation; pre-integrated-gpu falls back to
               pre-integrated-cpu with an error, cpuraycaster.cpp:123-129),
               preIntegrationTableSize (deriveFromBitDepth = 0 / 256 / 512 /
-              1024, cpuraycaster.cpp:51-74),
+              1024, cpuraycaster.cpp:51-74), interactionCoarseness (3,
+              1..8) and interactionQuality (1.0, 0.01..1)
+              (volumeraycaster.cpp:65-66),
               transferFunction (keys + domain + gamma + thresholds),
               lightPosition, lightAmbient, lightDiffuse, lightSpecular,
               materialShininess, applyLightAttenuation, lightAttenuation,
@@ -28,6 +30,15 @@ reference so tests read like its processor code:
               Pre-integration tables are cached per (step, size, mode), one
               at a time, like PreIntegrationTableMap's default size 1
               (preintegrationtablemap.cpp:59-95).
+              process(interacting=True) renders as SingleVolumeRaycaster does
+              in interaction mode (singlevolumeraycaster.cpp:253-256): at
+              output size / interactionCoarseness (integer division) with the
+              sampling rate times interactionQuality
+              (VolumeRaycaster::getSamplingStepSize, volumeraycaster.cpp:312-322),
+              then rescaled bilinearly to the output size
+              (rescaleRendering, volumeraycaster.cpp:348-375). The coarse
+              frame's rays go through the coarse pixel centres (analytic
+              entry/exit at the coarse size).
 """
 from __future__ import annotations
 
@@ -38,7 +49,7 @@ import numpy as np
 
 from . import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, FHN, FHP, ISO, MIDA, MIP, MOP,
                OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, Context, PreIntegrationTable, TransferFunction, Volume, VrcError,
-               default_params, make_camera, render, sampling_step)
+               default_params, image_rescale, make_camera, render, sampling_step)
 
 log = logging.getLogger("voreen.CudaRaycaster")
 
@@ -103,6 +114,8 @@ class CudaRaycaster:
         self.classification = "transfer-function"
         self.preIntegrationTableSize = 0
         self.gammaValue = 0.0
+        self.interactionCoarseness = 3
+        self.interactionQuality = 1.0
         self.transferFunction = TransFunc1DKeys()
         self.lightPosition = (2.3, 1.5, 1.5, 1.0)
         self.lightAmbient = (0.4, 0.4, 0.4, 1.0)
@@ -163,7 +176,7 @@ class CudaRaycaster:
             self._preint = (key, PreIntegrationTable(self._ctx, src, step, integral))
         return self._preint[1]
 
-    def process(self, analytic_entry_exit: bool = False):
+    def process(self, analytic_entry_exit: bool = False, interacting: bool = False):
         if self._ctx is None:
             self.initialize()
         if not (self.volumeInport.hasData() and (analytic_entry_exit or self.isReady())):
@@ -179,6 +192,9 @@ class CudaRaycaster:
             self._error("CPU raycaster does not support computing the pre-integration table on the GPU. "
                         "Falling back to CPU.")
             self.classification = "pre-integrated-cpu"
+            return
+        if not (1 <= int(self.interactionCoarseness) <= 8) or not (0.01 <= self.interactionQuality <= 1.0):
+            self._error(f"interaction settings out of range: {self.interactionCoarseness}/{self.interactionQuality}")
             return
         if not (0.01 <= self.samplingRate <= 20.0):
             self._error(f"samplingRate {self.samplingRate} outside [0.01, 20]")
@@ -218,7 +234,22 @@ class CudaRaycaster:
             p.light_attenuation[:] = list(self.lightAttenuation)
             p.camera = self.camera
             p.entry_exit_mode = EE_ANALYTIC if analytic_entry_exit else EE_BUFFERS
-            img, stats = render(self._ctx, self._vol, tf, p, entry, exit_pts, OUT_RGBA32F)
+            coarse = interacting and int(self.interactionCoarseness) > 1
+            if interacting:
+                p.sampling_rate = self.samplingRate * self.interactionQuality
+            if coarse:
+                import torch
+                c = int(self.interactionCoarseness)
+                p.width, p.height = max(1, W // c), max(1, H // c)
+                p.entry_exit_mode = EE_ANALYTIC
+                small = torch.empty((p.height, p.width, 4), dtype=torch.float32, device=f"cuda:{self._device}")
+                _, stats = render(self._ctx, self._vol, tf, p, None, None, OUT_RGBA32F, small)
+                full = torch.empty((H, W, 4), dtype=torch.float32, device=f"cuda:{self._device}")
+                image_rescale(self._ctx, small, full, OUT_RGBA32F)
+                self._ctx.synchronize()
+                img = full.cpu().numpy()
+            else:
+                img, stats = render(self._ctx, self._vol, tf, p, entry, exit_pts, OUT_RGBA32F)
             tf.close()
             self.outport.setData(img)
             self.lastStats = stats
