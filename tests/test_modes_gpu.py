@@ -71,12 +71,14 @@ def test_preint_table_equals_oracle(ctx, orc, res, integral):
     np.testing.assert_array_equal(_bits(got), _bits(ref))
 
 
-def _preint_case(ctx, orc, integral, vol_kind, shading=v.SHADE_NONE, res=0):
+def _preint_case(ctx, orc, integral, vol_kind, shading=v.SHADE_NONE, res=0, rate=None):
     if vol_kind == "blobs":
         w = synth.config1(size=(64, 72, 56), image=(160, 128))
     else:
         w = synth.config2(size=(96, 80, 72), image=(200, 150))
     p = w.params(shading=shading)
+    if rate is not None:
+        p.sampling_rate = rate
     p.classification = v.CLASSIFY_PREINTEGRATED
     tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
     c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing)
@@ -87,10 +89,14 @@ def _preint_case(ctx, orc, integral, vol_kind, shading=v.SHADE_NONE, res=0):
     return c, table
 
 
-@pytest.mark.parametrize("integral,vol_kind", [(False, "blobs"), (True, "blobs"), (False, "shells"),
-                                               (True, "shells")])
-def test_preint_render_bit_exact(ctx, orc, integral, vol_kind):
-    c, table = _preint_case(ctx, orc, integral, vol_kind)
+@pytest.mark.parametrize("integral,vol_kind,rate", [(False, "blobs", None), (True, "blobs", None),
+                                                    (False, "shells", None), (True, "shells", None),
+                                                    (False, "shells", 0.8), (False, "shells", 1.0)])
+def test_preint_render_bit_exact(ctx, orc, integral, vol_kind, rate):
+    """Rates above 1 let empty-to-empty segments skip (a step moves less than a
+    voxel per axis); at rate <= 1 the first sample of every empty run is
+    classified as usual."""
+    c, table = _preint_case(ctx, orc, integral, vol_kind, rate=rate)
     img, st = c.gpu()
     o32, s32, _ = c.oracle(32, preint_table=table.download())
     assert st.samples == s32.sum()

@@ -675,6 +675,10 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: the pre-integration table was built for another step size");
         P.pi_table = pi->d_table;
         P.pi_res = pi->res;
+        {
+            const int* d = vol->desc.dims;
+            P.pi_chain = P.step * float(std::max(d[0], std::max(d[1], d[2]))) <= 0.99f ? 1 : 0;
+        }
         P.tf_table = nullptr;
         P.tf_width = 0;  // the TF table is not read
         occ_prefix = pi->d_prefix;

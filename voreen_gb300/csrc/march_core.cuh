@@ -454,6 +454,10 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     float4 res = make_float4(0.f, 0.f, 0.f, 0.f);
     float max_int = 0.f;
     float last = 0.f;  // lastIntensity (cpuraycaster.cpp:235), TF-normalised
+    // pre-integration: whether the previous sample lay in an empty cell, and
+    // whether `last` still has to be read at t_last (the last skipped sample)
+    bool prev_empty = false, last_stale = false;
+    float t_last = 0.f;
     float t = 0.f;
     float hit_t = -1.f, hit_g = 0.f;  // first sample with alpha > 0 (auxiliary output)
     bool finished = false;
@@ -488,7 +492,30 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     empty = true;
                 }
             }
-            if (PI && empty) {
+            if (PI && empty && P.pi_chain && prev_empty) {
+                // This sample and the previous one lie in empty cells that
+                // share a voxel (a step moves less than a voxel per axis), so
+                // their value ranges overlap and every table entry between
+                // the two samples has alpha 0: skip it and the rest of its
+                // cell; `last` is read when a sample is next classified.
+                ++cnt.runs;
+                float tp = t;
+                t = a_(t, step);
+                ++loop;
+                const float lim = fminf(tsafe, tend);
+                while (t <= lim && loop < LOOP_CAP) {
+                    jump_empty_run<true>(t, loop, step, lim, &tp);
+                    if (t <= lim && loop < LOOP_CAP) {
+                        tp = t;
+                        t = a_(t, step);
+                        ++loop;
+                    }
+                }
+                finished = t > tend;
+                last_stale = true;
+                t_last = tp;
+                continue;
+            } else if (PI && empty) {
                 // A pre-integrated colour also depends on the previous sample,
                 // which may lie outside the cell: classify this sample as
                 // usual, skip the ones after it that stay in the cell (both
@@ -531,6 +558,18 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             const float rw = a_(m_(intensity, P.rwm_scale), P.rwm_offset);
             float4 c;
             if (PI) {
+                if (last_stale) {  // the previous sample was skipped: read its TF coordinate
+                    ++cnt.fetched;
+                    const float px_ = a_(f.x, m_(t_last, dx)), py_ = a_(f.y, m_(t_last, dy)),
+                                pz_ = a_(f.z, m_(t_last, dz));
+                    const float rwp = a_(m_(tap_norm<DT>(P, bricks, to_voxel(P, 0, px_), to_voxel(P, 1, py_),
+                                                        to_voxel(P, 2, pz_)),
+                                            P.rwm_scale),
+                                         P.rwm_offset);
+                    last = rw_to_tf(rwp, P.tf_lo, P.tf_hi);
+                    last_stale = false;
+                }
+                prev_empty = skip_after;  // this sample is classified; its cell was empty iff skip_after
                 // PreIntegrationTable::classify(last, cur) (preintegrationtable.cpp:256-279)
                 const float cur = rw_to_tf(rw, P.tf_lo, P.tf_hi);
                 c = __ldg(P.pi_table + (size_t)tf_index(cur, P.pi_res) * P.pi_res + tf_index(last, P.pi_res));
@@ -644,14 +683,9 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                 }
             }
             finished = t > tend;
-            if (skipped && !finished) {
-                ++cnt.fetched;
-                const float px_ = a_(f.x, m_(tp, dx)), py_ = a_(f.y, m_(tp, dy)), pz_ = a_(f.z, m_(tp, dz));
-                const float rwp = a_(m_(tap_norm<DT>(P, bricks, to_voxel(P, 0, px_), to_voxel(P, 1, py_),
-                                                    to_voxel(P, 2, pz_)),
-                                        P.rwm_scale),
-                                     P.rwm_offset);
-                last = rw_to_tf(rwp, P.tf_lo, P.tf_hi);
+            if (skipped) {  // `last` is read when a sample is next classified
+                last_stale = true;
+                t_last = tp;
             }
         }
     }

@@ -78,6 +78,7 @@ struct MarchParams {
     float aux_gscale;            // gradient magnitude scale for aux.y
     const float4* pi_table;      // pre-integration table [back * pi_res + front]; nullptr = classify by the TF
     int pi_res;
+    int pi_chain;                // a step moves less than 0.99 voxel per axis: empty-to-empty segments skip
     float mida_gamma;            // "gammaValue" of MIDA compositing
 };
 
