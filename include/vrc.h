@@ -54,7 +54,7 @@
 extern "C" {
 #endif
 
-#define VRC_ABI_VERSION 1
+#define VRC_ABI_VERSION 2
 
 typedef enum {
     VRC_OK = 0,
@@ -218,6 +218,12 @@ typedef struct {
     int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
     int classification;         /* vrc_classification, default VRC_CLASSIFY_TF */
     float mida_gamma;           /* "gammaValue" for VRC_MIDA, in [-1, 1], default 0 */
+    /* Proxy-geometry clipping of analytic entry/exit (and vrc_entry_exit):
+     * OptimizedProxyGeometry "enableClipping" / "clipRegion", an inclusive
+     * voxel box; the cube becomes [llf - 0.5, urb + 0.5] in voxel coordinates
+     * (optimizedproxygeometry.cpp:420-448). Ignored in buffer mode. */
+    int enable_clipping;
+    int clip_llf[3], clip_urb[3];
 } vrc_render_params;
 
 /* Fills `p` with the reference's property defaults for a W x H image. */

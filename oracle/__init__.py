@@ -63,6 +63,8 @@ def lib():
                                            C.c_void_p]
         L.oracle_preint_table.argtypes = [C.c_void_p, C.c_int, C.c_float, C.c_int, C.c_void_p]
         L.oracle_entry_exit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
+        L.oracle_entry_exit_box.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p,
+                                            C.c_void_p, C.c_void_p]
         for name in ("oracle_render_f32", "oracle_render_f64"):
             getattr(L, name).argtypes = [P(OrcVolume), P(OrcTF), P(OrcParams), C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -157,11 +159,18 @@ def preint_table(source_rgba: np.ndarray, step: float, use_integral: bool = Fals
     return out
 
 
-def entry_exit(inv_mvp: np.ndarray, width: int, height: int, quantize16: bool = False):
+def entry_exit(inv_mvp: np.ndarray, width: int, height: int, quantize16: bool = False, box=None):
+    """box: ((lo x, y, z), (hi x, y, z)) texture-space clip box, None = the unit cube."""
     m = np.ascontiguousarray(inv_mvp, dtype=np.float64)
     e = np.zeros((height, width, 4), np.float32)
     x = np.zeros((height, width, 4), np.float32)
-    lib().oracle_entry_exit(_ptr(m), width, height, 1 if quantize16 else 0, _ptr(e), _ptr(x))
+    if box is None:
+        lib().oracle_entry_exit(_ptr(m), width, height, 1 if quantize16 else 0, _ptr(e), _ptr(x))
+    else:
+        lo = np.ascontiguousarray(box[0], dtype=np.float64)
+        hi = np.ascontiguousarray(box[1], dtype=np.float64)
+        lib().oracle_entry_exit_box(_ptr(m), width, height, 1 if quantize16 else 0, _ptr(lo), _ptr(hi), _ptr(e),
+                                    _ptr(x))
     return e, x
 
 

@@ -568,6 +568,12 @@ void oracle_preint_table(const uint8_t* src, int res, float d, int use_integral,
 }
 
 void oracle_entry_exit(const double* m, int W, int H, int quantize16, float* entry, float* exitp) {
+    const double lo[3] = {0.0, 0.0, 0.0}, hi[3] = {1.0, 1.0, 1.0};
+    oracle_entry_exit_box(m, W, H, quantize16, lo, hi, entry, exitp);
+}
+
+void oracle_entry_exit_box(const double* m, int W, int H, int quantize16, const double* box_lo, const double* box_hi,
+                           float* entry, float* exitp) {
 #ifdef _OPENMP
 #pragma omp parallel for schedule(static)
 #endif
@@ -592,9 +598,9 @@ void oracle_entry_exit(const double* m, int W, int H, int quantize16, float* ent
             bool hit = true;
             for (int i = 0; i < 3 && hit; ++i) {
                 if (d[i] == 0.0) {
-                    if (o[i] < 0.0 || o[i] > 1.0) hit = false;
+                    if (o[i] < box_lo[i] || o[i] > box_hi[i]) hit = false;
                 } else {
-                    double a = (0.0 - o[i]) / d[i], b = (1.0 - o[i]) / d[i];
+                    double a = (box_lo[i] - o[i]) / d[i], b = (box_hi[i] - o[i]) / d[i];
                     if (a > b) std::swap(a, b);
                     s0 = std::max(s0, a);
                     s1 = std::min(s1, b);
@@ -608,8 +614,8 @@ void oracle_entry_exit(const double* m, int W, int H, int quantize16, float* ent
             }
             for (int i = 0; i < 3; ++i) {
                 double a = o[i] + s0 * d[i], b = o[i] + s1 * d[i];
-                a = std::min(1.0, std::max(0.0, a));
-                b = std::min(1.0, std::max(0.0, b));
+                a = std::min(box_hi[i], std::max(box_lo[i], a));
+                b = std::min(box_hi[i], std::max(box_lo[i], b));
                 if (quantize16) {
                     a = std::floor(a * 65535.0 + 0.5) / 65535.0;
                     b = std::floor(b * 65535.0 + 0.5) / 65535.0;

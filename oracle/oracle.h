@@ -96,6 +96,11 @@ void oracle_preint_table(const uint8_t* source_rgba, int res, float step, int us
  * the whole pixel is 0). */
 void oracle_entry_exit(const double* inv_mvp, int width, int height, int quantize16,
                        float* entry_rgba, float* exit_rgba);
+/* The same for the proxy cube clipped to [box_lo, box_hi] in texture space
+ * (OptimizedProxyGeometry::processCube with clipping,
+ * modules/base/processors/proxygeometry/optimizedproxygeometry.cpp:420-448). */
+void oracle_entry_exit_box(const double* inv_mvp, int width, int height, int quantize16, const double* box_lo,
+                           const double* box_hi, float* entry_rgba, float* exit_rgba);
 
 /* Full-frame march. entry/exit: W*H float4. out: W*H float4 (RGBA, not
  * clamped). samples_out (nullable): per-pixel loop iteration count.

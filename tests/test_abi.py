@@ -31,7 +31,7 @@ def test_python_signatures_cover_the_headers(vrc_lib):
 
 
 def test_host_only_entry_points_work_without_gpu(vrc_lib):
-    assert vrc_lib.vrc_abi_version() == 1
+    assert vrc_lib.vrc_abi_version() == 2
     assert vrc_lib.vrc_status_string(0) == b"ok"
     assert vrc_lib.vrc_tf_table_width(0) == 256
     assert vrc_lib.vrc_tf_table_width(1) == 4096

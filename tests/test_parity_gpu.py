@@ -150,6 +150,41 @@ def test_analytic_entry_exit_matches_buffers(ctx):
     np.testing.assert_array_equal(_bits(img_a), _bits(img_b))
 
 
+def test_clip_region_entry_exit(ctx):
+    """Proxy-geometry clipping (OptimizedProxyGeometry clipRegion): analytic
+    entry/exit on the clipped cube against the FP64 oracle's, rendering from
+    them equals rendering in analytic mode, and the march only reaches the
+    clip box (+ the half-voxel border)."""
+    w = synth.config2(size=(64, 60, 56), image=(160, 120), compositing=v.DVR)
+    p = w.params(shading=v.SHADE_NONE)
+    p.enable_clipping = 1
+    p.clip_llf[:] = [8, 5, 20]
+    p.clip_urb[:] = [40, 59, 50]
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, p, w.spacing, entry=np.zeros((1,)), exit_pts=np.zeros((1,)))
+    e, x = v.entry_exit(ctx, c.vol, p)
+    dims = np.array(c.vol.dims, np.float64)
+    lo = np.maximum(0.0, np.array([8, 5, 20]) / dims)
+    hi = np.minimum(1.0, (np.array([40, 59, 50]) + 1.0) / dims)
+    _, _, inv = v.camera_matrices(p.camera, c.vol.desc, p.width, p.height)
+    oe, ox = oracle.entry_exit(inv, p.width, p.height, False, box=(lo, hi))
+    hit = (e[..., 3] > 0) & (oe[..., 3] > 0)
+    assert hit.sum() > 100
+    assert ((e[..., 3] > 0) != (oe[..., 3] > 0)).sum() <= 0.002 * hit.sum() + 2
+    assert np.abs(e[hit] - oe[hit]).max() < 2e-5 and np.abs(x[hit] - ox[hit]).max() < 2e-5
+    pts = np.concatenate([e[hit][:, :3], x[hit][:, :3]])
+    assert np.all(pts >= lo - 1e-6) and np.all(pts <= hi + 1e-6)
+    img_b, _ = v.render(ctx, c.vol, c.tf, p, e, x, v.OUT_RGBA32F)
+    p.entry_exit_mode = v.EE_ANALYTIC
+    img_a, _ = v.render(ctx, c.vol, c.tf, p, None, None, v.OUT_RGBA32F)
+    np.testing.assert_array_equal(_bits(img_a), _bits(img_b))
+    o32, _, _ = c.oracle(32, entry=e, exit_pts=x)
+    np.testing.assert_array_equal(_bits(img_b), _bits(o32))
+    p.clip_llf[0] = 50  # llf > urb
+    with pytest.raises(v.VrcError, match="INVALID_ARG"):
+        v.render(ctx, c.vol, c.tf, p, None, None, v.OUT_RGBA32F)
+
+
 def test_output_formats(ctx):
     w, c = _c1_case(ctx, size=(48, 40, 36), image=(96, 64))
     f32, _ = c.gpu(v.OUT_RGBA32F)

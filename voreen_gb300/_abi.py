@@ -48,7 +48,8 @@ class RenderParams(C.Structure):
                 ("light_attenuation", C.c_float * 3), ("camera", Camera), ("entry_exit_mode", C.c_int),
                 ("quantize_entry_exit", C.c_int), ("empty_space_skipping", C.c_int), ("skip_cell_size", C.c_int),
                 ("tile_width", C.c_int), ("region", C.c_int * 4), ("classification", C.c_int),
-                ("mida_gamma", C.c_float)]
+                ("mida_gamma", C.c_float), ("enable_clipping", C.c_int), ("clip_llf", C.c_int * 3),
+                ("clip_urb", C.c_int * 3)]
 
 
 class BatchItem(C.Structure):

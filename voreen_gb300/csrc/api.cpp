@@ -599,6 +599,21 @@ vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render
     }
     P.tiles_x = (P.rx1 - P.rx0 + tw - 1) / tw;
     P.tiles_y = (P.ry1 - P.ry0 + (32 / tw) - 1) / (32 / tw);
+    for (int i = 0; i < 3; ++i) {
+        P.box_lo[i] = 0.f;
+        P.box_hi[i] = 1.f;
+    }
+    if (p->enable_clipping) {
+        // OptimizedProxyGeometry::processCube: voxel box [llf - 0.5, urb + 0.5]
+        // intersected with the volume, then voxelToTexture = (v + 0.5) / dim
+        for (int i = 0; i < 3; ++i) {
+            if (p->clip_llf[i] > p->clip_urb[i])
+                return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: clip region with llf > urb");
+            const double dim = double(d.dims[i]);
+            P.box_lo[i] = float(std::max(0.0, double(p->clip_llf[i]) / dim));
+            P.box_hi[i] = float(std::min(1.0, (double(p->clip_urb[i]) + 1.0) / dim));
+        }
+    }
     if (p->entry_exit_mode == VRC_EE_ANALYTIC) {
         double inv[16];
         if (vrc_camera_matrices(&p->camera, &d, p->width, p->height, nullptr, nullptr, inv) != VRC_OK)

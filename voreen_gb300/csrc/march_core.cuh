@@ -242,9 +242,9 @@ __device__ bool analytic_entry_exit(const MarchParams& P, int px, int py, float4
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
         if (d[i] == 0.f) {
-            if (o[i] < 0.f || o[i] > 1.f) hit = false;
+            if (o[i] < P.box_lo[i] || o[i] > P.box_hi[i]) hit = false;
         } else {
-            float a = d_(s_(0.f, o[i]), d[i]), b = d_(s_(1.f, o[i]), d[i]);
+            float a = d_(s_(P.box_lo[i], o[i]), d[i]), b = d_(s_(P.box_hi[i], o[i]), d[i]);
             if (a > b) {
                 const float t = a;
                 a = b;
@@ -262,8 +262,8 @@ __device__ bool analytic_entry_exit(const MarchParams& P, int px, int py, float4
     float en[3], ex[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-        float a = clampf_(a_(o[i], m_(s0, d[i])), 0.f, 1.f);
-        float b = clampf_(a_(o[i], m_(s1, d[i])), 0.f, 1.f);
+        float a = clampf_(a_(o[i], m_(s0, d[i])), P.box_lo[i], P.box_hi[i]);
+        float b = clampf_(a_(o[i], m_(s1, d[i])), P.box_lo[i], P.box_hi[i]);
         if (P.quantize) {
             a = d_(floorf(a_(m_(a, 65535.f), 0.5f)), 65535.f);
             b = d_(floorf(a_(m_(b, 65535.f), 0.5f)), 65535.f);

@@ -66,6 +66,7 @@ struct MarchParams {
     const float4* entry;
     const float4* exitp;
     float inv_mvp[16];
+    float box_lo[3], box_hi[3];  // proxy cube in texture space ([0, 1] unless clipped)
     void* out;
     int out_format;
     unsigned long long* counters;  // [samples, fetched, shaded]

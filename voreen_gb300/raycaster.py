@@ -116,6 +116,10 @@ class CudaRaycaster:
         self.gammaValue = 0.0
         self.interactionCoarseness = 3
         self.interactionQuality = 1.0
+        # proxy geometry of the analytic entry/exit (OptimizedProxyGeometry
+        # "enableClipping" / "clipRegion": inclusive voxel box (llf, urb))
+        self.enableClipping = False
+        self.clipRegion = None
         self.transferFunction = TransFunc1DKeys()
         self.lightPosition = (2.3, 1.5, 1.5, 1.0)
         self.lightAmbient = (0.4, 0.4, 0.4, 1.0)
@@ -234,6 +238,10 @@ class CudaRaycaster:
             p.light_attenuation[:] = list(self.lightAttenuation)
             p.camera = self.camera
             p.entry_exit_mode = EE_ANALYTIC if analytic_entry_exit else EE_BUFFERS
+            if self.enableClipping and self.clipRegion is not None:
+                p.enable_clipping = 1
+                p.clip_llf[:] = [int(c) for c in self.clipRegion[0]]
+                p.clip_urb[:] = [int(c) for c in self.clipRegion[1]]
             coarse = interacting and int(self.interactionCoarseness) > 1
             if interacting:
                 p.sampling_rate = self.samplingRate * self.interactionQuality
