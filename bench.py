@@ -316,6 +316,73 @@ def run_preint(args, warmup, ws, rank, local):
         print(json.dumps(line))
 
 
+def run_ingest(args, warmup, ws, rank, local):
+    """Volume ingest: the 512^3 uint16 CT-like volume written as a .vvd + .raw
+    pair (256 MiB, in the page cache after writing), loaded by
+    vrc_volume_load_vvd (file -> two pinned 64 MiB chunks -> device ->
+    bricks + min/max) against a plain host read of the raw file (what a CPU
+    reader does) and an upload of the same voxels from host memory."""
+    import shutil
+
+    import torch
+
+    import voreen_gb300 as v
+    from voreen_gb300 import build as vbuild
+    vbuild.build()
+    dev = local if ws > 1 else 0
+    torch.cuda.set_device(dev)
+    ctx = v.Context(dev)
+    w = build_workload(args.small)
+    tmp = tempfile.mkdtemp(prefix="vrc_ingest_")
+    try:
+        path = os.path.join(tmp, "ct.vvd")
+        raw = v.write_vvd(path, w.voxels, spacing=w.spacing)
+        nbytes = os.path.getsize(raw)
+        steps = max(3, min(args.steps, 20))
+
+        def timed(fn):
+            for _ in range(warmup):
+                fn()
+            ts = []
+            for _ in range(steps):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                fn()
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            return statistics.median(ts)
+
+        def load():
+            vol = v.Volume.load_vvd(ctx, path)
+            ctx.synchronize()
+            vol.close()
+
+        def host_read():
+            np.fromfile(raw, np.uint16)
+
+        def upload():
+            vol = v.Volume(ctx, w.voxels, w.spacing)
+            ctx.synchronize()
+            vol.close()
+
+        t_load, t_read, t_up = timed(load), timed(host_read), timed(upload)
+        vol = v.Volume.load_vvd(ctx, path)
+        ref = v.Volume(ctx, w.voxels, w.spacing)
+        same = vol.minmax() == ref.minmax() and vol.device_bytes == ref.device_bytes
+        line = {"metric": "volume ingest GB/s (.vvd raw file -> bricked device volume with min/max)",
+                "value": nbytes / t_load / 1e9, "unit": "GB/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
+                "ms_per_step": t_load * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "u16", "data": "synthetic (seeded procedural CT-like shells, written as .vvd + .raw)",
+                "config": {"workload": f"{w.dims[0]}x{w.dims[1]}x{w.dims[2]} u16 .vvd ingest", "bytes": nbytes,
+                           "page_cache": "warm (file just written)"},
+                "host_read_gbs": nbytes / t_read / 1e9, "upload_from_host_memory_gbs": nbytes / t_up / 1e9,
+                "loaded_equals_uploaded": bool(same), "device_bytes": vol.device_bytes}
+        if rank == 0:
+            print(json.dumps(line))
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+
+
 def run_upsampler_layers(args, warmup, ws, rank, local):
     """Every 3x3 convolution of the upsampler at 960 x 540 (random BF16
     weights and inputs), timed with CUDA events on the tcgen05 kernel (each
@@ -573,11 +640,13 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--small", action="store_true", help="256^3 / 960x540 variant for quick checks")
     ap.add_argument("--workload", default="ct",
-                    choices=["ct", "mip", "blobs", "batch", "learned", "large", "preint", "upsampler_layers"],
+                    choices=["ct", "mip", "blobs", "batch", "learned", "large", "preint", "upsampler_layers",
+                             "ingest"],
                     help="ct: 512^3 u16 shaded DVR 1080p (default); mip: the same under MIP; blobs: 128^3 u8 "
                          "DVR 512x512; batch: 64 mixed requests in one launch; learned: upsampler vs plain; "
                          "large: 2048x2048x1024 u16 at 3840x2160; preint: pre-integrated classification; "
-                         "upsampler_layers: the learned path's convolutions, tcgen05 vs mma.sync")
+                         "upsampler_layers: the learned path's convolutions, tcgen05 vs mma.sync; "
+                         "ingest: .vvd volume loading")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
@@ -614,6 +683,9 @@ def main():
         return
     if args.workload == "upsampler_layers":
         run_upsampler_layers(args, warmup, ws, rank, local)
+        return
+    if args.workload == "ingest":
+        run_ingest(args, warmup, ws, rank, local)
         return
 
     w = build_workload(args.small, args.workload)

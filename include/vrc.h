@@ -10,6 +10,9 @@
  *   vrc_volume_upload   VolumeGL upload of a VolumeRAM representation
  *                       src/core/datastructures/volume/volumegl.cpp:126-168
  *                       (+ brick min/max, optimizedproxygeometry.cpp:894-987)
+ *   vrc_vvd_read_header, vrc_volume_load_vvd
+ *                       VvdVolumeReader::read, modules/core/io/vvdvolumereader.cpp,
+ *                       modules/core/io/vvdformat.cpp:53-89
  *   vrc_volume_minmax   VolumeMinMax derived data used for TF domain fitting
  *                       src/core/properties/transfunc/1d/1dkeys/transfunc1dkeysproperty.cpp:104-140
  *   vrc_tf_bake_keys    TransFunc1D::createTextureData + TransFunc1DKeys::getMappingForValueUByte
@@ -131,6 +134,34 @@ vrc_status vrc_volume_minmax(vrc_volume* vol, float* min_norm, float* max_norm);
 vrc_status vrc_volume_brick_minmax(vrc_volume* vol, int nbricks_out[3], float* out_min, float* out_max);
 /* Device bytes held by the bricked layout. */
 size_t vrc_volume_device_bytes(const vrc_volume* vol);
+
+/* ---- volume ingest (.vvd) ------------------------------------------------
+ * Voreen's .vvd volume files (VvdVolumeReader, modules/core/io/vvdvolumereader.cpp,
+ * vvdformat.cpp:53-89): the header's RawData format ("uint8", "uint16",
+ * "float"), dimensions and raw file (a `filename` attribute relative to the
+ * .vvd, or the path list of VoreenFilePathHelper, first existing entry), the
+ * Offset / Spacing / RealWorldMapping meta items (Voreen's defaults when
+ * absent) and the VolumeMinMax derived item. */
+typedef struct {
+    int dtype;              /* vrc_dtype of the raw voxels */
+    int dims[3];
+    float spacing[3], offset[3];
+    float rwm_scale, rwm_offset;
+    int has_minmax;         /* the file holds a VolumeMinMax item: */
+    float min_norm, max_norm;  /* its minNorm / maxNorm */
+    char raw_path[4096];    /* the resolved raw file */
+} vrc_vvd_info;
+
+/* Host-only header parse. VRC_ERR_UNSUPPORTED for other formats or voxels
+ * stored inside the XML; VRC_ERR_NOT_READY when the file or its raw file is
+ * missing. */
+vrc_status vrc_vvd_read_header(const char* vvd_path, vrc_vvd_info* info);
+/* Header parse, then the raw file streamed through two 64 MiB pinned host
+ * chunks (read of one chunk overlaps the device copy of the other) into a
+ * bricked device volume with its min/max tables (vrc_volume_upload).
+ * info_out may be NULL. */
+vrc_status vrc_volume_load_vvd(vrc_context* ctx, const char* vvd_path, int brick_size, vrc_volume** out,
+                               vrc_vvd_info* info_out);
 
 /* ---- transfer function --------------------------------------------------- */
 typedef struct {

@@ -1,0 +1,89 @@
+"""Volume ingest (.vvd) header parsing on the CPU: synthetic files in both
+RawData forms, Voreen's defaults, error statuses, and -- where the Voreen tree
+is present -- the sample volumes it ships, checked against an independent
+XML parse and their own VolumeMinMax derived items."""
+import os
+import xml.etree.ElementTree as ET
+
+import numpy as np
+import pytest
+
+import voreen_gb300 as v
+from voreen_gb300 import _abi
+
+REF_VOLUMES = "/root/reference/voreen/resource/voreenve/volumes"
+
+
+def test_synthetic_headers(vrc_lib, tmp_path):
+    vox = (np.arange(5 * 6 * 7) % 251).astype(np.uint8).reshape(5, 6, 7)
+    v.write_vvd(str(tmp_path / "a.vvd"), vox, spacing=(0.5, 0.25, 2.0), offset=(-1.0, 0.5, 3.0), rwm=(255.0, -1.5))
+    i = v.read_vvd_header(str(tmp_path / "a.vvd"))
+    assert (i.dtype, tuple(i.dims)) == (v.U8, (7, 6, 5))
+    assert tuple(i.spacing) == (0.5, 0.25, 2.0) and tuple(i.offset) == (-1.0, 0.5, 3.0)
+    assert (i.rwm_scale, i.rwm_offset, i.has_minmax) == (255.0, -1.5, 0)
+    assert i.raw_path.decode() == str(tmp_path / "a.raw")
+    # path-list form: the first existing entry is taken; defaults for absent meta items
+    v.write_vvd(str(tmp_path / "b.vvd"), vox.astype(np.uint16), path_list=True)
+    (tmp_path / "b.vvd").write_text((tmp_path / "b.vvd").read_text().replace(
+        '<MetaItem name="Offset"', '<MetaItem name="Ignored"').replace('<MetaItem name="Spacing"', '<MetaItem name="X"'))
+    i = v.read_vvd_header(str(tmp_path / "b.vvd"))
+    assert i.dtype == v.U16 and tuple(i.spacing) == (1.0, 1.0, 1.0) and tuple(i.offset) == (0.0, 0.0, 0.0)
+    assert (i.rwm_scale, i.rwm_offset) == (1.0, 0.0)
+    assert i.raw_path.decode() == str(tmp_path / "b.raw")
+
+
+def test_header_errors(vrc_lib, tmp_path):
+    vox = np.zeros((2, 3, 4), np.float32)
+    v.write_vvd(str(tmp_path / "c.vvd"), vox)
+    text = (tmp_path / "c.vvd").read_text()
+    (tmp_path / "d.vvd").write_text(text.replace('format="float"', 'format="int16"'))
+    info = _abi.VvdInfo()
+    L = v.lib()
+    assert L.vrc_vvd_read_header(str(tmp_path / "d.vvd").encode(), info) == 4      # VRC_ERR_UNSUPPORTED
+    os.remove(tmp_path / "c.raw")
+    assert L.vrc_vvd_read_header(str(tmp_path / "c.vvd").encode(), info) == 0      # header alone parses
+    (tmp_path / "e.vvd").write_text(text.replace('filename="c.raw"', ''))
+    assert L.vrc_vvd_read_header(str(tmp_path / "e.vvd").encode(), info) == 6      # no raw file: not ready
+    assert L.vrc_vvd_read_header(str(tmp_path / "none.vvd").encode(), info) == 6
+
+
+def _ref_files():
+    if not os.path.isdir(REF_VOLUMES):
+        return []
+    return sorted(f for f in os.listdir(REF_VOLUMES) if f.endswith(".vvd"))
+
+
+@pytest.mark.parametrize("name", _ref_files() or ["(no Voreen tree)"])
+def test_shipped_volumes(vrc_lib, name):
+    if name == "(no Voreen tree)":
+        pytest.skip("the Voreen tree with its sample volumes is not present")
+    path = os.path.join(REF_VOLUMES, name)
+    text = open(path, encoding="utf-8").read()
+    root = ET.fromstring(text[text.index("<?xml"):])  # some files open with a comment before the declaration
+    raw = root.find(".//RawData")
+    info = _abi.VvdInfo()
+    st = v.lib().vrc_vvd_read_header(path.encode(), info)
+    fmt = raw.get("format")
+    if fmt not in ("uint8", "uint16", "float"):
+        assert st == 4  # multi-channel data: not a scalar volume
+        return
+    assert st == 0
+    assert tuple(info.dims) == tuple(int(raw.get(k)) for k in "xyz")
+    assert info.dtype == {"uint8": v.U8, "uint16": v.U16, "float": v.F32}[fmt]
+    for key, field in (("Spacing", info.spacing), ("Offset", info.offset)):
+        item = root.find(f".//MetaItem[@name='{key}']/value")
+        if item is not None:
+            assert tuple(field) == tuple(np.float32(item.get(k)) for k in "xyz")
+    # Voreen's own VolumeMinMax against the raw voxels normalised as vrc normalises them
+    mm = root.find(".//DerivedItem[@type='VolumeMinMax']")
+    if mm is not None and os.path.exists(info.raw_path.decode()):
+        if mm.get("minNorm") is not None:
+            lo, hi = float(mm.get("minNorm")), float(mm.get("maxNorm"))
+        else:
+            lo = float(mm.find("minNormValues/channel").get("value"))
+            hi = float(mm.find("maxNormValues/channel").get("value"))
+        assert info.has_minmax == 1 and (info.min_norm, info.max_norm) == (np.float32(lo), np.float32(hi))
+        vox = np.fromfile(info.raw_path.decode(), {v.U8: np.uint8, v.U16: np.uint16, v.F32: np.float32}[info.dtype])
+        scale = {v.U8: 255.0, v.U16: 65535.0, v.F32: 1.0}[info.dtype]
+        assert np.float32(vox.min() / scale) == pytest.approx(lo, abs=1e-7)
+        assert np.float32(vox.max() / scale) == pytest.approx(hi, abs=1e-7)

@@ -24,7 +24,7 @@ from ._abi import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUF
                    Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
 
 __all__ = ["VrcError", "Context", "Volume", "TransferFunction", "PreIntegrationTable", "render", "entry_exit",
-           "default_params", "sampling_step", "image_rescale", "camera_matrices", "lib", "DVR", "MIP", "ISO", "MOP", "MIDA", "FHP",
+           "default_params", "sampling_step", "image_rescale", "read_vvd_header", "write_vvd", "camera_matrices", "lib", "DVR", "MIP", "ISO", "MOP", "MIDA", "FHP",
            "FHN", "CLASSIFY_TF", "CLASSIFY_PREINTEGRATED", "SHADE_NONE", "SHADE_PHONG", "U8", "U16", "F32",
            "OUT_RGBA8", "OUT_RGBA16", "OUT_RGBA32F", "EE_BUFFERS", "EE_ANALYTIC", "Camera", "RenderParams",
            "RenderStats", "VolumeDesc", "TFKey"]
@@ -129,6 +129,21 @@ class Volume:
         self.handle = C.c_void_p()
         _check(lib().vrc_volume_upload(ctx.handle, C.byref(self.desc), _ptr(voxels), 1 if _is_device(voxels) else 0,
                                        brick_size, C.byref(self.handle)), ctx, "vrc_volume_upload")
+
+    @classmethod
+    def load_vvd(cls, ctx: Context, path: str, brick_size: int = 0) -> "Volume":
+        """A Voreen .vvd volume file straight into the bricked device layout
+        (vrc_volume_load_vvd); the header is in `.vvd_info`."""
+        self = cls.__new__(cls)
+        self.ctx = ctx
+        self.handle = C.c_void_p()
+        info = _abi.VvdInfo()
+        _check(lib().vrc_volume_load_vvd(ctx.handle, path.encode(), brick_size, C.byref(self.handle), C.byref(info)),
+               ctx, "vrc_volume_load_vvd")
+        self.vvd_info = info
+        self.desc = make_desc(info.dtype, tuple(info.dims), tuple(info.spacing), tuple(info.offset),
+                              (info.rwm_scale, info.rwm_offset))
+        return self
 
     @property
     def dims(self):
@@ -266,6 +281,51 @@ class PreIntegrationTable:
             self.close()
         except Exception:
             pass
+
+
+def read_vvd_header(path: str):
+    """vrc_vvd_read_header: the parsed .vvd header (VvdInfo)."""
+    info = _abi.VvdInfo()
+    _check(lib().vrc_vvd_read_header(path.encode(), C.byref(info)), None, "vrc_vvd_read_header")
+    return info
+
+
+def write_vvd(path: str, voxels: np.ndarray, spacing=(1.0, 1.0, 1.0), offset=(0.0, 0.0, 0.0), rwm=None,
+              path_list: bool = False):
+    """Write (Z, Y, X) voxels as <path>.raw plus a .vvd header in Voreen's
+    layout (RawData with a `filename` attribute, or with the path list of
+    newer files). For tests and benchmarks; the product reads, it does not
+    need to write."""
+    import os
+    voxels = np.ascontiguousarray(voxels)
+    fmt = {np.dtype(np.uint8): "uint8", np.dtype(np.uint16): "uint16", np.dtype(np.float32): "float"}[voxels.dtype]
+    raw = os.path.splitext(path)[0] + ".raw"
+    voxels.tofile(raw)
+    Z, Y, X = voxels.shape
+    name = os.path.basename(raw)
+    if path_list:
+        rawdata = (f'<RawData format="{fmt}" x="{X}" y="{Y}" z="{Z}">\n'
+                   f'                <Paths noPathSet="false">\n                    <paths>\n'
+                   f'                        <item value="missing/{name}" />\n'
+                   f'                        <item value="{name}" />\n'
+                   f'                    </paths>\n                </Paths>\n            </RawData>')
+    else:
+        rawdata = f'<RawData filename="{name}" format="{fmt}" x="{X}" y="{Y}" z="{Z}" />'
+    meta = (f'                <MetaItem name="Offset" type="Vec3MetaData">\n'
+            f'                    <value x="{offset[0]!r}" y="{offset[1]!r}" z="{offset[2]!r}" />\n'
+            f'                </MetaItem>\n'
+            f'                <MetaItem name="Spacing" type="Vec3MetaData">\n'
+            f'                    <value x="{spacing[0]!r}" y="{spacing[1]!r}" z="{spacing[2]!r}" />\n'
+            f'                </MetaItem>\n')
+    if rwm is not None:
+        meta += (f'                <MetaItem name="RealWorldMapping" type="RealWorldMappingMetaData">\n'
+                 f'                    <value scale="{rwm[0]!r}" offset="{rwm[1]!r}" unit="" />\n'
+                 f'                </MetaItem>\n')
+    with open(path, "w") as f:
+        f.write('<?xml version="1.0" ?>\n<VoreenData version="1">\n    <Volumes>\n        <Volume>\n'
+                f'            {rawdata}\n            <MetaData>\n{meta}            </MetaData>\n'
+                '        </Volume>\n    </Volumes>\n</VoreenData>\n')
+    return raw
 
 
 def image_rescale(ctx: Context, src, dst, out_format: int = OUT_RGBA32F):

@@ -29,6 +29,12 @@ class VolumeDesc(C.Structure):
                 ("rwm_scale", C.c_float), ("rwm_offset", C.c_float)]
 
 
+class VvdInfo(C.Structure):
+    _fields_ = [("dtype", C.c_int), ("dims", C.c_int * 3), ("spacing", C.c_float * 3), ("offset", C.c_float * 3),
+                ("rwm_scale", C.c_float), ("rwm_offset", C.c_float), ("has_minmax", C.c_int),
+                ("min_norm", C.c_float), ("max_norm", C.c_float), ("raw_path", C.c_char * 4096)]
+
+
 class TFKey(C.Structure):
     _fields_ = [("intensity", C.c_float), ("color_l", C.c_uint8 * 4), ("color_r", C.c_uint8 * 4)]
 
@@ -107,6 +113,8 @@ SIGNATURES = {
     "vrc_preint_destroy": (C.c_int, [VP]),
     "vrc_tf_set_preintegration": (C.c_int, [VP, VP]),
     "vrc_sampling_step": (C.c_float, [VP, C.c_float]),
+    "vrc_vvd_read_header": (C.c_int, [C.c_char_p, P(VvdInfo)]),
+    "vrc_volume_load_vvd": (C.c_int, [VP, C.c_char_p, C.c_int, P(VP), P(VvdInfo)]),
     "vrc_image_rescale": (C.c_int, [VP, VP, C.c_int, C.c_int, VP, C.c_int, C.c_int, C.c_int]),
     "vrc_synth_volume": (C.c_int, [C.c_int, C.c_int, P(C.c_int), C.c_uint64, VP]),
     "vrc_synth_tubes_device": (C.c_int, [VP, P(C.c_int), C.c_int, C.c_uint64, C.c_float, VP]),
