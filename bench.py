@@ -551,7 +551,8 @@ def run_large(args, warmup, ws, rank, local):
     gen_s = time.time() - t0
     ctx = v.Context(dev)
     t0 = time.time()
-    vol = v.Volume(ctx, vox_d, (1.0, 1.0, 1.0))
+    placement = v.PLACE_HOST if args.placement == "host" else v.PLACE_DEVICE
+    vol = v.Volume(ctx, vox_d, (1.0, 1.0, 1.0), placement=placement)
     ctx.synchronize()
     upload_s = time.time() - t0
     lo, hi = vol.minmax()
@@ -564,7 +565,9 @@ def run_large(args, warmup, ws, rank, local):
     p.camera = v.make_camera(pos, focus, near=near, far=far)
     p.light_position[:] = [*pos, 1.0]
     out = torch.empty((image[1], image[0], 4), dtype=torch.float32, device=f"cuda:{dev}")
+    t0 = time.time()
     _, st = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
+    first_ms = (time.time() - t0) * 1e3  # host placement: includes filling the device brick cache
     kms = [v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)[1].kernel_ms for _ in range(3)]
     for _ in range(warmup):
         v.render_async(ctx, vol, tf, p, None, None, out, v.OUT_RGBA32F)
@@ -580,6 +583,17 @@ def run_large(args, warmup, ws, rank, local):
         end.synchronize()
     clocks = clk.summary()
     ms = start.elapsed_time(end) / steps
+    cache = None
+    if placement == v.PLACE_HOST:
+        cached, reach = vol.cache_info()
+        # one frame with the cache off: every brick read over the host link
+        vol.set_cache_limit(0)
+        _, su = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
+        vol.set_cache_limit(2**62)
+        nb = int(np.prod(vol.brick_minmax()[2]))
+        cache = {"bricks_cached": cached, "bricks_reachable": reach, "bricks_total": nb,
+                 "cache_bytes": cached * (vol.host_bytes // nb), "first_frame_ms_with_fill": first_ms,
+                 "uncached_kernel_ms": su.kernel_ms}
     b_alg = st.samples * 16 + st.samples_shaded * 48 + image[0] * image[1] * 4
     k_ms = statistics.median(kms)
     peak, peak_kind = measured_peaks()
@@ -620,8 +634,9 @@ def run_large(args, warmup, ws, rank, local):
             "roofline": {"bound": "hbm", "achieved": b_alg / (k_ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": b_alg / (k_ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": b_alg},
-            "volume": {"voxels_bytes": int(host.nbytes), "device_bytes": vol.device_bytes, "generate_s": gen_s,
-                       "upload_s": upload_s, "upload_gbs": host.nbytes / upload_s / 1e9},
+            "volume": {"voxels_bytes": int(host.nbytes), "device_bytes": vol.device_bytes,
+                       "host_bytes": vol.host_bytes, "placement": args.placement, "generate_s": gen_s,
+                       "upload_s": upload_s, "upload_gbs": host.nbytes / upload_s / 1e9, "brick_cache": cache},
             "parity_band": {"rows": [r0, r0 + 2], "max_abs": float(band.max()), "oracle_samples":
                             int(s32[r0:r0 + 2].sum()), "cpu_seconds": cpu_s},
             "learned": {"frames_per_s": 1000.0 / ms_learned, "speedup_vs_plain": ms / ms_learned,
@@ -648,6 +663,8 @@ def main():
                          "upsampler_layers: the learned path's convolutions, tcgen05 vs mma.sync; "
                          "ingest: .vvd volume loading")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--placement", default="device", choices=["device", "host"],
+                    help="large workload: brick pool in HBM or in pinned host memory read over NVLink-C2C")
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
     ap.add_argument("--shading", default="phong", choices=["phong", "none"], help="exploration only")
     ap.add_argument("--no-skip", action="store_true", help="disable empty-space skipping (exploration only)")

@@ -125,6 +125,16 @@ typedef struct {
  * device pointer. brick_size: 0 = default (32); otherwise 8, 16, 32 or 64. */
 vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels,
                              int voxels_on_device, int brick_size, vrc_volume** out);
+/* Brick-pool placement: device memory (HBM), or pinned host memory that
+ * the kernels read through its mapped device address -- over NVLink-C2C on
+ * Grace hosts -- so a volume larger than the GPU's memory can be rendered
+ * (the min/max tables stay in device memory). With VRC_PLACE_HOST and host
+ * voxels, the bricking kernels also read the caller's voxels in place
+ * (cudaHostRegister for the duration of the call), so no device copy of
+ * the volume is made at any point. */
+typedef enum { VRC_PLACE_DEVICE = 0, VRC_PLACE_HOST = 1 } vrc_placement;
+vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels,
+                                    int voxels_on_device, int brick_size, int placement, vrc_volume** out);
 vrc_status vrc_volume_destroy(vrc_volume* vol);
 /* Min/max of the normalised intensity (getVoxelNormalized) over the volume. */
 vrc_status vrc_volume_minmax(vrc_volume* vol, float* min_norm, float* max_norm);
@@ -132,8 +142,23 @@ vrc_status vrc_volume_minmax(vrc_volume* vol, float* min_norm, float* max_norm);
  * one voxel on the high side, the trilinear support). out_* may be NULL to
  * query nbricks only. */
 vrc_status vrc_volume_brick_minmax(vrc_volume* vol, int nbricks_out[3], float* out_min, float* out_max);
-/* Device bytes held by the bricked layout. */
+/* Device bytes held by the bricked layout (and its tables). */
 size_t vrc_volume_device_bytes(const vrc_volume* vol);
+/* Pinned host bytes of a VRC_PLACE_HOST brick pool (0 otherwise). */
+size_t vrc_volume_host_bytes(const vrc_volume* vol);
+/* Device brick cache of a VRC_PLACE_HOST pool. vrc_render copies the bricks
+ * the current transfer function can reach (value range meets a visible
+ * entry, plus their 26 neighbours) into device memory before the march, up
+ * to `bytes` (default: unlimited, bounded by free device memory less 1 GiB;
+ * 0 = no cache). Bricks already cached are kept across TF changes; bricks
+ * left out are read from the host pool, so the image never depends on the
+ * cache. The device-side counterpart of the reference's brick pool
+ * managers, which keep a bounded set of bricks resident in RAM in front of
+ * a larger store (OctreeBrickPoolManagerBase::getBrick,
+ * include/voreen/core/datastructures/octree/octreebrickpoolmanager.h:99-165). */
+vrc_status vrc_volume_set_cache_limit(vrc_volume* vol, size_t bytes);
+/* Bricks held by the cache and bricks the last TF could reach. */
+vrc_status vrc_volume_cache_info(const vrc_volume* vol, long long* cached, long long* reachable);
 
 /* ---- volume ingest (.vvd) ------------------------------------------------
  * Voreen's .vvd volume files (VvdVolumeReader, modules/core/io/vvdvolumereader.cpp,

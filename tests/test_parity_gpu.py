@@ -263,3 +263,66 @@ def test_device_tube_volume_parity(ctx):
     img, st = c.gpu(shading=v.SHADE_PHONG)
     o32, s32, _ = c.oracle(32)
     assert np.abs(img - o32).max() <= 1e-4
+
+
+@pytest.mark.parametrize("from_device", [False, True])
+def test_host_placed_brick_pool(ctx, from_device):
+    """A brick pool in pinned host memory (read by the march through its mapped
+    address) renders exactly as the device-resident one, and no device copy of
+    the voxels is kept."""
+    torch = pytest.importorskip("torch")
+    w = synth.config2(size=(97, 80, 66), image=(160, 120))
+    src = torch.from_numpy(w.voxels).cuda() if from_device else w.voxels
+    a = v.Volume(ctx, src, w.spacing, placement=v.PLACE_HOST)
+    b = v.Volume(ctx, w.voxels, w.spacing)
+    assert a.minmax() == b.minmax()
+    assert a.host_bytes > 0 and a.device_bytes < b.device_bytes and b.host_bytes == 0
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    for shading in (v.SHADE_NONE, v.SHADE_PHONG):
+        p = w.params(entry_exit_mode=v.EE_ANALYTIC, shading=shading)
+        ia, sa = v.render(ctx, a, tf, p, None, None, v.OUT_RGBA32F)
+        ib, sb = v.render(ctx, b, tf, p, None, None, v.OUT_RGBA32F)
+        np.testing.assert_array_equal(_bits(ia), _bits(ib))
+        assert sa.samples == sb.samples
+
+
+@pytest.mark.gpu
+def test_host_pool_device_cache(ctx):
+    """The device brick cache of a host-placed pool never changes an image:
+    with no cache, a partial one (the rest read from the host pool) and a
+    full one, across TF changes that keep part of the cached set, and for
+    DVR (with and without shading) and MIP."""
+    pytest.importorskip("torch")
+    w = synth.config2(size=(97, 80, 66), image=(160, 120))
+    a = v.Volume(ctx, w.voxels, w.spacing, placement=v.PLACE_HOST)
+    b = v.Volume(ctx, w.voxels, w.spacing)
+    nb = int(np.prod(a.brick_minmax()[2]))
+    brick_bytes = a.host_bytes // nb
+    keys2 = [(0.0, (0, 0, 0, 0)), (0.55, (0, 0, 0, 0)), (0.7, (250, 200, 90, 160)), (1.0, (255, 255, 255, 255))]
+    tfs = [v.TransferFunction(ctx, v.TransferFunction.bake(k, w.tf_width), w.domain) for k in (w.tf_keys, keys2)]
+    cases = [(v.DVR, v.SHADE_NONE), (v.DVR, v.SHADE_PHONG), (v.MIP, v.SHADE_NONE)]
+    seen = set()
+    for limit in (None, 0, "half", None):
+        if limit == "half":
+            a.set_cache_limit(brick_bytes * max(1, a.cache_info()[1] // 2))
+        elif limit is not None:
+            a.set_cache_limit(limit)
+        else:
+            a.set_cache_limit(2**62)
+        for tf in tfs:
+            for comp, shading in cases:
+                p = w.params(entry_exit_mode=v.EE_ANALYTIC, shading=shading, compositing=comp)
+                ia, sa = v.render(ctx, a, tf, p, None, None, v.OUT_RGBA32F)
+                ib, sb = v.render(ctx, b, tf, p, None, None, v.OUT_RGBA32F)
+                np.testing.assert_array_equal(_bits(ia), _bits(ib))
+                assert sa.samples == sb.samples
+                cached, reach = a.cache_info()
+                assert 0 < reach <= nb and cached <= reach
+                if limit == 0:
+                    assert cached == 0
+                elif limit == "half":
+                    assert 0 < cached < reach
+                else:
+                    assert cached == reach
+                seen.add((limit, cached == reach))
+    assert len(seen) == 3

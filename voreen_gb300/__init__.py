@@ -20,7 +20,7 @@ import numpy as np
 
 from . import _abi
 from ._abi import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, F32, FHN, FHP, ISO, MIDA, MIP,
-                   MOP, NOALLOC_MAX_CELLS, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, U8, U16,
+                   MOP, NOALLOC_MAX_CELLS, PLACE_DEVICE, PLACE_HOST, OUT_RGBA8, OUT_RGBA16, OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, U8, U16,
                    Camera, RenderParams, RenderStats, TFKey, VolumeDesc)
 
 __all__ = ["VrcError", "Context", "Volume", "TransferFunction", "PreIntegrationTable", "render", "entry_exit",
@@ -114,7 +114,7 @@ class Volume:
     """
 
     def __init__(self, ctx: Context, voxels, spacing=(1.0, 1.0, 1.0), offset=(0.0, 0.0, 0.0), rwm=(1.0, 0.0),
-                 brick_size: int = 0):
+                 brick_size: int = 0, placement: int = 0):
         self.ctx = ctx
         if _is_device(voxels):
             import torch
@@ -127,8 +127,9 @@ class Volume:
             shape = voxels.shape
         self.desc = make_desc(dt, (shape[2], shape[1], shape[0]), spacing, offset, rwm)
         self.handle = C.c_void_p()
-        _check(lib().vrc_volume_upload(ctx.handle, C.byref(self.desc), _ptr(voxels), 1 if _is_device(voxels) else 0,
-                                       brick_size, C.byref(self.handle)), ctx, "vrc_volume_upload")
+        _check(lib().vrc_volume_upload_placed(ctx.handle, C.byref(self.desc), _ptr(voxels),
+                                              1 if _is_device(voxels) else 0, brick_size, placement,
+                                              C.byref(self.handle)), ctx, "vrc_volume_upload")
 
     @classmethod
     def load_vvd(cls, ctx: Context, path: str, brick_size: int = 0) -> "Volume":
@@ -170,6 +171,21 @@ class Volume:
     @property
     def device_bytes(self) -> int:
         return int(lib().vrc_volume_device_bytes(self.handle))
+
+    @property
+    def host_bytes(self) -> int:
+        return int(lib().vrc_volume_host_bytes(self.handle))
+
+    def set_cache_limit(self, nbytes: int):
+        """Device brick cache budget of a host-placed pool (0 = read the host
+        pool only; the default is bounded by free device memory)."""
+        _check(lib().vrc_volume_set_cache_limit(self.handle, int(nbytes)), self.ctx, "vrc_volume_set_cache_limit")
+
+    def cache_info(self):
+        """(bricks cached, bricks the last TF could reach)."""
+        c, r = C.c_longlong(0), C.c_longlong(0)
+        _check(lib().vrc_volume_cache_info(self.handle, C.byref(c), C.byref(r)), self.ctx, "vrc_volume_cache_info")
+        return int(c.value), int(r.value)
 
     def close(self):
         if self.handle:

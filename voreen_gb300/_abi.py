@@ -21,6 +21,7 @@ CLASSIFY_TF, CLASSIFY_PREINTEGRATED = 0, 1
 SHADE_NONE, SHADE_PHONG = 0, 1
 OUT_RGBA8, OUT_RGBA32F, OUT_RGBA16 = 0, 1, 2
 EE_BUFFERS, EE_ANALYTIC = 0, 1
+PLACE_DEVICE, PLACE_HOST = 0, 1
 NOALLOC_MAX_CELLS = 2097152
 
 
@@ -89,6 +90,10 @@ SIGNATURES = {
     "vrc_context_stream": (VP, [VP]),
     "vrc_volume_upload": (C.c_int, [VP, P(VolumeDesc), VP, C.c_int, C.c_int, P(VP)]),
     "vrc_volume_destroy": (C.c_int, [VP]),
+    "vrc_volume_upload_placed": (C.c_int, [VP, P(VolumeDesc), VP, C.c_int, C.c_int, C.c_int, P(VP)]),
+    "vrc_volume_host_bytes": (C.c_size_t, [VP]),
+    "vrc_volume_set_cache_limit": (C.c_int, [VP, C.c_size_t]),
+    "vrc_volume_cache_info": (C.c_int, [VP, P(C.c_longlong), P(C.c_longlong)]),
     "vrc_volume_minmax": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),
     "vrc_volume_brick_minmax": (C.c_int, [VP, P(C.c_int), VP, VP]),
     "vrc_volume_device_bytes": (C.c_size_t, [VP]),

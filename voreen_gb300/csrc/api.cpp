@@ -253,7 +253,14 @@ void* vrc_context_stream(vrc_context* c) { return c ? (void*)c->stream : nullptr
 
 vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels, int on_device,
                              int brick_size, vrc_volume** out) {
+    return vrc_volume_upload_placed(ctx, desc, voxels, on_device, brick_size, VRC_PLACE_DEVICE, out);
+}
+
+vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels, int on_device,
+                                    int brick_size, int placement, vrc_volume** out) {
     if (!ctx || !out || !voxels) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: null argument");
+    if (placement != VRC_PLACE_DEVICE && placement != VRC_PLACE_HOST)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: unknown placement");
     *out = nullptr;
     if (!valid_desc(desc)) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_upload: invalid volume descriptor");
     if (brick_size == 0) brick_size = 32;
@@ -277,20 +284,41 @@ vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, cons
     const size_t nvox = (size_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const size_t brick_bytes = (size_t)L.nbricks() * L.brick_stride * bpv;
     void* staging = nullptr;
+    const void* registered = nullptr;  // caller's host voxels registered for direct device reads
     cudaError_t e = cudaSuccess;
     auto cleanup = [&](vrc_status s, const std::string& m) {
+        cudaStreamSynchronize(ctx->stream);
         if (staging) cudaFree(staging);
+        if (registered) cudaHostUnregister(const_cast<void*>(registered));
         vrc_volume_destroy(v);
         return fail(ctx, s, m);
     };
-    if ((e = cudaMalloc(&v->d_bricks, brick_bytes)) != cudaSuccess)
+    if (placement == VRC_PLACE_HOST) {
+        // brick pool in pinned host memory, read by the kernels through its
+        // mapped device address (NVLink-C2C on Grace hosts)
+        if ((e = cudaHostAlloc(&v->h_bricks, brick_bytes, cudaHostAllocMapped)) != cudaSuccess ||
+            (e = cudaHostGetDevicePointer(&v->d_bricks, v->h_bricks, 0)) != cudaSuccess)
+            return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: host brick pool allocation failed");
+        v->host_bytes = brick_bytes;
+    } else if ((e = cudaMalloc(&v->d_bricks, brick_bytes)) != cudaSuccess) {
         return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: brick pool allocation failed");
+    }
     if ((e = cudaMalloc((void**)&v->d_bmin, L.nbricks() * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc((void**)&v->d_bmax, L.nbricks() * sizeof(float))) != cudaSuccess)
         return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: min/max table allocation failed");
-    v->bytes = brick_bytes + 2 * L.nbricks() * sizeof(float);
+    v->bytes = (placement == VRC_PLACE_HOST ? 0 : brick_bytes) + 2 * L.nbricks() * sizeof(float);
     const void* lin = voxels;
-    if (!on_device) {
+    if (!on_device && placement == VRC_PLACE_HOST) {
+        // no device copy of the linear volume either: the bricking kernels read
+        // the caller's voxels through a mapped registration
+        void* dp = nullptr;
+        if ((e = cudaHostRegister(const_cast<void*>(voxels), nvox * bpv, cudaHostRegisterMapped)) != cudaSuccess)
+            return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: host registration: ") + cudaGetErrorString(e));
+        registered = voxels;
+        if ((e = cudaHostGetDevicePointer(&dp, const_cast<void*>(voxels), 0)) != cudaSuccess)
+            return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: mapped address: ") + cudaGetErrorString(e));
+        lin = dp;
+    } else if (!on_device) {
         if ((e = cudaMalloc(&staging, nvox * bpv)) != cudaSuccess)
             return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: staging allocation failed");
         if ((e = cudaMemcpyAsync(staging, voxels, nvox * bpv, cudaMemcpyHostToDevice, ctx->stream)) != cudaSuccess)
@@ -323,6 +351,8 @@ vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, cons
         return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: ") + cudaGetErrorString(e));
     if (staging) cudaFree(staging);
     staging = nullptr;
+    if (registered) cudaHostUnregister(const_cast<void*>(registered));
+    registered = nullptr;
     v->vmin = *std::min_element(mn.begin(), mn.end());
     v->vmax = *std::max_element(mx.begin(), mx.end());
     *out = v;
@@ -332,7 +362,15 @@ vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, cons
 vrc_status vrc_volume_destroy(vrc_volume* v) {
     if (!v) return VRC_ERR_INVALID_ARG;
     if (v->ctx) cudaSetDevice(v->ctx->device);
-    cudaFree(v->d_bricks);
+    if (v->h_bricks)
+        cudaFreeHost(v->h_bricks);
+    else
+        cudaFree(v->d_bricks);
+    cudaFree(v->d_cache);
+    cudaFree(v->d_slot);
+    cudaFree(v->d_occ_brick);
+    cudaFree(v->d_cache_ids);
+    cudaFree(v->d_cache_dst);
     cudaFree(v->d_bmin);
     cudaFree(v->d_bmax);
     for (auto& lv : v->levels) {
@@ -363,6 +401,36 @@ vrc_status vrc_volume_brick_minmax(vrc_volume* v, int nb[3], float* out_min, flo
 }
 
 size_t vrc_volume_device_bytes(const vrc_volume* v) { return v ? v->bytes : 0; }
+size_t vrc_volume_host_bytes(const vrc_volume* v) { return v ? v->host_bytes : 0; }
+
+vrc_status vrc_volume_set_cache_limit(vrc_volume* v, size_t bytes) {
+    if (!v) return VRC_ERR_INVALID_ARG;
+    v->cache_limit = bytes;
+    const size_t brick_bytes = (size_t)v->L.brick_stride * vrc::dtype_bytes(v->desc.dtype);
+    if (v->cache_slots > 0 && (size_t)v->cache_slots > bytes / brick_bytes) {
+        // shrink: release the cache, the next render fills a smaller one
+        if (v->ctx) cudaSetDevice(v->ctx->device);
+        cudaFree(v->d_cache);
+        cudaFree(v->d_cache_ids);
+        cudaFree(v->d_cache_dst);
+        v->d_cache = nullptr;
+        v->d_cache_ids = v->d_cache_dst = nullptr;
+        v->cache_slots = 0;
+        v->h_slot_brick.clear();
+        std::fill(v->h_slot.begin(), v->h_slot.end(), -1);
+    }
+    v->cache_valid = false;
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_cache_info(const vrc_volume* v, long long* cached, long long* reachable) {
+    if (!v || !cached || !reachable) return VRC_ERR_INVALID_ARG;
+    long long n = 0;
+    for (long long b : v->h_slot_brick) n += b >= 0 ? 1 : 0;
+    *cached = n;
+    *reachable = v->cache_reachable;
+    return VRC_OK;
+}
 
 vrc_status vrc_tf_bake_keys(const vrc_tf_key* keys, int nkeys, int width, float gamma, float threshold_lo,
                             float threshold_hi, uint8_t* out) {
@@ -663,6 +731,133 @@ extern "C" {
 
 namespace {
 
+// Fills the device cache of a host-resident brick pool for the bricks the
+// current TF can reach: bricks whose value range meets a visible TF entry
+// first, then their 26 neighbours (a sample near a face, a gradient tap or
+// the previous sample of a pre-integrated segment reads there), as many as
+// the cache limit holds. Bricks already cached keep their slot; only the new
+// ones are gathered over the host link. The march reads every brick that has
+// no slot from the host pool, so the cache never changes a result.
+vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ_prefix, int occ_width,
+                               const vrc_tf* tf, MarchParams& P, cudaStream_t s) {
+    const vrc::BrickLayout& L = vol->L;
+    const long long nb = L.nbricks();
+    const size_t words = (size_t)vrc::occupancy_bytes(nb) / 4;
+    if (!vol->d_occ_brick) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_occ_brick, words * 4));
+    VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width, vol->desc.rwm_scale,
+                                        vol->desc.rwm_offset, tf->lo, tf->hi, vol->d_occ_brick, s));
+    std::vector<uint32_t> occ(words);
+    VRC_CUDA(ctx, cudaMemcpyAsync(occ.data(), vol->d_occ_brick, words * 4, cudaMemcpyDeviceToHost, s));
+    VRC_CUDA(ctx, cudaStreamSynchronize(s));
+    const size_t brick_bytes = (size_t)L.brick_stride * vrc::dtype_bytes(vol->desc.dtype);
+    if (!(vol->cache_valid && occ == vol->h_occ)) {
+        // wanted bricks in priority order: occupied, then the dilation ring
+        std::vector<uint8_t> mark(nb, 0);
+        std::vector<long long> want;
+        for (long long b = 0; b < nb; ++b)
+            if ((occ[b >> 5] >> (b & 31)) & 1u) {
+                mark[b] = 2;
+                want.push_back(b);
+            }
+        const size_t n_occ = want.size();
+        for (size_t k = 0; k < n_occ; ++k) {
+            const long long b = want[k];
+            const int bx = int(b % L.nb[0]), by = int((b / L.nb[0]) % L.nb[1]), bz = int(b / ((long long)L.nb[0] * L.nb[1]));
+            for (int dz = -1; dz <= 1; ++dz)
+                for (int dy = -1; dy <= 1; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx) {
+                        const int x = bx + dx, y = by + dy, z = bz + dz;
+                        if (x < 0 || y < 0 || z < 0 || x >= L.nb[0] || y >= L.nb[1] || z >= L.nb[2]) continue;
+                        const long long n = ((long long)z * L.nb[1] + y) * L.nb[0] + x;
+                        if (!mark[n]) {
+                            mark[n] = 1;
+                            want.push_back(n);
+                        }
+                    }
+        }
+        vol->cache_reachable = (long long)want.size();
+        long long slots = std::min<long long>((long long)want.size(), (long long)(vol->cache_limit / brick_bytes));
+        if (slots > vol->cache_slots) {
+            // grow: fresh allocation, every wanted brick gathered again
+            size_t free_b = 0, total_b = 0;
+            VRC_CUDA(ctx, cudaMemGetInfo(&free_b, &total_b));
+            const size_t reserve = (size_t)1 << 30;  // left for the frame buffers and other work
+            const long long fit = free_b > reserve ? (long long)((free_b - reserve) / brick_bytes) : 0;
+            slots = std::min(slots, fit + vol->cache_slots);
+        }
+        if (slots > vol->cache_slots) {
+            cudaFree(vol->d_cache);
+            cudaFree(vol->d_cache_ids);
+            cudaFree(vol->d_cache_dst);
+            vol->d_cache = nullptr;
+            vol->d_cache_ids = vol->d_cache_dst = nullptr;
+            vol->cache_slots = 0;
+            vol->h_slot_brick.clear();
+            std::fill(vol->h_slot.begin(), vol->h_slot.end(), -1);
+            cudaError_t e = cudaMalloc(&vol->d_cache, (size_t)slots * brick_bytes);
+            if (e == cudaSuccess) e = cudaMalloc((void**)&vol->d_cache_ids, (size_t)slots * sizeof(long long));
+            if (e == cudaSuccess) e = cudaMalloc((void**)&vol->d_cache_dst, (size_t)slots * sizeof(long long));
+            if (e != cudaSuccess) {
+                cudaGetLastError();
+                cudaFree(vol->d_cache);
+                cudaFree(vol->d_cache_ids);
+                vol->d_cache = nullptr;
+                vol->d_cache_ids = nullptr;
+                vol->d_cache_dst = nullptr;
+                vol->cache_valid = false;
+                return VRC_OK;  // no cache: the march reads the host pool
+            }
+            vol->cache_slots = slots;
+            vol->h_slot_brick.assign((size_t)slots, -1);
+        }
+        if (vol->h_slot.size() != (size_t)nb) vol->h_slot.assign((size_t)nb, -1);
+        if (!vol->d_slot) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_slot, (size_t)nb * sizeof(int)));
+        // keep cached bricks that are still wanted within the slot budget
+        std::vector<uint8_t> keep(nb, 0);
+        for (long long k = 0; k < slots; ++k) keep[want[k]] = 1;
+        std::vector<long long> free_slots;
+        for (long long sl = 0; sl < vol->cache_slots; ++sl) {
+            const long long b = vol->h_slot_brick[sl];
+            if (b >= 0 && keep[b]) continue;
+            if (b >= 0) vol->h_slot[b] = -1;
+            vol->h_slot_brick[sl] = -1;
+            free_slots.push_back(sl);
+        }
+        std::vector<long long> ids, dst;
+        for (long long k = 0; k < slots; ++k) {
+            const long long b = want[k];
+            if (vol->h_slot[b] >= 0) continue;
+            const long long sl = free_slots.back();
+            free_slots.pop_back();
+            vol->h_slot[b] = (int)sl;
+            vol->h_slot_brick[sl] = b;
+            ids.push_back(b);
+            dst.push_back(sl);
+        }
+        if (!ids.empty()) {
+            VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_ids, ids.data(), ids.size() * sizeof(long long),
+                                          cudaMemcpyHostToDevice, s));
+            VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_dst, dst.data(), dst.size() * sizeof(long long),
+                                          cudaMemcpyHostToDevice, s));
+            VRC_CUDA(ctx, vrc::launch_brick_gather(vol->d_bricks, vol->d_cache_ids, vol->d_cache_dst,
+                                                   (long long)ids.size(), brick_bytes, vol->d_cache, s));
+        }
+        VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_slot, vol->h_slot.data(), (size_t)nb * sizeof(int),
+                                      cudaMemcpyHostToDevice, s));
+        // the host vectors are read by the copies above: finish them before
+        // they can change
+        VRC_CUDA(ctx, cudaStreamSynchronize(s));
+        vol->h_occ = occ;
+        vol->cache_valid = true;
+    }
+    if (vol->d_cache && vol->cache_slots > 0) {
+        P.bricks = vol->d_cache;
+        P.brick_slot = vol->d_slot;
+        P.host_pool = vol->d_bricks;
+    }
+    return VRC_OK;
+}
+
 vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
                        const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
                        int out_on_device, float* aux, vrc_render_stats* stats) {
@@ -772,6 +967,10 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             P.cshift_coarse = vol->L.shift;
             for (int i = 0; i < 3; ++i) P.ncc[i] = vol->L.nb[i];
         }
+    }
+    if (vol->h_bricks && vol->cache_limit > 0) {
+        if ((st = prepare_brick_cache(ctx, const_cast<vrc_volume*>(vol), occ_prefix, occ_width, tf, P, s)) != VRC_OK)
+            return st;
     }
     VRC_CUDA(ctx, cudaMemsetAsync(ctx->d_counters, 0, 16 * sizeof(unsigned long long), s));
     P.counters = ctx->d_counters;

@@ -160,6 +160,18 @@ __device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__
 }
 
 // Raw trilinear value at a clamped voxel position from the brick holding it.
+// Start of brick `brick`: in the pool directly, or, for a host-resident pool
+// with a device cache (brick_slot != nullptr), in the cache slot the table
+// names, and in the mapped host pool for a brick the cache does not hold
+// (slot -1), so every brick stays readable whatever the cache holds.
+template <typename T>
+__device__ __forceinline__ const T* brick_base(const MarchParams& P, const T* __restrict__ bricks, long long brick) {
+    if (!P.brick_slot) return bricks + brick * P.L.brick_stride;
+    const int slot = __ldg(P.brick_slot + brick);
+    return slot >= 0 ? bricks + (long long)slot * P.L.brick_stride
+                     : reinterpret_cast<const T*>(P.host_pool) + brick * P.L.brick_stride;
+}
+
 template <int DT>
 __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
                                                 float vx, float vy, float vz) {
@@ -170,7 +182,7 @@ __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const type
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
                   (ix - (bx << L.shift) + APRON_LO);
-    return tri_raw<DT>(bricks + brick * L.brick_stride, o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
+    return tri_raw<DT>(brick_base(P, bricks, brick), o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
 }
 
 // One central-difference lookup displaced along one axis: tap position `vt`
@@ -388,7 +400,7 @@ __device__ __forceinline__ float tap_norm(const MarchParams& P, const typename V
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
               lz = iz - (bz << L.shift) + APRON_LO;
-    return tri_at<DT>(bricks + brick * L.brick_stride, (lz * L.S + ly) * L.S + lx, L.S, L.S * L.S, s_(vx, flx),
+    return tri_at<DT>(brick_base(P, bricks, brick), (lz * L.S + ly) * L.S + lx, L.S, L.S * L.S, s_(vx, flx),
                       s_(vy, fly), s_(vz, flz));
 }
 
@@ -550,7 +562,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
             ++cnt.fetched;
             const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
-            const T* __restrict__ b = bricks + brick * L.brick_stride;
+            const T* __restrict__ b = brick_base(P, bricks, brick);
             const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
                       lz = iz - (bz << L.shift) + APRON_LO;
             const int o = (lz * S + ly) * S + lx;

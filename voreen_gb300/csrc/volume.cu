@@ -149,6 +149,33 @@ int grid_for(long long n, int block) {
 
 }  // namespace
 
+// One CTA per cached brick: 16-byte copies from the (host-resident) pool.
+// One CTA per cached brick; four 16-byte loads in flight per thread, since
+// the source is host memory read over the C2C link.
+__global__ void brick_gather_kernel(const uint4* __restrict__ pool, const long long* __restrict__ ids,
+                                    const long long* __restrict__ slots, long long words, uint4* __restrict__ cache) {
+    const uint4* src = pool + ids[blockIdx.x] * words;
+    uint4* dst = cache + slots[blockIdx.x] * words;
+    long long i = threadIdx.x;
+    for (; i + 3 * blockDim.x < words; i += 4 * blockDim.x) {
+        const uint4 a = src[i], b = src[i + blockDim.x], c = src[i + 2 * blockDim.x], d = src[i + 3 * blockDim.x];
+        dst[i] = a;
+        dst[i + blockDim.x] = b;
+        dst[i + 2 * blockDim.x] = c;
+        dst[i + 3 * blockDim.x] = d;
+    }
+    for (; i < words; i += blockDim.x) dst[i] = src[i];
+}
+
+cudaError_t launch_brick_gather(const void* pool, const long long* ids, const long long* dst, long long n,
+                                size_t brick_stride_bytes, void* cache, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    if (n > 0x7fffffffLL || brick_stride_bytes % 16) return cudaErrorInvalidValue;
+    brick_gather_kernel<<<(unsigned)n, 256, 0, s>>>(static_cast<const uint4*>(pool), ids, dst,
+                                                    (long long)(brick_stride_bytes / 16), static_cast<uint4*>(cache));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s) {
     const long long total = L.nbricks() * (long long)L.S * L.S * L.S;
     const int g = grid_for(total, 256);

@@ -7,6 +7,7 @@
 #include <map>
 #include <string>
 #include <utility>
+#include <vector>
 
 #include "../../include/vrc.h"
 
@@ -80,6 +81,8 @@ struct MarchParams {
     const float4* pi_table;      // pre-integration table [back * pi_res + front]; nullptr = classify by the TF
     int pi_res;
     int pi_chain;                // a step moves less than 0.99 voxel per axis: empty-to-empty segments skip
+    const int* brick_slot;       // brick -> slot in `bricks` (a device brick cache) or -1, nullptr = direct
+    const void* host_pool;       // mapped host pool read for slot -1
     float mida_gamma;            // "gammaValue" of MIDA compositing
 };
 
@@ -130,6 +133,10 @@ cudaError_t launch_entry_exit(const MarchParams& p, float4* entry, float4* exitp
 cudaError_t launch_batch_begin(unsigned long long* state, int nreq, cudaStream_t s);
 cudaError_t launch_march_batch(const BatchReq* reqs, int nreq, const unsigned* tile_prefix, unsigned total_tiles,
                                unsigned long long* state, int compositing, int shading, int num_sms, cudaStream_t s);
+// Copies brick ids[i] of `pool` to slot dst[i] of `cache` (brick_stride_bytes
+// each), i in [0, n).
+cudaError_t launch_brick_gather(const void* pool, const long long* ids, const long long* dst, long long n,
+                                size_t brick_stride_bytes, void* cache, cudaStream_t s);
 cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
                                 cudaStream_t s);
@@ -179,7 +186,24 @@ struct vrc_volume {
     vrc_context* ctx = nullptr;
     vrc_volume_desc desc{};
     vrc::BrickLayout L{};
-    void* d_bricks = nullptr;
+    void* d_bricks = nullptr;     // device address of the brick pool
+    void* h_bricks = nullptr;     // the pool's pinned host allocation (VRC_PLACE_HOST), else null
+    size_t host_bytes = 0;
+    // device cache of a host-resident pool: the bricks the current TF can
+    // reach (non-empty, dilated by one brick), as many as cache_limit bytes
+    // hold; the rest stay in the host pool and are read there
+    size_t cache_limit = SIZE_MAX;     // bytes; 0 = no cache
+    void* d_cache = nullptr;
+    long long cache_slots = 0;         // slots allocated in d_cache
+    int* d_slot = nullptr;             // nbricks entries: cache slot or -1
+    uint32_t* d_occ_brick = nullptr;   // per-brick occupancy bits under the current TF
+    long long* d_cache_ids = nullptr;  // bricks to gather (cache_slots entries)
+    long long* d_cache_dst = nullptr;  // their slots
+    std::vector<int> h_slot;           // host copy of d_slot
+    std::vector<long long> h_slot_brick;  // slot -> brick, -1 = free
+    std::vector<uint32_t> h_occ;       // occupancy the cache was filled for
+    bool cache_valid = false;
+    long long cache_reachable = 0;     // bricks the current TF can reach
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
     vrc_cell_level levels[2];  // skip cells of edge 8 and 16 (when smaller than the brick)
