@@ -326,3 +326,27 @@ def test_host_pool_device_cache(ctx):
                     assert cached == reach
                 seen.add((limit, cached == reach))
     assert len(seen) == 3
+
+
+@pytest.mark.gpu
+def test_pinned_host_buffers_in_place(ctx):
+    """Pinned host entry/exit points and output are used in place by the
+    kernel (mapped addresses); pageable ones are staged. Every combination
+    gives the same image."""
+    torch = pytest.importorskip("torch")
+    w = synth.config2(size=(90, 77, 64), image=(150, 110))
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    p = w.params(shading=v.SHADE_PHONG)
+    e, x = v.entry_exit(ctx, vol, p)
+
+    def pin(a):
+        return torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()
+
+    for fmt, dt in ((v.OUT_RGBA8, np.uint8), (v.OUT_RGBA32F, np.float32)):
+        ref, sr = v.render(ctx, vol, tf, p, e, x, fmt)
+        for ee in ((pin(e), pin(x)), (pin(e), x), (e, pin(x))):
+            for o in (None, pin(np.zeros(ref.shape, dt))):
+                img, st = v.render(ctx, vol, tf, p, ee[0], ee[1], fmt, o)
+                np.testing.assert_array_equal(img, ref)
+                assert st.samples == sr.samples

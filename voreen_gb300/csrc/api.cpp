@@ -906,10 +906,29 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     const size_t npix = (size_t)p->width * p->height;
     cudaStream_t s = ctx->stream;
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[0], s));
+    // Pinned host buffers (cudaHostAlloc / cudaHostRegister) are read and
+    // written by the kernel in place through their mapped addresses (over
+    // NVLink-C2C on Grace hosts): each pixel's entry/exit points are read once
+    // and its colour written once, so staging them through device memory
+    // would only add a copy before and after the march. Pageable buffers are
+    // staged.
+    auto mapped = [](const void* h) -> void* {
+        cudaPointerAttributes a;
+        if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    };
     if (p->entry_exit_mode == VRC_EE_BUFFERS) {
+        void* me = ee_on_device ? nullptr : mapped(entry);
+        void* mx = ee_on_device || !me ? nullptr : mapped(exitp);
         if (ee_on_device) {
             P.entry = reinterpret_cast<const float4*>(entry);
             P.exitp = reinterpret_cast<const float4*>(exitp);
+        } else if (me && mx) {
+            P.entry = reinterpret_cast<const float4*>(me);
+            P.exitp = reinterpret_cast<const float4*>(mx);
         } else {
             VRC_CUDA(ctx, ensure(&ctx->d_ee, &ctx->ee_bytes, 2 * npix * sizeof(float4)));
             float4* d = reinterpret_cast<float4*>(ctx->d_ee);
@@ -920,8 +939,11 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         }
     }
     const size_t px_bytes = out_format == VRC_OUT_RGBA32F ? 16 : (out_format == VRC_OUT_RGBA16 ? 8 : 4);
+    void* mout = out_on_device ? nullptr : mapped(out);
     if (out_on_device) {
         P.out = out;
+    } else if (mout) {
+        P.out = mout;
     } else {
         VRC_CUDA(ctx, ensure(&ctx->d_out, &ctx->out_bytes, npix * px_bytes));
         P.out = ctx->d_out;
@@ -979,7 +1001,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
     VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
-    if (!out_on_device) VRC_CUDA(ctx, cudaMemcpyAsync(out, P.out, npix * px_bytes, cudaMemcpyDeviceToHost, s));
+    if (!out_on_device && !mout) VRC_CUDA(ctx, cudaMemcpyAsync(out, P.out, npix * px_bytes, cudaMemcpyDeviceToHost, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
     if (stats || !out_on_device) VRC_CUDA(ctx, cudaStreamSynchronize(s));
     if (stats) {
