@@ -555,6 +555,12 @@ def run_large(args, warmup, ws, rank, local):
     vol = v.Volume(ctx, vox_d, (1.0, 1.0, 1.0), placement=placement)
     ctx.synchronize()
     upload_s = time.time() - t0
+    if placement == v.PLACE_HOST and args.cache_gb is not None:
+        vol.set_cache_limit(int(args.cache_gb * 1e9))
+    if placement == v.PLACE_HOST and args.lod:
+        t0 = time.time()
+        vol.set_lod(True)
+        lod_build_s = time.time() - t0
     lo, hi = vol.minmax()
     keys, domain = synth.tubes_tf(5002, 2, (lo, hi))
     tf_rgba = v.TransferFunction.bake(keys, 4096)
@@ -568,6 +574,14 @@ def run_large(args, warmup, ws, rank, local):
     t0 = time.time()
     _, st = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
     first_ms = (time.time() - t0) * 1e3  # host placement: includes filling the device brick cache
+    # host placement: per-frame wall time and bricks read without a cache slot
+    # while the cache refines towards the view's working set
+    settle = []
+    if placement == v.PLACE_HOST:
+        for _ in range(6):
+            t0 = time.time()
+            _, sk = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
+            settle.append({"ms": (time.time() - t0) * 1e3, "kernel_ms": sk.kernel_ms, "missed": vol.cache_info()[2]})
     kms = [v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)[1].kernel_ms for _ in range(3)]
     for _ in range(warmup):
         v.render_async(ctx, vol, tf, p, None, None, out, v.OUT_RGBA32F)
@@ -585,15 +599,23 @@ def run_large(args, warmup, ws, rank, local):
     ms = start.elapsed_time(end) / steps
     cache = None
     if placement == v.PLACE_HOST:
-        cached, reach = vol.cache_info()
+        cached, reach, missed_timed = vol.cache_info()
         # one frame with the cache off: every brick read over the host link
         vol.set_cache_limit(0)
+        lod_on = bool(args.lod)
+        if lod_on:
+            vol.set_lod(False)
         _, su = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
-        vol.set_cache_limit(2**62)
+        vol.set_cache_limit(int(args.cache_gb * 1e9) if args.cache_gb is not None else 2**62)
+        if lod_on:
+            vol.set_lod(True)
         nb = int(np.prod(vol.brick_minmax()[2]))
         cache = {"bricks_cached": cached, "bricks_reachable": reach, "bricks_total": nb,
                  "cache_bytes": cached * (vol.host_bytes // nb), "first_frame_ms_with_fill": first_ms,
-                 "uncached_kernel_ms": su.kernel_ms}
+                 "uncached_kernel_ms": su.kernel_ms, "cache_limit_gb": args.cache_gb, "lod": bool(args.lod),
+                 "frames_after_first": settle, "missed_in_last_timed_frame": missed_timed}
+        if args.lod:
+            cache["lod_build_s"] = lod_build_s
     b_alg = st.samples * 16 + st.samples_shaded * 48 + image[0] * image[1] * 4
     k_ms = statistics.median(kms)
     peak, peak_kind = measured_peaks()
@@ -663,6 +685,10 @@ def main():
                          "upsampler_layers: the learned path's convolutions, tcgen05 vs mma.sync; "
                          "ingest: .vvd volume loading")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cache-gb", type=float, default=None,
+                    help="large workload, host placement: device brick cache budget (default: free memory)")
+    ap.add_argument("--lod", action="store_true",
+                    help="large workload, host placement: sample uncached bricks from a half-resolution level")
     ap.add_argument("--placement", default="device", choices=["device", "host"],
                     help="large workload: brick pool in HBM or in pinned host memory read over NVLink-C2C")
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")

@@ -157,8 +157,25 @@ size_t vrc_volume_host_bytes(const vrc_volume* vol);
  * a larger store (OctreeBrickPoolManagerBase::getBrick,
  * include/voreen/core/datastructures/octree/octreebrickpoolmanager.h:99-165). */
 vrc_status vrc_volume_set_cache_limit(vrc_volume* vol, size_t bytes);
-/* Bricks held by the cache and bricks the last TF could reach. */
-vrc_status vrc_volume_cache_info(const vrc_volume* vol, long long* cached, long long* reachable);
+/* While the cache holds fewer bricks than the TF reaches (or a level of
+ * detail is attached), each render records the bricks it reads; before the
+ * next render, bricks read without a cache slot displace cached bricks that
+ * were not read, least recently read first (the used/missing brick flags and
+ * LRU brick pool of Voreen's octree raycaster, singleoctreeraycaster.cl).
+ * A still view converges to a cache holding its working set.
+ * vrc_volume_cache_info: bricks held by the cache, bricks the last TF could
+ * reach, and bricks the last tracked render read without a slot. */
+vrc_status vrc_volume_cache_info(const vrc_volume* vol, long long* cached, long long* reachable, long long* missed);
+/* Level of detail for a VRC_PLACE_HOST pool: a device-resident
+ * half-resolution level (each voxel the mean of 2x2x2 voxels, clamped at
+ * the volume's edges: VolumeOctree's HalfSampleMean parent bricks,
+ * volumeoctree.cpp:188-202), built on the first enable. While enabled, a
+ * brick without a cache slot is sampled from that level at the same
+ * texture-space point instead of from the host pool -- the coarser node
+ * Voreen's octree raycaster reads where a brick is not on the GPU -- so
+ * frames stay fast and approach the full-resolution image as refinement
+ * fills the cache. VRC_ERR_UNSUPPORTED for device-resident pools. */
+vrc_status vrc_volume_set_lod(vrc_volume* vol, int enable);
 
 /* ---- volume ingest (.vvd) ------------------------------------------------
  * Voreen's .vvd volume files (VvdVolumeReader, modules/core/io/vvdvolumereader.cpp,

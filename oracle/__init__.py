@@ -211,6 +211,30 @@ def brick_minmax(vol: OrcVolume, brick: int, apron_hi: int = 1):
     return mn, mx, nb
 
 
+def half_sample_mean(vox: np.ndarray) -> np.ndarray:
+    """Half-resolution level of a (Z, Y, X) volume: each voxel the mean of the
+    2x2x2 block at twice its index, indices clamped to the volume. Integers
+    follow HalfSampleMean (src/core/datastructures/octree/volumeoctree.cpp:
+    188-202): exact sum, divided by 8 with truncation; floats are summed in
+    z, y, x order in float32 and scaled by 1/8."""
+    d = vox.shape
+    d1 = tuple((n + 1) // 2 for n in d)
+    idx = [np.minimum(2 * np.arange(d1[a])[:, None] + np.arange(2)[None, :], d[a] - 1) for a in range(3)]
+    if vox.dtype == np.float32:
+        acc = np.zeros(d1, np.float32)
+        for dz in range(2):
+            for dy in range(2):
+                for dx in range(2):
+                    acc = acc + vox[np.ix_(idx[0][:, dz], idx[1][:, dy], idx[2][:, dx])]
+        return (acc * np.float32(0.125)).astype(np.float32)
+    acc = np.zeros(d1, np.uint64)
+    for dz in range(2):
+        for dy in range(2):
+            for dx in range(2):
+                acc += vox[np.ix_(idx[0][:, dz], idx[1][:, dy], idx[2][:, dx])].astype(np.uint64)
+    return (acc // 8).astype(vox.dtype)
+
+
 # ---- the reference pin library (present only where the reference tree is) ----
 _ref = None
 

@@ -50,3 +50,20 @@ def test_synth_is_deterministic_and_in_range():
     assert a.max() <= 4095
     f = v.synth_volume(0, v.F32, (16, 16, 16), 3)
     assert f.min() >= 0 and f.max() <= 1
+
+
+def test_half_sample_mean_known_answers():
+    """HalfSampleMean: truncating integer mean of each 2x2x2 block, indices
+    clamped at odd edges; float mean in float32."""
+    v = np.arange(3 * 5 * 4, dtype=np.uint16).reshape(3, 5, 4)
+    h = oracle.half_sample_mean(v)
+    assert h.shape == (2, 3, 2) and h.dtype == np.uint16
+    assert h[0, 0, 0] == (0 + 1 + 4 + 5 + 20 + 21 + 24 + 25) // 8
+    # last z block of an odd axis repeats the edge slice: z indices (2, 2)
+    blk = [int(v[2, y, x]) for y in (2, 3) for x in (0, 1)] * 2
+    assert h[1, 1, 0] == sum(blk) // 8
+    c = np.full((7, 6, 5), 201, np.uint8)
+    assert np.all(oracle.half_sample_mean(c) == 201)
+    f = np.random.default_rng(3).random((4, 4, 4), dtype=np.float32)
+    hf = oracle.half_sample_mean(f)
+    np.testing.assert_allclose(hf[1, 0, 1], f[2:4, 0:2, 2:4].mean(), rtol=1e-6)

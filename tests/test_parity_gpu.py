@@ -316,7 +316,7 @@ def test_host_pool_device_cache(ctx):
                 ib, sb = v.render(ctx, b, tf, p, None, None, v.OUT_RGBA32F)
                 np.testing.assert_array_equal(_bits(ia), _bits(ib))
                 assert sa.samples == sb.samples
-                cached, reach = a.cache_info()
+                cached, reach, _ = a.cache_info()
                 assert 0 < reach <= nb and cached <= reach
                 if limit == 0:
                     assert cached == 0

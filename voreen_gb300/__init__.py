@@ -182,10 +182,17 @@ class Volume:
         _check(lib().vrc_volume_set_cache_limit(self.handle, int(nbytes)), self.ctx, "vrc_volume_set_cache_limit")
 
     def cache_info(self):
-        """(bricks cached, bricks the last TF could reach)."""
-        c, r = C.c_longlong(0), C.c_longlong(0)
-        _check(lib().vrc_volume_cache_info(self.handle, C.byref(c), C.byref(r)), self.ctx, "vrc_volume_cache_info")
-        return int(c.value), int(r.value)
+        """(bricks cached, bricks the last TF could reach, bricks the last
+        tracked render read without a cache slot)."""
+        c, r, m = C.c_longlong(0), C.c_longlong(0), C.c_longlong(0)
+        _check(lib().vrc_volume_cache_info(self.handle, C.byref(c), C.byref(r), C.byref(m)), self.ctx,
+               "vrc_volume_cache_info")
+        return int(c.value), int(r.value), int(m.value)
+
+    def set_lod(self, enable: bool = True):
+        """Sample bricks without a cache slot from a device-resident
+        half-resolution level (host-placed pools only)."""
+        _check(lib().vrc_volume_set_lod(self.handle, 1 if enable else 0), self.ctx, "vrc_volume_set_lod")
 
     def close(self):
         if self.handle:

@@ -371,6 +371,8 @@ vrc_status vrc_volume_destroy(vrc_volume* v) {
     cudaFree(v->d_occ_brick);
     cudaFree(v->d_cache_ids);
     cudaFree(v->d_cache_dst);
+    cudaFree(v->d_used);
+    cudaFree(v->d_lod);
     cudaFree(v->d_bmin);
     cudaFree(v->d_bmax);
     for (auto& lv : v->levels) {
@@ -423,12 +425,63 @@ vrc_status vrc_volume_set_cache_limit(vrc_volume* v, size_t bytes) {
     return VRC_OK;
 }
 
-vrc_status vrc_volume_cache_info(const vrc_volume* v, long long* cached, long long* reachable) {
-    if (!v || !cached || !reachable) return VRC_ERR_INVALID_ARG;
+vrc_status vrc_volume_cache_info(const vrc_volume* v, long long* cached, long long* reachable, long long* missed) {
+    if (!v || !cached || !reachable || !missed) return VRC_ERR_INVALID_ARG;
     long long n = 0;
     for (long long b : v->h_slot_brick) n += b >= 0 ? 1 : 0;
     *cached = n;
     *reachable = v->cache_reachable;
+    *missed = v->last_misses;
+    if (v->used_pending && v->ctx) {
+        // the last render's bits (refinement consumes them at the next render)
+        const long long nb = v->L.nbricks();
+        const size_t words = (size_t)vrc::occupancy_bytes(nb) / 4;
+        std::vector<uint32_t> used(words);
+        cudaError_t e = cudaSetDevice(v->ctx->device);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(used.data(), v->d_used, words * 4, cudaMemcpyDeviceToHost, v->ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(v->ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(v->ctx, e, "vrc_volume_cache_info");
+        long long m = 0;
+        for (size_t w = 0; w < words; ++w)
+            for (uint32_t bits = used[w]; bits; bits &= bits - 1) {
+                const long long b = (long long)w * 32 + __builtin_ctz(bits);
+                if (b < nb && v->h_slot[b] < 0) ++m;
+            }
+        *missed = m;
+    }
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_set_lod(vrc_volume* v, int enable) {
+    if (!v || !v->ctx) return VRC_ERR_INVALID_ARG;
+    vrc_context* ctx = v->ctx;
+    if (!v->h_bricks) return fail(ctx, VRC_ERR_UNSUPPORTED, "vrc_volume_set_lod: the volume's brick pool is in device memory");
+    if (enable && !v->d_lod) {
+        VRC_CUDA(ctx, cudaSetDevice(ctx->device));
+        BrickLayout& H = v->lod_L;
+        H = v->L;
+        for (int i = 0; i < 3; ++i) {
+            H.dims[i] = (v->L.dims[i] + 1) / 2;
+            H.nb[i] = (H.dims[i] + H.B - 1) / H.B;
+        }
+        const int bpv = vrc::dtype_bytes(v->desc.dtype);
+        const size_t n1 = (size_t)H.dims[0] * H.dims[1] * H.dims[2];
+        void* lin = nullptr;
+        cudaError_t e = cudaMalloc(&lin, n1 * bpv);
+        if (e == cudaSuccess) e = cudaMalloc(&v->d_lod, (size_t)H.nbricks() * H.brick_stride * bpv);
+        if (e == cudaSuccess) e = vrc::launch_half_sample(v->d_bricks, v->desc.dtype, v->L, H.dims, lin, ctx->stream);
+        if (e == cudaSuccess) e = vrc::launch_brick_build(lin, v->desc.dtype, H, v->d_lod, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        cudaFree(lin);
+        if (e != cudaSuccess) {
+            cudaFree(v->d_lod);
+            v->d_lod = nullptr;
+            return cuda_fail(ctx, e, "vrc_volume_set_lod");
+        }
+        v->bytes += (size_t)H.nbricks() * H.brick_stride * bpv;
+    }
+    v->lod_on = enable != 0;
     return VRC_OK;
 }
 
@@ -731,13 +784,42 @@ extern "C" {
 
 namespace {
 
-// Fills the device cache of a host-resident brick pool for the bricks the
-// current TF can reach: bricks whose value range meets a visible TF entry
-// first, then their 26 neighbours (a sample near a face, a gradient tap or
-// the previous sample of a pre-integrated segment reads there), as many as
-// the cache limit holds. Bricks already cached keep their slot; only the new
-// ones are gathered over the host link. The march reads every brick that has
-// no slot from the host pool, so the cache never changes a result.
+// Copies bricks ids[i] of the host pool to cache slots dst[i] and uploads
+// the slot table; waits for both, since they read the host vectors.
+vrc_status commit_slots(vrc_context* ctx, vrc_volume* vol, const std::vector<long long>& ids,
+                        const std::vector<long long>& dst, size_t brick_bytes, cudaStream_t s) {
+    if (!ids.empty()) {
+        VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_ids, ids.data(), ids.size() * sizeof(long long),
+                                      cudaMemcpyHostToDevice, s));
+        VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_dst, dst.data(), dst.size() * sizeof(long long),
+                                      cudaMemcpyHostToDevice, s));
+        VRC_CUDA(ctx, vrc::launch_brick_gather(vol->d_bricks, vol->d_cache_ids, vol->d_cache_dst, (long long)ids.size(),
+                                               brick_bytes, vol->d_cache, s));
+    }
+    VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_slot, vol->h_slot.data(), vol->h_slot.size() * sizeof(int),
+                                  cudaMemcpyHostToDevice, s));
+    VRC_CUDA(ctx, cudaStreamSynchronize(s));
+    return VRC_OK;
+}
+
+// Device cache of a host-resident brick pool, refreshed before each march.
+//
+// Prefetch by TF: when the TF (its per-brick occupancy) changes, the cache
+// is filled with the bricks the TF can reach -- bricks whose value range
+// meets a visible TF entry first, then their 26 neighbours (a sample near a
+// face, a gradient tap or the previous sample of a pre-integrated segment
+// reads there) -- as many as the cache limit holds. Bricks already cached
+// keep their slot; only new ones are gathered over the host link.
+//
+// Refinement by view: while the cache holds fewer bricks than the TF
+// reaches (or a level of detail is attached), the march records every brick
+// it reads. Before the next frame, bricks it read without a slot displace
+// cached bricks it did not read, least recently read first -- the
+// used/missing brick flags and LRU brick pool of Voreen's octree raycaster
+// (singleoctreeraycaster.cl, octreebrickpoolmanager.h:99-165).
+//
+// A brick without a slot is read from the host pool (exact) or, with a level
+// of detail attached, from the device-resident half-resolution level.
 vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ_prefix, int occ_width,
                                const vrc_tf* tf, MarchParams& P, cudaStream_t s) {
     const vrc::BrickLayout& L = vol->L;
@@ -746,10 +828,18 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
     if (!vol->d_occ_brick) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_occ_brick, words * 4));
     VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width, vol->desc.rwm_scale,
                                         vol->desc.rwm_offset, tf->lo, tf->hi, vol->d_occ_brick, s));
-    std::vector<uint32_t> occ(words);
+    std::vector<uint32_t> occ(words), used;
     VRC_CUDA(ctx, cudaMemcpyAsync(occ.data(), vol->d_occ_brick, words * 4, cudaMemcpyDeviceToHost, s));
+    if (vol->used_pending) {
+        used.resize(words);
+        VRC_CUDA(ctx, cudaMemcpyAsync(used.data(), vol->d_used, words * 4, cudaMemcpyDeviceToHost, s));
+        vol->used_pending = false;
+    }
     VRC_CUDA(ctx, cudaStreamSynchronize(s));
     const size_t brick_bytes = (size_t)L.brick_stride * vrc::dtype_bytes(vol->desc.dtype);
+    if (vol->h_slot.size() != (size_t)nb) vol->h_slot.assign((size_t)nb, -1);
+    if (vol->h_last_used.size() != (size_t)nb) vol->h_last_used.assign((size_t)nb, 0);
+    if (!vol->d_slot) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_slot, (size_t)nb * sizeof(int)));
     if (!(vol->cache_valid && occ == vol->h_occ)) {
         // wanted bricks in priority order: occupied, then the dilation ring
         std::vector<uint8_t> mark(nb, 0);
@@ -804,14 +894,12 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
                 vol->d_cache = nullptr;
                 vol->d_cache_ids = nullptr;
                 vol->d_cache_dst = nullptr;
-                vol->cache_valid = false;
-                return VRC_OK;  // no cache: the march reads the host pool
+                slots = 0;  // no cache: every brick is read from the host pool (or the level of detail)
+            } else {
+                vol->cache_slots = slots;
+                vol->h_slot_brick.assign((size_t)slots, -1);
             }
-            vol->cache_slots = slots;
-            vol->h_slot_brick.assign((size_t)slots, -1);
         }
-        if (vol->h_slot.size() != (size_t)nb) vol->h_slot.assign((size_t)nb, -1);
-        if (!vol->d_slot) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_slot, (size_t)nb * sizeof(int)));
         // keep cached bricks that are still wanted within the slot budget
         std::vector<uint8_t> keep(nb, 0);
         for (long long k = 0; k < slots; ++k) keep[want[k]] = 1;
@@ -834,26 +922,75 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
             ids.push_back(b);
             dst.push_back(sl);
         }
-        if (!ids.empty()) {
-            VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_ids, ids.data(), ids.size() * sizeof(long long),
-                                          cudaMemcpyHostToDevice, s));
-            VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_cache_dst, dst.data(), dst.size() * sizeof(long long),
-                                          cudaMemcpyHostToDevice, s));
-            VRC_CUDA(ctx, vrc::launch_brick_gather(vol->d_bricks, vol->d_cache_ids, vol->d_cache_dst,
-                                                   (long long)ids.size(), brick_bytes, vol->d_cache, s));
-        }
-        VRC_CUDA(ctx, cudaMemcpyAsync(vol->d_slot, vol->h_slot.data(), (size_t)nb * sizeof(int),
-                                      cudaMemcpyHostToDevice, s));
-        // the host vectors are read by the copies above: finish them before
-        // they can change
-        VRC_CUDA(ctx, cudaStreamSynchronize(s));
+        vrc_status st = commit_slots(ctx, vol, ids, dst, brick_bytes, s);
+        if (st != VRC_OK) return st;
         vol->h_occ = occ;
         vol->cache_valid = true;
     }
-    if (vol->d_cache && vol->cache_slots > 0) {
-        P.bricks = vol->d_cache;
+    if (!used.empty()) {
+        // refinement from the bricks the last frame read
+        const uint32_t stamp = ++vol->frame;
+        std::vector<long long> missed;
+        for (size_t w = 0; w < words; ++w)
+            for (uint32_t bits = used[w]; bits; bits &= bits - 1) {
+                const long long b = (long long)w * 32 + __builtin_ctz(bits);
+                if (b >= nb) break;
+                vol->h_last_used[b] = stamp;
+                if (vol->h_slot[b] < 0) missed.push_back(b);
+            }
+        vol->last_misses = (long long)missed.size();
+        if (!missed.empty() && vol->cache_slots > 0) {
+            // free slots first, then slots whose brick the frame did not read, oldest first
+            std::vector<long long> cand;
+            std::vector<std::pair<uint32_t, long long>> stale;
+            for (long long sl = 0; sl < vol->cache_slots; ++sl) {
+                const long long b = vol->h_slot_brick[sl];
+                if (b < 0)
+                    cand.push_back(sl);
+                else if (vol->h_last_used[b] != stamp)
+                    stale.emplace_back(vol->h_last_used[b], sl);
+            }
+            std::stable_sort(stale.begin(), stale.end(),
+                             [](const std::pair<uint32_t, long long>& x, const std::pair<uint32_t, long long>& y) {
+                                 return x.first < y.first;
+                             });
+            for (const auto& e : stale) cand.push_back(e.second);
+            const size_t n = std::min(missed.size(), cand.size());
+            std::vector<long long> ids, dst;
+            for (size_t k = 0; k < n; ++k) {
+                const long long sl = cand[k], b = missed[k];
+                const long long old = vol->h_slot_brick[sl];
+                if (old >= 0) vol->h_slot[old] = -1;
+                vol->h_slot[b] = (int)sl;
+                vol->h_slot_brick[sl] = b;
+                ids.push_back(b);
+                dst.push_back(sl);
+            }
+            vrc_status st = commit_slots(ctx, vol, ids, dst, brick_bytes, s);
+            if (st != VRC_OK) return st;
+        }
+    }
+    const bool lod = vol->lod_on && vol->d_lod;
+    if (vol->cache_slots > 0 || lod) {
+        P.bricks = vol->d_cache ? vol->d_cache : vol->d_bricks;
         P.brick_slot = vol->d_slot;
         P.host_pool = vol->d_bricks;
+    }
+    if (lod) {
+        P.lod_bricks = vol->d_lod;
+        for (int i = 0; i < 3; ++i) {
+            P.lod_nb[i] = vol->lod_L.nb[i];
+            P.lod_dimf[i] = float(vol->lod_L.dims[i]);
+            P.lod_dim_m1[i] = float(vol->lod_L.dims[i] - 1);
+        }
+    }
+    if (vol->cache_slots > 0 && (lod || vol->cache_slots < vol->cache_reachable)) {
+        if (!vol->d_used) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_used, words * 4));
+        VRC_CUDA(ctx, cudaMemsetAsync(vol->d_used, 0, words * 4, s));
+        P.brick_used = vol->d_used;
+        vol->used_pending = true;
+    } else {
+        vol->last_misses = 0;
     }
     return VRC_OK;
 }
@@ -990,7 +1127,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             for (int i = 0; i < 3; ++i) P.ncc[i] = vol->L.nb[i];
         }
     }
-    if (vol->h_bricks && vol->cache_limit > 0) {
+    if (vol->h_bricks && (vol->cache_limit > 0 || vol->lod_on)) {
         if ((st = prepare_brick_cache(ctx, const_cast<vrc_volume*>(vol), occ_prefix, occ_width, tf, P, s)) != VRC_OK)
             return st;
     }

@@ -159,17 +159,55 @@ __device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__
     return __fmaf_rn(fz, y1 - y0, y0);
 }
 
-// Raw trilinear value at a clamped voxel position from the brick holding it.
 // Start of brick `brick`: in the pool directly, or, for a host-resident pool
 // with a device cache (brick_slot != nullptr), in the cache slot the table
-// names, and in the mapped host pool for a brick the cache does not hold
-// (slot -1), so every brick stays readable whatever the cache holds.
+// names. A brick the cache does not hold (slot -1) is read in the mapped
+// host pool, so every brick stays readable whatever the cache holds -- or,
+// with a level of detail attached, not at all: nullptr, and the caller
+// samples the half-resolution level instead.
 template <typename T>
 __device__ __forceinline__ const T* brick_base(const MarchParams& P, const T* __restrict__ bricks, long long brick) {
     if (!P.brick_slot) return bricks + brick * P.L.brick_stride;
     const int slot = __ldg(P.brick_slot + brick);
-    return slot >= 0 ? bricks + (long long)slot * P.L.brick_stride
-                     : reinterpret_cast<const T*>(P.host_pool) + brick * P.L.brick_stride;
+    if (slot >= 0) return bricks + (long long)slot * P.L.brick_stride;
+    return P.lod_bricks ? nullptr : reinterpret_cast<const T*>(P.host_pool) + brick * P.L.brick_stride;
+}
+
+// Records that a brick was read this frame (cache refinement). Lanes of the
+// warp reading the same brick share one atomic.
+__device__ __forceinline__ void mark_used(const MarchParams& P, long long brick) {
+    const unsigned peers = __match_any_sync(__activemask(), (unsigned long long)brick);
+    if ((int)(threadIdx.x & 31) == __ffs(peers) - 1) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
+}
+
+// The half-resolution level at texture-space point (sx, sy, sz), sampled
+// like the full level (clamped voxel position, trilinear from the brick
+// holding the floor voxel): normalised (RAW false) or raw values. This is
+// the coarser octree level Voreen's octree raycaster reads where a brick is
+// not on the GPU (singleoctreeraycaster.cl), here the 2x2x2 mean of
+// VolumeOctree's half-sampled parent bricks (volumeoctree.cpp:188-202).
+template <int DT, bool RAW>
+__device__ __noinline__ float lod_tap(const MarchParams& P, float sx, float sy, float sz) {
+    using T = typename Vox<DT>::T;
+    const BrickLayout& L = P.L;
+    const float vx = clampf_(s_(m_(P.lod_dimf[0], sx), 0.5f), 0.f, P.lod_dim_m1[0]);
+    const float vy = clampf_(s_(m_(P.lod_dimf[1], sy), 0.5f), 0.f, P.lod_dim_m1[1]);
+    const float vz = clampf_(s_(m_(P.lod_dimf[2], sz), 0.5f), 0.f, P.lod_dim_m1[2]);
+    const float flx = floorf(vx), fly = floorf(vy), flz = floorf(vz);
+    const int ix = (int)flx, iy = (int)fly, iz = (int)flz;
+    const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
+    const long long brick = ((long long)bz * P.lod_nb[1] + by) * P.lod_nb[0] + bx;
+    const T* b = reinterpret_cast<const T*>(P.lod_bricks) + brick * L.brick_stride;
+    const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
+                  (ix - (bx << L.shift) + APRON_LO);
+    const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
+    return RAW ? tri_raw<DT>(b, o, L.S, L.S * L.S, fx, fy, fz) : tri_at<DT>(b, o, L.S, L.S * L.S, fx, fy, fz);
+}
+
+// The same from a full-resolution voxel position (gradient and previous-sample taps).
+template <int DT, bool RAW>
+__device__ __forceinline__ float lod_tap_voxel(const MarchParams& P, float vx, float vy, float vz) {
+    return lod_tap<DT, RAW>(P, d_(a_(vx, 0.5f), P.dimf[0]), d_(a_(vy, 0.5f), P.dimf[1]), d_(a_(vz, 0.5f), P.dimf[2]));
 }
 
 template <int DT>
@@ -182,7 +220,10 @@ __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const type
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
                   (ix - (bx << L.shift) + APRON_LO);
-    return tri_raw<DT>(brick_base(P, bricks, brick), o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
+    if (P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
+    const typename Vox<DT>::T* b = brick_base(P, bricks, brick);
+    if (!b) return lod_tap_voxel<DT, true>(P, vx, vy, vz);
+    return tri_raw<DT>(b, o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
 }
 
 // One central-difference lookup displaced along one axis: tap position `vt`
@@ -197,7 +238,7 @@ __device__ __forceinline__ float grad_tap(const MarchParams& P, const typename V
     const int it = (int)fl;
     const int lt = lc + (it - ic);
     const int S = P.L.S, S2 = P.L.S * P.L.S;
-    if (lt >= 0 && lt <= P.L.B + 1) {
+    if (b && lt >= 0 && lt <= P.L.B + 1) {
         const int stride = AXIS == 0 ? 1 : (AXIS == 1 ? S : S2);
         const float ft = vt - fl;
         return tri_raw<DT>(b, o + (it - ic) * stride, S, S2, AXIS == 0 ? ft : fx, AXIS == 1 ? ft : fy,
@@ -400,7 +441,10 @@ __device__ __forceinline__ float tap_norm(const MarchParams& P, const typename V
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
               lz = iz - (bz << L.shift) + APRON_LO;
-    return tri_at<DT>(brick_base(P, bricks, brick), (lz * L.S + ly) * L.S + lx, L.S, L.S * L.S, s_(vx, flx),
+    if (P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
+    const typename Vox<DT>::T* b = brick_base(P, bricks, brick);
+    if (!b) return lod_tap_voxel<DT, false>(P, vx, vy, vz);
+    return tri_at<DT>(b, (lz * L.S + ly) * L.S + lx, L.S, L.S * L.S, s_(vx, flx),
                       s_(vy, fly), s_(vz, flz));
 }
 
@@ -472,6 +516,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     float t_last = 0.f;
     float t = 0.f;
     float hit_t = -1.f, hit_g = 0.f;  // first sample with alpha > 0 (auxiliary output)
+    long long marked = -1;             // last brick recorded as read (cache refinement)
     bool finished = false;
     int loop = 0;
     while (!finished && loop < LOOP_CAP) {
@@ -563,10 +608,14 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             ++cnt.fetched;
             const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
             const T* __restrict__ b = brick_base(P, bricks, brick);
+            if (P.brick_used && brick != marked) {
+                marked = brick;
+                mark_used(P, brick);
+            }
             const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
                       lz = iz - (bz << L.shift) + APRON_LO;
             const int o = (lz * S + ly) * S + lx;
-            const float intensity = tri_at<DT>(b, o, S, S2, fx, fy, fz);
+            const float intensity = b ? tri_at<DT>(b, o, S, S2, fx, fy, fz) : lod_tap<DT, false>(P, sx, sy, sz);
             const float rw = a_(m_(intensity, P.rwm_scale), P.rwm_offset);
             float4 c;
             if (PI) {

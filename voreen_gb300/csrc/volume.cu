@@ -37,6 +37,43 @@ __global__ void brick_build_kernel(const T* __restrict__ lin, BrickLayout L, T* 
 
 template <typename T> __device__ __forceinline__ float raw_to_float(T v) { return (float)v; }
 
+// Voxel (x, y, z) of a bricked volume (core voxels, no apron lookup needed).
+template <typename T>
+__device__ __forceinline__ T brick_voxel(const T* __restrict__ bricks, const BrickLayout& L, int x, int y, int z) {
+    const int bx = x >> L.shift, by = y >> L.shift, bz = z >> L.shift;
+    const long long b = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
+    return bricks[b * L.brick_stride +
+                  ((z - (bz << L.shift) + APRON_LO) * L.S + (y - (by << L.shift) + APRON_LO)) * L.S +
+                  (x - (bx << L.shift) + APRON_LO)];
+}
+
+// HalfSampleMean (volumeoctree.cpp:188-202) on the stored type: integers
+// summed exactly, divided by 8 with truncation; floats summed in z, y, x
+// order and scaled by 1/8.
+template <typename T> struct HalfSum { using A = uint32_t; };
+template <> struct HalfSum<float> { using A = float; };
+template <typename T> __device__ __forceinline__ T half_mean(typename HalfSum<T>::A s) { return (T)(s / 8u); }
+template <> __device__ __forceinline__ float half_mean<float>(float s) { return __fmul_rn(s, 0.125f); }
+
+template <typename T>
+__global__ void half_sample_kernel(const T* __restrict__ bricks, BrickLayout L, int d1x, int d1y, int d1z,
+                                   T* __restrict__ out) {
+    const long long total = (long long)d1x * d1y * d1z;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int x1 = (int)(i % d1x), y1 = (int)((i / d1x) % d1y), z1 = (int)(i / ((long long)d1x * d1y));
+        typename HalfSum<T>::A sum = 0;
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx) {
+                    const int x = min(2 * x1 + dx, L.dims[0] - 1), y = min(2 * y1 + dy, L.dims[1] - 1),
+                              z = min(2 * z1 + dz, L.dims[2] - 1);
+                    sum += (typename HalfSum<T>::A)brick_voxel(bricks, L, x, y, z);
+                }
+        out[i] = half_mean<T>(sum);
+    }
+}
+
 // One CTA per brick: min/max of the stored values over local [APRON_LO,
 // APRON_LO + B] on each axis (core + one voxel on the high side), i.e. the
 // voxels any trilinear stencil whose floor lies in the brick can touch.
@@ -188,6 +225,27 @@ cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout&
             break;
         default:
             brick_build_kernel<float><<<g, 256, 0, s>>>((const float*)linear, L, (float*)bricks);
+            break;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_half_sample(const void* bricks, int dtype, const BrickLayout& L, const int dims1[3], void* out,
+                               cudaStream_t s) {
+    const long long total = (long long)dims1[0] * dims1[1] * dims1[2];
+    const int g = grid_for(total, 256);
+    switch (dtype) {
+        case VRC_U8:
+            half_sample_kernel<uint8_t><<<g, 256, 0, s>>>((const uint8_t*)bricks, L, dims1[0], dims1[1], dims1[2],
+                                                          (uint8_t*)out);
+            break;
+        case VRC_U16:
+            half_sample_kernel<uint16_t><<<g, 256, 0, s>>>((const uint16_t*)bricks, L, dims1[0], dims1[1], dims1[2],
+                                                           (uint16_t*)out);
+            break;
+        default:
+            half_sample_kernel<float><<<g, 256, 0, s>>>((const float*)bricks, L, dims1[0], dims1[1], dims1[2],
+                                                        (float*)out);
             break;
     }
     return cudaGetLastError();

@@ -82,7 +82,11 @@ struct MarchParams {
     int pi_res;
     int pi_chain;                // a step moves less than 0.99 voxel per axis: empty-to-empty segments skip
     const int* brick_slot;       // brick -> slot in `bricks` (a device brick cache) or -1, nullptr = direct
-    const void* host_pool;       // mapped host pool read for slot -1
+    const void* host_pool;       // mapped host pool read for slot -1 (when lod_bricks is null)
+    const void* lod_bricks;      // half-resolution level read for slot -1, nullptr = read the host pool
+    int lod_nb[3];               // its brick grid (same brick size and stride as the full level)
+    float lod_dimf[3], lod_dim_m1[3];
+    uint32_t* brick_used;        // one bit per brick touched by a sample or tap, nullptr = not tracked
     float mida_gamma;            // "gammaValue" of MIDA compositing
 };
 
@@ -138,6 +142,11 @@ cudaError_t launch_march_batch(const BatchReq* reqs, int nreq, const unsigned* t
 cudaError_t launch_brick_gather(const void* pool, const long long* ids, const long long* dst, long long n,
                                 size_t brick_stride_bytes, void* cache, cudaStream_t s);
 cudaError_t launch_brick_build(const void* linear, int dtype, const BrickLayout& L, void* bricks, cudaStream_t s);
+// Half-resolution linear volume from a bricked one: voxel (x, y, z) = mean of
+// the full-resolution voxels 2x..2x+1 (clamped to the volume) on each axis;
+// integers summed exactly and divided by 8 with truncation.
+cudaError_t launch_half_sample(const void* bricks, int dtype, const BrickLayout& L, const int dims1[3], void* out,
+                               cudaStream_t s);
 cudaError_t launch_brick_minmax(const void* bricks, int dtype, const BrickLayout& L, float* bmin, float* bmax,
                                 cudaStream_t s);
 // Min/max of normalised intensity per cell of edge C over the cell's voxels
@@ -204,6 +213,18 @@ struct vrc_volume {
     std::vector<uint32_t> h_occ;       // occupancy the cache was filled for
     bool cache_valid = false;
     long long cache_reachable = 0;     // bricks the current TF can reach
+    // refinement: bricks the last frame touched (d_used) displace bricks it
+    // did not touch; h_last_used = frame that last touched a brick
+    uint32_t* d_used = nullptr;
+    std::vector<uint32_t> h_last_used;
+    uint32_t frame = 0;
+    bool used_pending = false;         // d_used holds the last frame's bits
+    long long last_misses = 0;         // bricks touched without a slot in the last frame
+    // half-resolution level (2x2x2 mean), device resident, sampled for
+    // bricks without a slot when lod_on
+    void* d_lod = nullptr;
+    vrc::BrickLayout lod_L{};
+    bool lod_on = false;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
     vrc_cell_level levels[2];  // skip cells of edge 8 and 16 (when smaller than the brick)
