@@ -165,9 +165,9 @@ __device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__
 // host pool, so every brick stays readable whatever the cache holds -- or,
 // with a level of detail attached, not at all: nullptr, and the caller
 // samples the half-resolution level instead.
-template <typename T>
+template <bool POOL, typename T>
 __device__ __forceinline__ const T* brick_base(const MarchParams& P, const T* __restrict__ bricks, long long brick) {
-    if (!P.brick_slot) return bricks + brick * P.L.brick_stride;
+    if (!POOL) return bricks + brick * P.L.brick_stride;
     const int slot = __ldg(P.brick_slot + brick);
     if (slot >= 0) return bricks + (long long)slot * P.L.brick_stride;
     return P.lod_bricks ? nullptr : reinterpret_cast<const T*>(P.host_pool) + brick * P.L.brick_stride;
@@ -210,7 +210,7 @@ __device__ __forceinline__ float lod_tap_voxel(const MarchParams& P, float vx, f
     return lod_tap<DT, RAW>(P, d_(a_(vx, 0.5f), P.dimf[0]), d_(a_(vy, 0.5f), P.dimf[1]), d_(a_(vz, 0.5f), P.dimf[2]));
 }
 
-template <int DT>
+template <int DT, bool POOL>
 __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
                                                 float vx, float vy, float vz) {
     const BrickLayout& L = P.L;
@@ -220,9 +220,9 @@ __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const type
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int o = ((iz - (bz << L.shift) + APRON_LO) * L.S + (iy - (by << L.shift) + APRON_LO)) * L.S +
                   (ix - (bx << L.shift) + APRON_LO);
-    if (P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
-    const typename Vox<DT>::T* b = brick_base(P, bricks, brick);
-    if (!b) return lod_tap_voxel<DT, true>(P, vx, vy, vz);
+    if (POOL && P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
+    const typename Vox<DT>::T* b = brick_base<POOL>(P, bricks, brick);
+    if (POOL && !b) return lod_tap_voxel<DT, true>(P, vx, vy, vz);
     return tri_raw<DT>(b, o, L.S, L.S * L.S, vx - flx, vy - fly, vz - flz);
 }
 
@@ -230,7 +230,7 @@ __device__ __noinline__ float tap_raw_any_brick(const MarchParams& P, const type
 // (clamped voxel coordinate on that axis, as calcGradientA's texture lookup
 // gives it) with the centre's coordinates on the other axes. Reads from the
 // centre's brick when the stencil fits in its apron.
-template <int DT, int AXIS>
+template <int DT, int AXIS, bool POOL>
 __device__ __forceinline__ float grad_tap(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
                                           const typename Vox<DT>::T* __restrict__ b, int o, int lc, int ic, float vt,
                                           float vx, float vy, float vz, float fx, float fy, float fz) {
@@ -238,13 +238,13 @@ __device__ __forceinline__ float grad_tap(const MarchParams& P, const typename V
     const int it = (int)fl;
     const int lt = lc + (it - ic);
     const int S = P.L.S, S2 = P.L.S * P.L.S;
-    if (b && lt >= 0 && lt <= P.L.B + 1) {
+    if ((!POOL || b) && lt >= 0 && lt <= P.L.B + 1) {
         const int stride = AXIS == 0 ? 1 : (AXIS == 1 ? S : S2);
         const float ft = vt - fl;
         return tri_raw<DT>(b, o + (it - ic) * stride, S, S2, AXIS == 0 ? ft : fx, AXIS == 1 ? ft : fy,
                            AXIS == 2 ? ft : fz);
     }
-    return tap_raw_any_brick<DT>(P, bricks, AXIS == 0 ? vt : vx, AXIS == 1 ? vt : vy, AXIS == 2 ? vt : vz);
+    return tap_raw_any_brick<DT, POOL>(P, bricks, AXIS == 0 ? vt : vx, AXIS == 1 ? vt : vy, AXIS == 2 ? vt : vz);
 }
 
 // phongShading (mod_shading.frag:134-151), ka = kd = TF colour, ks = 1.
@@ -431,7 +431,7 @@ __device__ __forceinline__ void jump_empty_run(float& t, int& loop, float step, 
 
 // Normalised trilinear value at a clamped voxel position, read from the
 // brick holding its floor voxel, in the exact order of the intensity sample.
-template <int DT>
+template <int DT, bool POOL>
 __device__ __forceinline__ float tap_norm(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
                                           float vx, float vy, float vz) {
     const BrickLayout& L = P.L;
@@ -441,9 +441,9 @@ __device__ __forceinline__ float tap_norm(const MarchParams& P, const typename V
     const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
     const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
               lz = iz - (bz << L.shift) + APRON_LO;
-    if (P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
-    const typename Vox<DT>::T* b = brick_base(P, bricks, brick);
-    if (!b) return lod_tap_voxel<DT, false>(P, vx, vy, vz);
+    if (POOL && P.brick_used) atomicOr(P.brick_used + (brick >> 5), 1u << (brick & 31));
+    const typename Vox<DT>::T* b = brick_base<POOL>(P, bricks, brick);
+    if (POOL && !b) return lod_tap_voxel<DT, false>(P, vx, vy, vz);
     return tri_at<DT>(b, (lz * L.S + ly) * L.S + lx, L.S, L.S * L.S, s_(vx, flx),
                       s_(vy, fly), s_(vz, flz));
 }
@@ -456,15 +456,15 @@ __device__ __forceinline__ float to_voxel(const MarchParams& P, int axis, float 
 // calcGradientA (mod_gradients.frag:202-214) with exactly rounded taps, in
 // the order the CPU restatement evaluates it: six normalised trilinear
 // lookups at +-1/dim in texture space, (v(-) - v(+)) * 0.5/spacing * rwmScale.
-template <int DT>
+template <int DT, bool POOL>
 __device__ F3 gradient_exact(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks, float sx, float sy,
                              float sz, float vx, float vy, float vz) {
-    const float v0 = tap_norm<DT>(P, bricks, to_voxel(P, 0, a_(sx, P.offs[0])), vy, vz);
-    const float v1 = tap_norm<DT>(P, bricks, vx, to_voxel(P, 1, a_(sy, P.offs[1])), vz);
-    const float v2 = tap_norm<DT>(P, bricks, vx, vy, to_voxel(P, 2, a_(sz, P.offs[2])));
-    const float v3 = tap_norm<DT>(P, bricks, to_voxel(P, 0, s_(sx, P.offs[0])), vy, vz);
-    const float v4 = tap_norm<DT>(P, bricks, vx, to_voxel(P, 1, s_(sy, P.offs[1])), vz);
-    const float v5 = tap_norm<DT>(P, bricks, vx, vy, to_voxel(P, 2, s_(sz, P.offs[2])));
+    const float v0 = tap_norm<DT, POOL>(P, bricks, to_voxel(P, 0, a_(sx, P.offs[0])), vy, vz);
+    const float v1 = tap_norm<DT, POOL>(P, bricks, vx, to_voxel(P, 1, a_(sy, P.offs[1])), vz);
+    const float v2 = tap_norm<DT, POOL>(P, bricks, vx, vy, to_voxel(P, 2, a_(sz, P.offs[2])));
+    const float v3 = tap_norm<DT, POOL>(P, bricks, to_voxel(P, 0, s_(sx, P.offs[0])), vy, vz);
+    const float v4 = tap_norm<DT, POOL>(P, bricks, vx, to_voxel(P, 1, s_(sy, P.offs[1])), vz);
+    const float v5 = tap_norm<DT, POOL>(P, bricks, vx, vy, to_voxel(P, 2, s_(sz, P.offs[2])));
     return F3{m_(m_(s_(v3, v0), P.spacing_rcp_half[0]), P.rwm_scale),
               m_(m_(s_(v4, v1), P.spacing_rcp_half[1]), P.rwm_scale),
               m_(m_(s_(v5, v2), P.spacing_rcp_half[2]), P.rwm_scale)};
@@ -481,7 +481,7 @@ __device__ __forceinline__ float4 mida_step(float4 r, float v, float4 c, float m
 }
 
 // One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
-template <int DT, int COMP, int SHADE, int EE>
+template <int DT, int COMP, int SHADE, int EE, bool POOL = false>
 __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
                             int py, Counters& cnt, float2& aux) {
     using T = typename Vox<DT>::T;
@@ -607,15 +607,16 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
             ++cnt.fetched;
             const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
-            const T* __restrict__ b = brick_base(P, bricks, brick);
-            if (P.brick_used && brick != marked) {
+            const T* __restrict__ b = brick_base<POOL>(P, bricks, brick);
+            if (POOL && P.brick_used && brick != marked) {
                 marked = brick;
                 mark_used(P, brick);
             }
             const int lx = ix - (bx << L.shift) + APRON_LO, ly = iy - (by << L.shift) + APRON_LO,
                       lz = iz - (bz << L.shift) + APRON_LO;
             const int o = (lz * S + ly) * S + lx;
-            const float intensity = b ? tri_at<DT>(b, o, S, S2, fx, fy, fz) : lod_tap<DT, false>(P, sx, sy, sz);
+            const float intensity =
+                (!POOL || b) ? tri_at<DT>(b, o, S, S2, fx, fy, fz) : lod_tap<DT, false>(P, sx, sy, sz);
             const float rw = a_(m_(intensity, P.rwm_scale), P.rwm_offset);
             float4 c;
             if (PI) {
@@ -623,7 +624,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     ++cnt.fetched;
                     const float px_ = a_(f.x, m_(t_last, dx)), py_ = a_(f.y, m_(t_last, dy)),
                                 pz_ = a_(f.z, m_(t_last, dz));
-                    const float rwp = a_(m_(tap_norm<DT>(P, bricks, to_voxel(P, 0, px_), to_voxel(P, 1, py_),
+                    const float rwp = a_(m_(tap_norm<DT, POOL>(P, bricks, to_voxel(P, 0, px_), to_voxel(P, 1, py_),
                                                         to_voxel(P, 2, pz_)),
                                             P.rwm_scale),
                                          P.rwm_offset);
@@ -653,12 +654,12 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                         const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
                         const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
                         const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float v0 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
-                        const float v1 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
-                        const float v2 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
-                        const float v3 = grad_tap<DT, 0>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
-                        const float v4 = grad_tap<DT, 1>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
-                        const float v5 = grad_tap<DT, 2>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
+                        const float v0 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
+                        const float v1 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
+                        const float v2 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
+                        const float v3 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
+                        const float v4 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
+                        const float v5 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
                         g = F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
                     }
                     const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
@@ -712,7 +713,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     // the gradient exactly rounded; a zero gradient gives 0.5
                     if (res.x == 0.f && res.y == 0.f && res.z == 0.f) {
                         const F3 g = t == 0.f ? clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py)
-                                              : gradient_exact<DT>(P, bricks, sx, sy, sz, vx, vy, vz);
+                                              : gradient_exact<DT, POOL>(P, bricks, sx, sy, sz, vx, vy, vz);
                         const F3 n = normalize3(g);
                         res = make_float4(a_(d_(n.x, 2.f), 0.5f), a_(d_(n.y, 2.f), 0.5f), a_(d_(n.z, 2.f), 0.5f), 1.f);
                     }
@@ -759,7 +760,7 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
 #define VRC_MARCH_MIN_BLOCKS 3
 #endif
 
-template <int DT, int COMP, int SHADE, int EE>
+template <int DT, int COMP, int SHADE, int EE, bool POOL>
 __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchParams P) {
     extern __shared__ float4 s_tf[];
     for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_table[i];
@@ -789,7 +790,7 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
                             l.z == 0.f && l.w == 0.f;
             float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
             float2 ax = make_float2(1.f, 0.f);
-            if (!bg) r = march_ray<DT, COMP, SHADE, EE>(P, s_tf, f, l, px, py, cnt, ax);
+            if (!bg) r = march_ray<DT, COMP, SHADE, EE, POOL>(P, s_tf, f, l, px, py, cnt, ax);
             write_out(P, pix, r);
             if (P.aux) P.aux[pix] = ax;
         }
@@ -811,9 +812,9 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
     }
 }
 
-template <int DT, int COMP, int SHADE, int EE>
+template <int DT, int COMP, int SHADE, int EE, bool POOL>
 cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
-    auto k = march_kernel<DT, COMP, SHADE, EE>;
+    auto k = march_kernel<DT, COMP, SHADE, EE, POOL>;
     const size_t smem = (size_t)p.tf_width * sizeof(float4);
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -831,8 +832,13 @@ cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
 
 template <int DT, int COMP, int SHADE>
 cudaError_t launch_ee(const MarchParams& p, int num_sms, cudaStream_t s) {
-    return p.ee_mode == VRC_EE_ANALYTIC ? launch_t<DT, COMP, SHADE, VRC_EE_ANALYTIC>(p, num_sms, s)
-                                        : launch_t<DT, COMP, SHADE, VRC_EE_BUFFERS>(p, num_sms, s);
+    // POOL: a host-resident brick pool read through the device cache's slot
+    // table (and its level of detail); device-resident pools compile without it
+    if (p.brick_slot)
+        return p.ee_mode == VRC_EE_ANALYTIC ? launch_t<DT, COMP, SHADE, VRC_EE_ANALYTIC, true>(p, num_sms, s)
+                                            : launch_t<DT, COMP, SHADE, VRC_EE_BUFFERS, true>(p, num_sms, s);
+    return p.ee_mode == VRC_EE_ANALYTIC ? launch_t<DT, COMP, SHADE, VRC_EE_ANALYTIC, false>(p, num_sms, s)
+                                        : launch_t<DT, COMP, SHADE, VRC_EE_BUFFERS, false>(p, num_sms, s);
 }
 
 template <int DT, int COMP>
