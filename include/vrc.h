@@ -157,6 +157,14 @@ size_t vrc_volume_host_bytes(const vrc_volume* vol);
  * a larger store (OctreeBrickPoolManagerBase::getBrick,
  * include/voreen/core/datastructures/octree/octreebrickpoolmanager.h:99-165). */
 vrc_status vrc_volume_set_cache_limit(vrc_volume* vol, size_t bytes);
+/* Bytes of bricks gathered into the cache per render (0, the default =
+ * unlimited); at least one brick. With a budget, a TF change or a new view
+ * streams its bricks in over several renders, the bricks the last render
+ * read without a slot first -- Voreen's octree raycaster's per-frame brick
+ * upload budget (brickUploadBudgetMB, modules/opencl/processors/
+ * singleoctreeraycastercl.cpp:304). Images stay exact (or, with the level
+ * of detail on, converge) whatever the budget. */
+vrc_status vrc_volume_set_cache_upload_budget(vrc_volume* vol, size_t bytes_per_render);
 /* While the cache holds fewer bricks than the TF reaches (or a level of
  * detail is attached), each render records the bricks it reads; before the
  * next render, bricks read without a cache slot displace cached bricks that

@@ -148,3 +148,41 @@ def test_lod_rejected_for_device_pool(ctx):
     vol = v.Volume(ctx, w.voxels, w.spacing)
     with pytest.raises(v.VrcError):
         vol.set_lod(True)
+
+
+def test_upload_budget_streams_bricks_in(ctx):
+    """A per-render upload budget of 3 bricks: the cache grows by at most 3
+    bricks a render, every image stays exact, and the cache ends up holding
+    every brick the TF reaches."""
+    w, host, dev, tf, brick_bytes = _setup(ctx)
+    host.set_cache_upload_budget(3 * brick_bytes)
+    p = w.params(shading=v.SHADE_PHONG, entry_exit_mode=v.EE_ANALYTIC)
+    ref, _ = v.render(ctx, dev, tf, p, None, None, v.OUT_RGBA32F)
+    prev = 0
+    for i in range(200):
+        img, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+        np.testing.assert_array_equal(_bits(img), _bits(ref))
+        cached, reach, missed = host.cache_info()
+        assert cached - prev <= 3
+        prev = cached
+        if cached == reach:
+            break
+    assert cached == reach and i >= (reach - 1) // 3
+
+
+def test_upload_budget_with_lod_converges(ctx):
+    w, host, dev, tf, brick_bytes = _setup(ctx)
+    host.set_cache_upload_budget(4 * brick_bytes)
+    host.set_lod(True)
+    p = w.params(shading=v.SHADE_NONE, entry_exit_mode=v.EE_ANALYTIC)
+    ref, _ = v.render(ctx, dev, tf, p, None, None, v.OUT_RGBA32F)
+    first, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+    for _ in range(200):
+        img, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+        cached, reach, missed = host.cache_info()
+        if cached == reach and missed == 0:
+            break
+    # the last render read only cached bricks (misses are counted after it)
+    img, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+    np.testing.assert_array_equal(_bits(img), _bits(ref))
+    assert not np.array_equal(_bits(first), _bits(ref))

@@ -98,3 +98,52 @@ def test_process_preintegrated_like_the_oracle(ctx, classification):
                               oracle_params(p, preint_table=table), e, x, 32)
     np.testing.assert_array_equal(img.view(np.uint32), ref.view(np.uint32))
     r.deinitialize()
+
+
+def test_brick_streaming_property_defaults(vrc_lib):
+    r = CudaRaycaster()
+    assert r.brickPoolPlacement == "device" and r.brickBufferSizeMB == 0
+    assert r.brickUploadBudgetMB == 32 and r.useIterativeRefinement and not r.useLevelOfDetail
+    r.brickPoolPlacement = "disk"
+    r.volumeInport.setData(VolumeData(np.zeros((4, 4, 4), np.uint8)))
+    r._ctx = object()  # no device needed: the settings check comes first
+    r.process(analytic_entry_exit=True)
+    assert "brick settings" in r.lastError and not r.outport.hasData()
+
+
+@pytest.mark.gpu
+def test_process_host_placement_refines_to_the_device_image(ctx):
+    """brickPoolPlacement host with a small per-frame upload budget and the
+    level of detail: process() keeps setting `invalidated` while bricks
+    stream in, and the frame after the last one is the device-resident image."""
+    w = synth.config2(size=(96, 80, 64), image=(160, 120))
+    vd = VolumeData(w.voxels, w.spacing)
+
+    def proc(**kw):
+        r = CudaRaycaster()
+        r.volumeInport.setData(vd)
+        r.transferFunction.keys = w.tf_keys
+        r.transferFunction.width = w.tf_width
+        r.transferFunction.domain = w.domain
+        r.camera = w.params().camera
+        r.shading = "phong"
+        r.outport.setData(np.zeros((w.height, w.width, 4), np.float32))
+        for k, val in kw.items():
+            setattr(r, k, val)
+        return r
+
+    dev = proc()
+    dev.process(analytic_entry_exit=True)
+    ref = dev.outport.getData().copy()
+    host = proc(brickPoolPlacement="host", brickUploadBudgetMB=1, useLevelOfDetail=True)
+    frames = 0
+    host.process(analytic_entry_exit=True)
+    while host.invalidated and frames < 100:
+        host.process(analytic_entry_exit=True)
+        frames += 1
+    assert host.lastError == ""
+    assert frames >= 1  # 18 bricks of 85,760 B at 12 per frame
+    host.process(analytic_entry_exit=True)
+    np.testing.assert_array_equal(host.outport.getData(), ref)
+    dev.deinitialize()
+    host.deinitialize()

@@ -189,6 +189,11 @@ class Volume:
                "vrc_volume_cache_info")
         return int(c.value), int(r.value), int(m.value)
 
+    def set_cache_upload_budget(self, nbytes: int):
+        """Bytes of bricks gathered into the device cache per render (0 = unlimited)."""
+        _check(lib().vrc_volume_set_cache_upload_budget(self.handle, int(nbytes)), self.ctx,
+               "vrc_volume_set_cache_upload_budget")
+
     def set_lod(self, enable: bool = True):
         """Sample bricks without a cache slot from a device-resident
         half-resolution level (host-placed pools only)."""

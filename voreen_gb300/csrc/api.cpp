@@ -419,9 +419,16 @@ vrc_status vrc_volume_set_cache_limit(vrc_volume* v, size_t bytes) {
         v->d_cache_ids = v->d_cache_dst = nullptr;
         v->cache_slots = 0;
         v->h_slot_brick.clear();
+        v->free_slots.clear();
         std::fill(v->h_slot.begin(), v->h_slot.end(), -1);
     }
     v->cache_valid = false;
+    return VRC_OK;
+}
+
+vrc_status vrc_volume_set_cache_upload_budget(vrc_volume* v, size_t bytes_per_render) {
+    if (!v) return VRC_ERR_INVALID_ARG;
+    v->upload_budget = bytes_per_render;
     return VRC_OK;
 }
 
@@ -840,7 +847,11 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
     if (vol->h_slot.size() != (size_t)nb) vol->h_slot.assign((size_t)nb, -1);
     if (vol->h_last_used.size() != (size_t)nb) vol->h_last_used.assign((size_t)nb, 0);
     if (!vol->d_slot) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_slot, (size_t)nb * sizeof(int)));
+    bool table_changed = false;
     if (!(vol->cache_valid && occ == vol->h_occ)) {
+        // the slot table is uploaded whenever the cache is (re)planned: a new
+        // table, a reallocation or evictions all change it
+        table_changed = true;
         // wanted bricks in priority order: occupied, then the dilation ring
         std::vector<uint8_t> mark(nb, 0);
         std::vector<long long> want;
@@ -883,6 +894,7 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
             vol->d_cache_ids = vol->d_cache_dst = nullptr;
             vol->cache_slots = 0;
             vol->h_slot_brick.clear();
+            vol->free_slots.clear();
             std::fill(vol->h_slot.begin(), vol->h_slot.end(), -1);
             cudaError_t e = cudaMalloc(&vol->d_cache, (size_t)slots * brick_bytes);
             if (e == cudaSuccess) e = cudaMalloc((void**)&vol->d_cache_ids, (size_t)slots * sizeof(long long));
@@ -898,37 +910,41 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
             } else {
                 vol->cache_slots = slots;
                 vol->h_slot_brick.assign((size_t)slots, -1);
+                for (long long sl = slots - 1; sl >= 0; --sl) vol->free_slots.push_back(sl);
             }
         }
-        // keep cached bricks that are still wanted within the slot budget
+        // keep cached bricks that are still wanted within the slot budget;
+        // the wanted ones not cached yet queue for gathering
         std::vector<uint8_t> keep(nb, 0);
         for (long long k = 0; k < slots; ++k) keep[want[k]] = 1;
-        std::vector<long long> free_slots;
         for (long long sl = 0; sl < vol->cache_slots; ++sl) {
             const long long b = vol->h_slot_brick[sl];
-            if (b >= 0 && keep[b]) continue;
-            if (b >= 0) vol->h_slot[b] = -1;
+            if (b < 0 || keep[b]) continue;
+            vol->h_slot[b] = -1;
             vol->h_slot_brick[sl] = -1;
-            free_slots.push_back(sl);
+            vol->free_slots.push_back(sl);
         }
-        std::vector<long long> ids, dst;
-        for (long long k = 0; k < slots; ++k) {
-            const long long b = want[k];
-            if (vol->h_slot[b] >= 0) continue;
-            const long long sl = free_slots.back();
-            free_slots.pop_back();
-            vol->h_slot[b] = (int)sl;
-            vol->h_slot_brick[sl] = b;
-            ids.push_back(b);
-            dst.push_back(sl);
-        }
-        vrc_status st = commit_slots(ctx, vol, ids, dst, brick_bytes, s);
-        if (st != VRC_OK) return st;
+        vol->pending.clear();
+        vol->pending_pos = 0;
+        for (long long k = 0; k < slots; ++k)
+            if (vol->h_slot[want[k]] < 0) vol->pending.push_back(want[k]);
         vol->h_occ = occ;
         vol->cache_valid = true;
     }
+    // this render's gathers: bricks the last frame read without a slot first
+    // (into free slots, else slots of bricks it did not read, oldest first),
+    // then queued TF-wanted bricks into free slots, up to the upload budget
+    const size_t budget = vol->upload_budget ? std::max<size_t>(1, vol->upload_budget / brick_bytes) : SIZE_MAX;
+    std::vector<long long> ids, dst;
+    auto place = [&](long long b, long long sl) {
+        const long long old = vol->h_slot_brick[sl];
+        if (old >= 0) vol->h_slot[old] = -1;
+        vol->h_slot[b] = (int)sl;
+        vol->h_slot_brick[sl] = b;
+        ids.push_back(b);
+        dst.push_back(sl);
+    };
     if (!used.empty()) {
-        // refinement from the bricks the last frame read
         const uint32_t stamp = ++vol->frame;
         std::vector<long long> missed;
         for (size_t w = 0; w < words; ++w)
@@ -940,36 +956,40 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
             }
         vol->last_misses = (long long)missed.size();
         if (!missed.empty() && vol->cache_slots > 0) {
-            // free slots first, then slots whose brick the frame did not read, oldest first
-            std::vector<long long> cand;
             std::vector<std::pair<uint32_t, long long>> stale;
             for (long long sl = 0; sl < vol->cache_slots; ++sl) {
                 const long long b = vol->h_slot_brick[sl];
-                if (b < 0)
-                    cand.push_back(sl);
-                else if (vol->h_last_used[b] != stamp)
-                    stale.emplace_back(vol->h_last_used[b], sl);
+                if (b >= 0 && vol->h_last_used[b] != stamp) stale.emplace_back(vol->h_last_used[b], sl);
             }
             std::stable_sort(stale.begin(), stale.end(),
                              [](const std::pair<uint32_t, long long>& x, const std::pair<uint32_t, long long>& y) {
                                  return x.first < y.first;
                              });
-            for (const auto& e : stale) cand.push_back(e.second);
-            const size_t n = std::min(missed.size(), cand.size());
-            std::vector<long long> ids, dst;
-            for (size_t k = 0; k < n; ++k) {
-                const long long sl = cand[k], b = missed[k];
-                const long long old = vol->h_slot_brick[sl];
-                if (old >= 0) vol->h_slot[old] = -1;
-                vol->h_slot[b] = (int)sl;
-                vol->h_slot_brick[sl] = b;
-                ids.push_back(b);
-                dst.push_back(sl);
+            size_t next_stale = 0;
+            for (long long b : missed) {
+                if (ids.size() >= budget) break;
+                if (!vol->free_slots.empty()) {
+                    place(b, vol->free_slots.back());
+                    vol->free_slots.pop_back();
+                } else if (next_stale < stale.size()) {
+                    place(b, stale[next_stale++].second);
+                } else {
+                    break;
+                }
             }
-            vrc_status st = commit_slots(ctx, vol, ids, dst, brick_bytes, s);
-            if (st != VRC_OK) return st;
         }
     }
+    while (vol->pending_pos < vol->pending.size() && ids.size() < budget && !vol->free_slots.empty()) {
+        const long long b = vol->pending[vol->pending_pos++];
+        if (vol->h_slot[b] >= 0) continue;
+        place(b, vol->free_slots.back());
+        vol->free_slots.pop_back();
+    }
+    if (!ids.empty() || table_changed) {
+        vrc_status st = commit_slots(ctx, vol, ids, dst, brick_bytes, s);
+        if (st != VRC_OK) return st;
+    }
+    const long long resident = vol->cache_slots - (long long)vol->free_slots.size();
     const bool lod = vol->lod_on && vol->d_lod;
     if (vol->cache_slots > 0 || lod) {
         P.bricks = vol->d_cache ? vol->d_cache : vol->d_bricks;
@@ -984,7 +1004,7 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
             P.lod_dim_m1[i] = float(vol->lod_L.dims[i] - 1);
         }
     }
-    if (vol->cache_slots > 0 && (lod || vol->cache_slots < vol->cache_reachable)) {
+    if (vol->cache_slots > 0 && (lod || resident < vol->cache_reachable)) {
         if (!vol->d_used) VRC_CUDA(ctx, cudaMalloc((void**)&vol->d_used, words * 4));
         VRC_CUDA(ctx, cudaMemsetAsync(vol->d_used, 0, words * 4, s));
         P.brick_used = vol->d_used;

@@ -211,6 +211,10 @@ struct vrc_volume {
     std::vector<int> h_slot;           // host copy of d_slot
     std::vector<long long> h_slot_brick;  // slot -> brick, -1 = free
     std::vector<uint32_t> h_occ;       // occupancy the cache was filled for
+    std::vector<long long> free_slots; // slots holding no brick
+    std::vector<long long> pending;    // TF-wanted bricks not gathered yet, priority order
+    size_t pending_pos = 0;
+    size_t upload_budget = 0;          // bytes gathered per render, 0 = unlimited
     bool cache_valid = false;
     long long cache_reachable = 0;     // bricks the current TF can reach
     // refinement: bricks the last frame touched (d_used) displace bricks it

@@ -39,6 +39,19 @@ reference so tests read like its processor code:
               (rescaleRendering, volumeraycaster.cpp:348-375). The coarse
               frame's rays go through the coarse pixel centres (analytic
               entry/exit at the coarse size).
+  bricks      Volumes larger than device memory, with the streaming controls
+              of Voreen's octree raycaster (SingleOctreeRaycasterCL,
+              modules/opencl/processors/singleoctreeraycastercl.cpp:294-305):
+              brickPoolPlacement ("device" / "host": the bricked volume in
+              pinned host memory), brickBufferSizeMB (device brick cache;
+              0 = as much as free device memory allows, the reference's 512 MB
+              default is too small for a GB300), brickUploadBudgetMB (32, bricks
+              gathered per frame), useLevelOfDetail (a half-resolution level
+              stands in for bricks not in the cache) and useIterativeRefinement
+              (true): after a frame that read bricks without a slot the
+              processor sets `invalidated`, as the reference invalidates
+              itself until no more bricks are uploaded
+              (singleoctreeraycastercl.cpp:780-838, 880-894).
 """
 from __future__ import annotations
 
@@ -48,7 +61,8 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, FHN, FHP, ISO, MIDA, MIP, MOP,
-               OUT_RGBA32F, SHADE_NONE, SHADE_PHONG, Context, PreIntegrationTable, TransferFunction, Volume, VrcError,
+               OUT_RGBA32F, PLACE_DEVICE, PLACE_HOST, SHADE_NONE, SHADE_PHONG, Context, PreIntegrationTable,
+               TransferFunction, Volume, VrcError,
                default_params, image_rescale, make_camera, render, sampling_step)
 
 log = logging.getLogger("voreen.CudaRaycaster")
@@ -57,6 +71,7 @@ COMPOSITING = {"dvr": DVR, "mip": MIP, "iso": ISO, "mop": MOP, "mida": MIDA, "fh
 CLASSIFICATION = ("transfer-function", "pre-integrated-gpu", "pre-integrated-cpu", "pre-integrated-approximation")
 PREINT_TABLE_SIZES = (0, 256, 512, 1024)
 SHADING = {"none": SHADE_NONE, "phong": SHADE_PHONG}
+PLACEMENT = {"device": PLACE_DEVICE, "host": PLACE_HOST}
 
 
 @dataclass
@@ -129,12 +144,20 @@ class CudaRaycaster:
         self.applyLightAttenuation = False
         self.lightAttenuation = (1.0, 0.0, 0.0)
         self.camera = make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0))
+        self.brickPoolPlacement = "device"
+        self.brickBufferSizeMB = 0
+        self.brickUploadBudgetMB = 32
+        self.useLevelOfDetail = False
+        self.useIterativeRefinement = True
+        self.invalidated = False
         self.lastError = ""
         self._device = device
         self._ctx = None
         self._vol = None
         self._vol_src = None
         self._preint = None       # (key, PreIntegrationTable): the cached table
+        self._vol_placement = None
+        self._last_missed = -1
 
     # Processor lifecycle ---------------------------------------------------
     def initialize(self):
@@ -203,13 +226,26 @@ class CudaRaycaster:
         if not (0.01 <= self.samplingRate <= 20.0):
             self._error(f"samplingRate {self.samplingRate} outside [0.01, 20]")
             return
+        if self.brickPoolPlacement not in PLACEMENT or not (0 <= self.brickBufferSizeMB) or \
+                not (1 <= self.brickUploadBudgetMB <= 1024):
+            self._error(f"brick settings out of range: {self.brickPoolPlacement}/{self.brickBufferSizeMB}/"
+                        f"{self.brickUploadBudgetMB}")
+            return
         vd: VolumeData = self.volumeInport.getData()
+        self.invalidated = False
         try:
-            if self._vol is None or self._vol_src is not vd:
+            placement = PLACEMENT[self.brickPoolPlacement]
+            if self._vol is None or self._vol_src is not vd or self._vol_placement != placement:
                 if self._vol is not None:
                     self._vol.close()
-                self._vol = Volume(self._ctx, vd.voxels, vd.spacing, vd.offset, vd.rwm)
+                self._vol = Volume(self._ctx, vd.voxels, vd.spacing, vd.offset, vd.rwm, placement=placement)
                 self._vol_src = vd
+                self._vol_placement = placement
+            if placement == PLACE_HOST:
+                mb = 1 << 20
+                self._vol.set_cache_limit(int(self.brickBufferSizeMB) * mb if self.brickBufferSizeMB else 2**62)
+                self._vol.set_cache_upload_budget(int(self.brickUploadBudgetMB) * mb)
+                self._vol.set_lod(bool(self.useLevelOfDetail))
             self._fit_tf(self._vol)
             t = self.transferFunction
             rgba = TransferFunction.bake(t.keys, t.width, t.gamma, t.threshold)
@@ -261,5 +297,15 @@ class CudaRaycaster:
             tf.close()
             self.outport.setData(img)
             self.lastStats = stats
+            if placement == PLACE_HOST and self.useIterativeRefinement:
+                # another frame helps while the cache is still filling, or
+                # while the bricks read without a slot keep changing; a frame
+                # that can bring in nothing new ends the refinement
+                cached, reachable, missed = self._vol.cache_info()
+                nb = int(np.prod(self._vol.brick_minmax()[2]))
+                capacity = (int(self.brickBufferSizeMB) << 20) // max(1, self._vol.host_bytes // nb) \
+                    if self.brickBufferSizeMB else reachable
+                self.invalidated = cached < min(reachable, capacity) or (missed > 0 and missed != self._last_missed)
+                self._last_missed = missed
         except VrcError as e:
             self._error(str(e))
