@@ -14,7 +14,7 @@ def declared_symbols():
         if f.endswith(".h"):
             src = open(os.path.join(inc, f)).read()
             src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-            names |= set(re.findall(r"\b(vrc_[a-z0-9_]+)\s*\(", src))
+            names |= set(re.findall(r"\b(vrcp?_[a-z0-9_]+)\s*\(", src))
     return names
 
 
@@ -27,7 +27,7 @@ def test_library_exports_every_declared_symbol(vrc_lib):
 
 def test_python_signatures_cover_the_headers(vrc_lib):
     from voreen_gb300 import _abi
-    assert declared_symbols() == set(_abi.SIGNATURES) | set(_abi.NN_SIGNATURES)
+    assert declared_symbols() == set(_abi.SIGNATURES) | set(_abi.NN_SIGNATURES) | set(_abi.PROC_SIGNATURES)
 
 
 def test_host_only_entry_points_work_without_gpu(vrc_lib):

@@ -16,13 +16,15 @@ def test_ports_and_property_defaults(vrc_lib):
     assert r.outport.name == "image.output"
     assert r.samplingRate == 2.0 and r.isoValue == 0.5
     assert r.compositing == "dvr" and r.gradient == "central-differences"
-    assert r.lightPosition == (2.3, 1.5, 1.5, 1.0) and r.materialShininess == 60.0
+    # FloatVec4Property: float32 values
+    assert np.allclose(r.lightPosition, (2.3, 1.5, 1.5, 1.0), rtol=0, atol=1e-6) and r.materialShininess == 60.0
+    assert r.lightAmbient[:3] == (np.float32(0.4),) * 3 and r.lightAttenuation == (1.0, 0.0, 0.0)
+    assert r.className == "CudaRaycaster" and r.category == "Raycasting"
     assert not r.isReady()
 
 
 def test_process_not_ready_logs_and_returns(vrc_lib):
     r = CudaRaycaster()
-    r._ctx = object()  # no device needed: process() must stop before touching it
     r.process()
     assert "not ready" in r.lastError and not r.outport.hasData()
 
@@ -58,7 +60,6 @@ def test_preintegrated_gpu_falls_back_with_an_error(vrc_lib):
     """cpuraycaster.cpp:123-129: pre-integrated-gpu logs an error, selects
     pre-integrated-cpu and renders nothing this call."""
     r = CudaRaycaster()
-    r._ctx = object()
     w = synth.config1(size=(8, 8, 8), image=(4, 4))
     r.volumeInport.setData(VolumeData(w.voxels))
     r.entryPort.setData(np.zeros((4, 4, 4), np.float32))
@@ -106,7 +107,6 @@ def test_brick_streaming_property_defaults(vrc_lib):
     assert r.brickUploadBudgetMB == 32 and r.useIterativeRefinement and not r.useLevelOfDetail
     r.brickPoolPlacement = "disk"
     r.volumeInport.setData(VolumeData(np.zeros((4, 4, 4), np.uint8)))
-    r._ctx = object()  # no device needed: the settings check comes first
     r.process(analytic_entry_exit=True)
     assert "brick settings" in r.lastError and not r.outport.hasData()
 
@@ -147,3 +147,30 @@ def test_process_host_placement_refines_to_the_device_image(ctx):
     np.testing.assert_array_equal(host.outport.getData(), ref)
     dev.deinitialize()
     host.deinitialize()
+
+
+def test_properties_by_id_through_the_c_shim(vrc_lib):
+    """The C shim addresses properties by id like Processor::getProperty(id):
+    unknown ids and wrong kinds are errors, values round-trip."""
+    import ctypes as C
+    r = CudaRaycaster()
+    h = r._h
+    assert vrc_lib.vrcp_class_name() == b"CudaRaycaster" and vrc_lib.vrcp_category() == b"Raycasting"
+    f = C.c_float()
+    assert vrc_lib.vrcp_set_float(h, b"samplingRate", C.c_float(4.5)) == 0
+    assert vrc_lib.vrcp_get_float(h, b"samplingRate", C.byref(f)) == 0 and f.value == 4.5
+    assert vrc_lib.vrcp_set_float(h, b"noSuchProperty", C.c_float(1)) != 0
+    assert vrc_lib.vrcp_set_int(h, b"samplingRate", 3) != 0  # a float property
+    assert vrc_lib.vrcp_set_string(h, b"compositing", b"mida") == 0 and r.compositing == "mida"
+    buf = C.create_string_buffer(4)
+    assert vrc_lib.vrcp_get_string(h, b"classification", buf, 4) == 0 and buf.value == b"tra"
+    assert vrc_lib.vrcp_set_floatv(h, b"lightPosition", (C.c_float * 3)(1, 2, 3), 3) != 0  # vec4
+    r.clipRegion = ((1, 2, 3), (10, 20, 30))
+    r._push()
+    v = (C.c_int * 6)()
+    assert vrc_lib.vrcp_get_intv(h, b"clipRegion", v, 6) == 0 and list(v) == [1, 2, 3, 10, 20, 30]
+    r.samplingRate = 25.0  # accepted, rejected by process() like Voreen's range check there
+    r.volumeInport.setData(VolumeData(np.zeros((4, 4, 4), np.uint8)))
+    r.process(analytic_entry_exit=True)
+    assert "samplingRate" in r.lastError and not r.outport.hasData()
+    r.close()

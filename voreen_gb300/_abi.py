@@ -151,6 +151,41 @@ NN_SIGNATURES = {
     "vrc_nn_weights_tc": [VP, _I, _I, _I, _I, VP, VP],
 }
 
+# include/vrc_processor.h: the CudaRaycaster processor shim
+_S = C.c_char_p
+PROC_SIGNATURES = {
+    "vrcp_create": (C.c_int, [C.c_int, P(VP)]),
+    "vrcp_destroy": (C.c_int, [VP]),
+    "vrcp_class_name": (_S, []),
+    "vrcp_category": (_S, []),
+    "vrcp_set_float": (C.c_int, [VP, _S, C.c_float]),
+    "vrcp_get_float": (C.c_int, [VP, _S, P(C.c_float)]),
+    "vrcp_set_int": (C.c_int, [VP, _S, C.c_int]),
+    "vrcp_get_int": (C.c_int, [VP, _S, P(C.c_int)]),
+    "vrcp_set_string": (C.c_int, [VP, _S, _S]),
+    "vrcp_get_string": (C.c_int, [VP, _S, C.c_char_p, C.c_int]),
+    "vrcp_set_floatv": (C.c_int, [VP, _S, P(C.c_float), C.c_int]),
+    "vrcp_get_floatv": (C.c_int, [VP, _S, P(C.c_float), C.c_int]),
+    "vrcp_set_intv": (C.c_int, [VP, _S, P(C.c_int), C.c_int]),
+    "vrcp_get_intv": (C.c_int, [VP, _S, P(C.c_int), C.c_int]),
+    "vrcp_set_camera": (C.c_int, [VP, P(Camera)]),
+    "vrcp_get_camera": (C.c_int, [VP, P(Camera)]),
+    "vrcp_set_tf_keys": (C.c_int, [VP, P(TFKey), C.c_int, C.c_float, C.c_float, C.c_float]),
+    "vrcp_set_tf_domain": (C.c_int, [VP, C.c_float, C.c_float, C.c_int, C.c_int]),
+    "vrcp_get_tf": (C.c_int, [VP, P(C.c_int), P(C.c_float), P(C.c_float), P(C.c_int)]),
+    "vrcp_set_volume": (C.c_int, [VP, P(VolumeDesc), VP]),
+    "vrcp_set_entry_exit": (C.c_int, [VP, VP, VP, C.c_int, C.c_int]),
+    "vrcp_set_output_size": (C.c_int, [VP, C.c_int, C.c_int]),
+    "vrcp_is_ready": (C.c_int, [VP]),
+    "vrcp_initialize": (None, [VP]),
+    "vrcp_deinitialize": (None, [VP]),
+    "vrcp_process": (None, [VP, C.c_int, C.c_int]),
+    "vrcp_output": (C.c_int, [VP, P(P(C.c_float)), P(C.c_int), P(C.c_int)]),
+    "vrcp_last_error": (_S, [VP]),
+    "vrcp_last_stats": (C.c_int, [VP, P(RenderStats)]),
+    "vrcp_invalidated": (C.c_int, [VP]),
+}
+
 _lib = None
 
 
@@ -169,6 +204,10 @@ def load(path: str = LIB_PATH):
     for name, args in NN_SIGNATURES.items():
         fn = getattr(L, name)
         fn.restype = C.c_int
+        fn.argtypes = args
+    for name, (res, args) in PROC_SIGNATURES.items():
+        fn = getattr(L, name)
+        fn.restype = res
         fn.argtypes = args
     _lib = L
     return L

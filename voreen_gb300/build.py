@@ -37,6 +37,7 @@ SOURCES = [
     ("ingest.cpp", []),
     ("noalloc.cu", []),
     ("batch.cpp", []),
+    ("processor.cpp", []),
     ("nn.cu", []),
     ("nn_tc.cu", []),
     ("synth_tubes.cu", []),

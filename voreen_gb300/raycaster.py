@@ -1,5 +1,8 @@
-"""Processor-shaped host interface mirroring Voreen's CPURaycaster /
-SingleVolumeRaycaster surface over the C ABI.
+"""Python binding of the CudaRaycaster processor (include/vrc_processor.h,
+csrc/processor.cpp): Voreen's CPURaycaster / SingleVolumeRaycaster surface,
+implemented in C++ over the C ABI. Attributes map to the processor's
+properties by id, as Voreen's Python bindings do; ports hold numpy data that
+the processor borrows for the duration of process().
 
 Port names, property names, defaults and error behaviour follow the
 reference so tests read like its processor code:
@@ -55,23 +58,24 @@ reference so tests read like its processor code:
 """
 from __future__ import annotations
 
+import ctypes as C
 import logging
 from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import (CLASSIFY_PREINTEGRATED, CLASSIFY_TF, DVR, EE_ANALYTIC, EE_BUFFERS, FHN, FHP, ISO, MIDA, MIP, MOP,
-               OUT_RGBA32F, PLACE_DEVICE, PLACE_HOST, SHADE_NONE, SHADE_PHONG, Context, PreIntegrationTable,
-               TransferFunction, Volume, VrcError,
-               default_params, image_rescale, make_camera, render, sampling_step)
+from . import _abi, lib, make_camera, make_desc
+from ._abi import F32, U8, U16, Camera, RenderStats, TFKey
 
 log = logging.getLogger("voreen.CudaRaycaster")
 
-COMPOSITING = {"dvr": DVR, "mip": MIP, "iso": ISO, "mop": MOP, "mida": MIDA, "fhp": FHP, "fhn": FHN}
-CLASSIFICATION = ("transfer-function", "pre-integrated-gpu", "pre-integrated-cpu", "pre-integrated-approximation")
-PREINT_TABLE_SIZES = (0, 256, 512, 1024)
-SHADING = {"none": SHADE_NONE, "phong": SHADE_PHONG}
-PLACEMENT = {"device": PLACE_DEVICE, "host": PLACE_HOST}
+# property id -> kind, as include/vrc_processor.h lists them
+_FLOAT = ("samplingRate", "isoValue", "gammaValue", "interactionQuality", "materialShininess")
+_INT = ("preIntegrationTableSize", "interactionCoarseness", "brickBufferSizeMB", "brickUploadBudgetMB")
+_BOOL = ("enableClipping", "applyLightAttenuation", "useLevelOfDetail", "useIterativeRefinement")
+_STRING = ("compositing", "shading", "gradient", "classification", "brickPoolPlacement")
+_FLOATV = {"lightPosition": 4, "lightAmbient": 4, "lightDiffuse": 4, "lightSpecular": 4, "lightAttenuation": 3}
+_NP_DTYPE = {np.dtype(np.uint8): U8, np.dtype(np.uint16): U16, np.dtype(np.float32): F32}
 
 
 @dataclass
@@ -112,200 +116,160 @@ class TransFunc1DKeys:
     domain_fitted: bool = False
 
 
+def _id(name: str) -> bytes:
+    return name.encode()
+
+
 class CudaRaycaster:
     className = "CudaRaycaster"
     category = "Raycasting"
 
     def __init__(self, device: int = 0):
-        self.volumeInport = Port("volumehandle.volumehandle")
-        self.entryPort = Port("image.entrypoints")
-        self.exitPort = Port("image.exitpoints")
-        self.outport = Port("image.output")
-        self.samplingRate = 2.0
-        self.isoValue = 0.5
-        self.compositing = "dvr"
-        self.shading = "none"
-        self.gradient = "central-differences"
-        self.classification = "transfer-function"
-        self.preIntegrationTableSize = 0
-        self.gammaValue = 0.0
-        self.interactionCoarseness = 3
-        self.interactionQuality = 1.0
-        # proxy geometry of the analytic entry/exit (OptimizedProxyGeometry
-        # "enableClipping" / "clipRegion": inclusive voxel box (llf, urb))
-        self.enableClipping = False
-        self.clipRegion = None
-        self.transferFunction = TransFunc1DKeys()
-        self.lightPosition = (2.3, 1.5, 1.5, 1.0)
-        self.lightAmbient = (0.4, 0.4, 0.4, 1.0)
-        self.lightDiffuse = (0.8, 0.8, 0.8, 1.0)
-        self.lightSpecular = (0.6, 0.6, 0.6, 1.0)
-        self.materialShininess = 60.0
-        self.applyLightAttenuation = False
-        self.lightAttenuation = (1.0, 0.0, 0.0)
-        self.camera = make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0))
-        self.brickPoolPlacement = "device"
-        self.brickBufferSizeMB = 0
-        self.brickUploadBudgetMB = 32
-        self.useLevelOfDetail = False
-        self.useIterativeRefinement = True
-        self.invalidated = False
-        self.lastError = ""
-        self._device = device
-        self._ctx = None
-        self._vol = None
-        self._vol_src = None
-        self._preint = None       # (key, PreIntegrationTable): the cached table
-        self._vol_placement = None
-        self._last_missed = -1
+        h = C.c_void_p()
+        st = lib().vrcp_create(device, C.byref(h))
+        if st != _abi.VRC_OK:
+            raise RuntimeError(f"vrcp_create: {st}")
+        object.__setattr__(self, "_h", h)
+        object.__setattr__(self, "volumeInport", Port("volumehandle.volumehandle"))
+        object.__setattr__(self, "entryPort", Port("image.entrypoints"))
+        object.__setattr__(self, "exitPort", Port("image.exitpoints"))
+        object.__setattr__(self, "outport", Port("image.output"))
+        object.__setattr__(self, "transferFunction", TransFunc1DKeys())
+        object.__setattr__(self, "camera", make_camera((0.0, 0.0, 3.0), (0.0, 0.0, 0.0)))
+        object.__setattr__(self, "clipRegion", None)
+        object.__setattr__(self, "lastStats", None)
+        object.__setattr__(self, "_vol_src", None)
+        object.__setattr__(self, "_borrowed", ())
+
+    # properties by id ------------------------------------------------------
+    def __getattr__(self, name):
+        L, h = lib(), object.__getattribute__(self, "_h")
+        if name in _FLOAT:
+            v = C.c_float()
+            L.vrcp_get_float(h, _id(name), C.byref(v))
+            return v.value
+        if name in _INT or name in _BOOL:
+            v = C.c_int()
+            L.vrcp_get_int(h, _id(name), C.byref(v))
+            return bool(v.value) if name in _BOOL else v.value
+        if name in _STRING:
+            buf = C.create_string_buffer(256)
+            L.vrcp_get_string(h, _id(name), buf, 256)
+            return buf.value.decode()
+        if name in _FLOATV:
+            n = _FLOATV[name]
+            v = (C.c_float * n)()
+            L.vrcp_get_floatv(h, _id(name), v, n)
+            return tuple(float(x) for x in v)
+        if name == "lastError":
+            return (L.vrcp_last_error(h) or b"").decode()
+        if name == "invalidated":
+            return bool(L.vrcp_invalidated(h))
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        L, h = lib(), self._h
+        if name in _FLOAT:
+            L.vrcp_set_float(h, _id(name), float(value))
+        elif name in _INT or name in _BOOL:
+            L.vrcp_set_int(h, _id(name), int(value))
+        elif name in _STRING:
+            L.vrcp_set_string(h, _id(name), str(value).encode())
+        elif name in _FLOATV:
+            n = _FLOATV[name]
+            v = [float(x) for x in value][:n]
+            v += [1.0] * (n - len(v))
+            L.vrcp_set_floatv(h, _id(name), (C.c_float * n)(*v), n)
+        else:
+            object.__setattr__(self, name, value)
 
     # Processor lifecycle ---------------------------------------------------
     def initialize(self):
-        self._ctx = Context(self._device)
+        lib().vrcp_initialize(self._h)
 
     def deinitialize(self):
-        if self._preint is not None:
-            self._preint[1].close()
-        self._preint = None
-        if self._vol is not None:
-            self._vol.close()
-        self._vol = None
-        if self._ctx is not None:
-            self._ctx.close()
-        self._ctx = None
+        lib().vrcp_deinitialize(self._h)
+
+    def close(self):
+        if self._h:
+            lib().vrcp_destroy(self._h)
+            object.__setattr__(self, "_h", C.c_void_p())
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
     def isReady(self) -> bool:
         """volume + entry/exit ports, as CPURaycaster::isReady (cpuraycaster.cpp:82-84)."""
         return self.volumeInport.hasData() and self.entryPort.isConnected() and self.exitPort.isConnected()
 
-    def _error(self, msg: str):
-        self.lastError = msg
-        log.error(msg)
-
-    def _fit_tf(self, vol: Volume):
-        tf = self.transferFunction
-        tf.width = TransferFunction.table_width(vol.dtype)
-        if not tf.domain_fitted and tf.domain == (0.0, 1.0):
-            lo, hi = vol.minmax()
-            s, o = vol.desc.rwm_scale, vol.desc.rwm_offset
-            tf.domain = (lo * s + o, hi * s + o)
-            tf.domain_fitted = True
-
-    def _preint_table(self, step: float) -> PreIntegrationTable:
+    def _push(self):
+        """Hands the port data and the compound properties to the processor."""
+        L, h = lib(), self._h
+        borrowed = []
+        vd = self.volumeInport.getData()
+        if vd is None:
+            if self._vol_src is not None:
+                L.vrcp_set_volume(h, None, None)
+            object.__setattr__(self, "_vol_src", None)
+        elif vd is not self._vol_src:
+            vox = np.ascontiguousarray(vd.voxels)
+            desc = make_desc(_NP_DTYPE[vox.dtype], vox.shape[::-1], vd.spacing, vd.offset, vd.rwm)
+            L.vrcp_set_volume(h, C.byref(desc), vox.ctypes.data_as(C.c_void_p))
+            object.__setattr__(self, "_vol_src", vd)
+            object.__setattr__(self, "_vol_array", vox)
+        e, x = self.entryPort.getData(), self.exitPort.getData()
+        if e is not None and x is not None:
+            e = np.ascontiguousarray(e, dtype=np.float32)
+            x = np.ascontiguousarray(x, dtype=np.float32)
+            borrowed += [e, x]
+            L.vrcp_set_entry_exit(h, e.ctypes.data_as(C.c_void_p), x.ctypes.data_as(C.c_void_p), e.shape[1],
+                                  e.shape[0])
+        else:
+            L.vrcp_set_entry_exit(h, None, None, 0, 0)
+        out = self.outport.getData()
+        if out is not None:
+            L.vrcp_set_output_size(h, out.shape[1], out.shape[0])
         t = self.transferFunction
-        res = PreIntegrationTable.resolution(t.width, self.preIntegrationTableSize)
-        integral = self.classification == "pre-integrated-approximation"
-        key = (step, res, integral, repr(t.keys), t.gamma, tuple(t.threshold))
-        if self._preint is None or self._preint[0] != key:
-            if self._preint is not None:
-                self._preint[1].close()
-            src = PreIntegrationTable.bake_source(t.keys, res, t.gamma, t.threshold)
-            self._preint = (key, PreIntegrationTable(self._ctx, src, step, integral))
-        return self._preint[1]
+        keys = (TFKey * max(1, len(t.keys)))()
+        for i, k in enumerate(t.keys):
+            keys[i].intensity = float(k[0])
+            keys[i].color_l[:] = [int(v) for v in k[1]]
+            keys[i].color_r[:] = [int(v) for v in (k[2] if len(k) > 2 else k[1])]
+        L.vrcp_set_tf_keys(h, keys, len(t.keys), float(t.gamma), float(t.threshold[0]), float(t.threshold[1]))
+        L.vrcp_set_tf_domain(h, float(t.domain[0]), float(t.domain[1]), 1 if t.domain_fitted else 0, int(t.width))
+        cam = self.camera
+        if not isinstance(cam, Camera):
+            cam = make_camera(cam.position, cam.focus)
+        L.vrcp_set_camera(h, C.byref(cam))
+        if self.clipRegion is None:
+            L.vrcp_set_intv(h, b"clipRegion", None, 0)
+        else:
+            v = [int(c) for c in self.clipRegion[0]] + [int(c) for c in self.clipRegion[1]]
+            L.vrcp_set_intv(h, b"clipRegion", (C.c_int * 6)(*v), 6)
+        object.__setattr__(self, "_borrowed", tuple(borrowed))
+
+    def _pull(self):
+        L, h = lib(), self._h
+        w, lo, hi, fitted = C.c_int(), C.c_float(), C.c_float(), C.c_int()
+        L.vrcp_get_tf(h, C.byref(w), C.byref(lo), C.byref(hi), C.byref(fitted))
+        t = self.transferFunction
+        t.width, t.domain, t.domain_fitted = w.value, (lo.value, hi.value), bool(fitted.value)
+        ptr, W, H = C.POINTER(C.c_float)(), C.c_int(), C.c_int()
+        if L.vrcp_output(h, C.byref(ptr), C.byref(W), C.byref(H)):
+            img = np.ctypeslib.as_array(ptr, shape=(H.value, W.value, 4)).copy()
+            self.outport.setData(img)
+            st = RenderStats()
+            L.vrcp_last_stats(h, C.byref(st))
+            object.__setattr__(self, "lastStats", st)
 
     def process(self, analytic_entry_exit: bool = False, interacting: bool = False):
-        if self._ctx is None:
-            self.initialize()
-        if not (self.volumeInport.hasData() and (analytic_entry_exit or self.isReady())):
-            self._error("not ready: volume and entry/exit points are required")
-            return
-        if self.compositing not in COMPOSITING or self.shading not in SHADING:
-            self._error(f"unsupported compositing/shading: {self.compositing}/{self.shading}")
-            return
-        if self.classification not in CLASSIFICATION or self.preIntegrationTableSize not in PREINT_TABLE_SIZES:
-            self._error(f"unsupported classification: {self.classification}/{self.preIntegrationTableSize}")
-            return
-        if self.classification == "pre-integrated-gpu":
-            self._error("CPU raycaster does not support computing the pre-integration table on the GPU. "
-                        "Falling back to CPU.")
-            self.classification = "pre-integrated-cpu"
-            return
-        if not (1 <= int(self.interactionCoarseness) <= 8) or not (0.01 <= self.interactionQuality <= 1.0):
-            self._error(f"interaction settings out of range: {self.interactionCoarseness}/{self.interactionQuality}")
-            return
-        if not (0.01 <= self.samplingRate <= 20.0):
-            self._error(f"samplingRate {self.samplingRate} outside [0.01, 20]")
-            return
-        if self.brickPoolPlacement not in PLACEMENT or not (0 <= self.brickBufferSizeMB) or \
-                not (1 <= self.brickUploadBudgetMB <= 1024):
-            self._error(f"brick settings out of range: {self.brickPoolPlacement}/{self.brickBufferSizeMB}/"
-                        f"{self.brickUploadBudgetMB}")
-            return
-        vd: VolumeData = self.volumeInport.getData()
-        self.invalidated = False
-        try:
-            placement = PLACEMENT[self.brickPoolPlacement]
-            if self._vol is None or self._vol_src is not vd or self._vol_placement != placement:
-                if self._vol is not None:
-                    self._vol.close()
-                self._vol = Volume(self._ctx, vd.voxels, vd.spacing, vd.offset, vd.rwm, placement=placement)
-                self._vol_src = vd
-                self._vol_placement = placement
-            if placement == PLACE_HOST:
-                mb = 1 << 20
-                self._vol.set_cache_limit(int(self.brickBufferSizeMB) * mb if self.brickBufferSizeMB else 2**62)
-                self._vol.set_cache_upload_budget(int(self.brickUploadBudgetMB) * mb)
-                self._vol.set_lod(bool(self.useLevelOfDetail))
-            self._fit_tf(self._vol)
-            t = self.transferFunction
-            rgba = TransferFunction.bake(t.keys, t.width, t.gamma, t.threshold)
-            tf = TransferFunction(self._ctx, rgba, t.domain)
-            if analytic_entry_exit:
-                H, W = self.outport.getData().shape[:2] if self.outport.hasData() else (512, 512)
-                entry = exit_pts = None
-            else:
-                entry, exit_pts = self.entryPort.getData(), self.exitPort.getData()
-                H, W = entry.shape[:2]
-            p = default_params(W, H)
-            p.sampling_rate = self.samplingRate
-            p.compositing = COMPOSITING[self.compositing]
-            p.shading = SHADING[self.shading]
-            p.iso_value = self.isoValue
-            p.mida_gamma = self.gammaValue
-            if self.classification.startswith("pre-integrated"):
-                p.classification = CLASSIFY_PREINTEGRATED
-                tf.set_preintegration(self._preint_table(sampling_step(self._vol, self.samplingRate)))
-            p.light_position[:] = list(self.lightPosition)
-            p.light_ambient[:] = list(self.lightAmbient)[:3]
-            p.light_diffuse[:] = list(self.lightDiffuse)[:3]
-            p.light_specular[:] = list(self.lightSpecular)[:3]
-            p.material_shininess = self.materialShininess
-            p.apply_attenuation = 1 if self.applyLightAttenuation else 0
-            p.light_attenuation[:] = list(self.lightAttenuation)
-            p.camera = self.camera
-            p.entry_exit_mode = EE_ANALYTIC if analytic_entry_exit else EE_BUFFERS
-            if self.enableClipping and self.clipRegion is not None:
-                p.enable_clipping = 1
-                p.clip_llf[:] = [int(c) for c in self.clipRegion[0]]
-                p.clip_urb[:] = [int(c) for c in self.clipRegion[1]]
-            coarse = interacting and int(self.interactionCoarseness) > 1
-            if interacting:
-                p.sampling_rate = self.samplingRate * self.interactionQuality
-            if coarse:
-                import torch
-                c = int(self.interactionCoarseness)
-                p.width, p.height = max(1, W // c), max(1, H // c)
-                p.entry_exit_mode = EE_ANALYTIC
-                small = torch.empty((p.height, p.width, 4), dtype=torch.float32, device=f"cuda:{self._device}")
-                _, stats = render(self._ctx, self._vol, tf, p, None, None, OUT_RGBA32F, small)
-                full = torch.empty((H, W, 4), dtype=torch.float32, device=f"cuda:{self._device}")
-                image_rescale(self._ctx, small, full, OUT_RGBA32F)
-                self._ctx.synchronize()
-                img = full.cpu().numpy()
-            else:
-                img, stats = render(self._ctx, self._vol, tf, p, entry, exit_pts, OUT_RGBA32F)
-            tf.close()
-            self.outport.setData(img)
-            self.lastStats = stats
-            if placement == PLACE_HOST and self.useIterativeRefinement:
-                # another frame helps while the cache is still filling, or
-                # while the bricks read without a slot keep changing; a frame
-                # that can bring in nothing new ends the refinement
-                cached, reachable, missed = self._vol.cache_info()
-                nb = int(np.prod(self._vol.brick_minmax()[2]))
-                capacity = (int(self.brickBufferSizeMB) << 20) // max(1, self._vol.host_bytes // nb) \
-                    if self.brickBufferSizeMB else reachable
-                self.invalidated = cached < min(reachable, capacity) or (missed > 0 and missed != self._last_missed)
-                self._last_missed = missed
-        except VrcError as e:
-            self._error(str(e))
+        self._push()
+        lib().vrcp_process(self._h, 1 if analytic_entry_exit else 0, 1 if interacting else 0)
+        self._pull()
+        object.__setattr__(self, "_borrowed", ())
+        err = self.lastError
+        if err:
+            log.error(err)
