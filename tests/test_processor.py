@@ -174,3 +174,40 @@ def test_properties_by_id_through_the_c_shim(vrc_lib):
     r.process(analytic_entry_exit=True)
     assert "samplingRate" in r.lastError and not r.outport.hasData()
     r.close()
+
+
+@pytest.mark.gpu
+def test_preintegrated_interaction_frame(ctx):
+    """Interaction mode with interactionQuality 0.5 marches at half the rate,
+    so the pre-integration table is built for that step: the coarse frame
+    equals a direct render with a table built for it, rescaled."""
+    import oracle
+    w = synth.config1(size=(48, 40, 44), image=(80, 64))
+    r = CudaRaycaster()
+    r.volumeInport.setData(VolumeData(w.voxels, w.spacing))
+    r.transferFunction.keys = w.tf_keys
+    r.classification = "pre-integrated-cpu"
+    r.camera = w.params().camera
+    r.outport.setData(np.zeros((64, 80, 4), np.float32))
+    r.interactionCoarseness = 2
+    r.interactionQuality = 0.5
+    r.process(analytic_entry_exit=True, interacting=True)
+    assert r.lastError == ""
+    img = r.outport.getData()
+    lo, hi = r.transferFunction.domain
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    step = v.sampling_step(vol, 1.0)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, 256), (lo, hi))
+    table = v.PreIntegrationTable(ctx, oracle.preint_source(w.tf_keys, 256), step)
+    tf.set_preintegration(table)
+    q = w.params(entry_exit_mode=v.EE_ANALYTIC)
+    q.width, q.height, q.sampling_rate, q.classification = 40, 32, 1.0, v.CLASSIFY_PREINTEGRATED
+    torch = pytest.importorskip("torch")
+    small = torch.empty((32, 40, 4), dtype=torch.float32, device="cuda:0")
+    full = torch.empty((64, 80, 4), dtype=torch.float32, device="cuda:0")
+    v.render(ctx, vol, tf, q, None, None, v.OUT_RGBA32F, small)
+    v.image_rescale(ctx, small, full, v.OUT_RGBA32F)
+    ctx.synchronize()
+    np.testing.assert_array_equal(img, full.cpu().numpy())
+    assert (img[..., 3] > 0).mean() > 0.05
+    r.deinitialize()

@@ -385,12 +385,17 @@ struct vrcp_processor {
 namespace {
 
 float* floatv(CudaRaycaster& r, const std::string& id, int* n) {
-    if (id == "lightPosition") return *n = 4, r.lightPosition;
-    if (id == "lightAmbient") return *n = 4, r.lightAmbient;
-    if (id == "lightDiffuse") return *n = 4, r.lightDiffuse;
-    if (id == "lightSpecular") return *n = 4, r.lightSpecular;
-    if (id == "lightAttenuation") return *n = 3, r.lightAttenuation;
-    return nullptr;
+    float* v = nullptr;
+    *n = 4;
+    if (id == "lightPosition") v = r.lightPosition;
+    else if (id == "lightAmbient") v = r.lightAmbient;
+    else if (id == "lightDiffuse") v = r.lightDiffuse;
+    else if (id == "lightSpecular") v = r.lightSpecular;
+    else if (id == "lightAttenuation") {
+        v = r.lightAttenuation;
+        *n = 3;
+    }
+    return v;
 }
 float* floatp(CudaRaycaster& r, const std::string& id) {
     if (id == "samplingRate") return &r.samplingRate;
