@@ -45,9 +45,16 @@ def _barrier_max(value: float, ws: int):
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device="cuda" if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _whole_job(ms_local: float, ws: int):
+    """Replicas: the slowest rank's time per step, and the frames/s of all
+    ranks together (each rank renders its own frame per step)."""
+    ms = _barrier_max(ms_local, ws)
+    return ms, 1000.0 / ms * ws
 
 
 def _barrier(ws: int):
@@ -839,9 +846,7 @@ def main():
         ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
     else:
         ms = start.elapsed_time(end) / args.steps
-    ms = _barrier_max(ms, ws)
-    fps_local = 1000.0 / ms
-    value = fps_local * ws
+    ms, value = _whole_job(ms, ws)
 
     # e2e: host entry/exit in, host RGBA8 frame out, through the C ABI
     e_pin = torch.from_numpy(e_host).pin_memory().numpy()
