@@ -801,11 +801,11 @@ def main():
     # per-frame stats (sample counts, kernel time) from untimed frames
     _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
     samples, shaded = st.samples, st.samples_shaded
-    launches_per_frame = st.kernel_launches
     kernel_ms = []
     for _ in range(3):
         _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA8, out_dev)
         kernel_ms.append(st.kernel_ms)
+    launches_per_frame = st.kernel_launches  # steady state: the occupancy bits are reused across frames
 
     if args.profile:
         for _ in range(args.steps):

@@ -101,6 +101,8 @@ typedef struct vrc_tf vrc_tf;
 
 /* ---- context ---------------------------------------------------------- */
 vrc_status vrc_context_create(int device, vrc_context** out);
+/* Destroy the context's volumes, TFs, pre-integration tables and batches
+ * first: they keep a pointer to it. */
 vrc_status vrc_context_destroy(vrc_context* ctx);
 vrc_status vrc_context_synchronize(vrc_context* ctx);
 /* The context's cudaStream_t, for callers that order their own work with it. */

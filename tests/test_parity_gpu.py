@@ -350,3 +350,45 @@ def test_pinned_host_buffers_in_place(ctx):
                 img, st = v.render(ctx, vol, tf, p, ee[0], ee[1], fmt, o)
                 np.testing.assert_array_equal(img, ref)
                 assert st.samples == sr.samples
+
+
+@pytest.mark.gpu
+def test_occupancy_reused_across_frames(ctx):
+    """The empty-space occupancy bits are computed once per (volume, TF,
+    cell edge) and reused by later frames; switching TFs, volumes or cell
+    edges recomputes them, and every image equals a fresh context's."""
+    w = synth.config2(size=(80, 72, 64), image=(120, 90))
+    keys2 = [(0.0, (0, 0, 0, 0)), (0.5, (0, 0, 0, 0)), (0.7, (250, 200, 90, 160)), (1.0, (255, 255, 255, 255))]
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tfa = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    tfb = v.TransferFunction(ctx, v.TransferFunction.bake(keys2, w.tf_width), w.domain)
+    p = w.params(entry_exit_mode=v.EE_ANALYTIC, shading=v.SHADE_PHONG)
+
+    def fresh(keys, cell=0):
+        c2 = v.Context(0)
+        vol2 = v.Volume(c2, w.voxels, w.spacing)
+        tf2 = v.TransferFunction(c2, v.TransferFunction.bake(keys, w.tf_width), w.domain)
+        q = w.params(entry_exit_mode=v.EE_ANALYTIC, shading=v.SHADE_PHONG, skip_cell_size=cell)
+        img, _ = v.render(c2, vol2, tf2, q, None, None, v.OUT_RGBA32F)
+        tf2.close()  # a context's objects go before the context
+        vol2.close()
+        c2.close()
+        return img
+
+    ref_a, ref_b = fresh(w.tf_keys), fresh(keys2)
+    img, st = v.render(ctx, vol, tfa, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 3 and np.array_equal(_bits(img), _bits(ref_a))
+    img, st = v.render(ctx, vol, tfa, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 1 and np.array_equal(_bits(img), _bits(ref_a))
+    img, st = v.render(ctx, vol, tfb, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 3 and np.array_equal(_bits(img), _bits(ref_b))
+    img, st = v.render(ctx, vol, tfa, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 3 and np.array_equal(_bits(img), _bits(ref_a))
+    p.skip_cell_size = 16
+    img, st = v.render(ctx, vol, tfa, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 3 and np.array_equal(_bits(img), _bits(fresh(w.tf_keys, 16)))
+    # a TF destroyed and re-created (possibly at the same address) is a new TF
+    tfa.close()
+    tfc = v.TransferFunction(ctx, v.TransferFunction.bake(keys2, w.tf_width), w.domain)
+    img, st = v.render(ctx, vol, tfc, p, None, None, v.OUT_RGBA32F)
+    assert st.kernel_launches == 3

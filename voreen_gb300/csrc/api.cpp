@@ -1035,6 +1035,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     const float kcorr = P.step * 200.f;  // SAMPLING_BASE_INTERVAL_RCP
     const int* occ_prefix = tf->d_prefix;
     int occ_width = tf->width;
+    uint64_t occ_source = tf->uid;
     if (p->classification == VRC_CLASSIFY_PREINTEGRATED) {
         const vrc_preint* pi = tf->preint;
         if (!pi) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: no pre-integration table attached to the TF");
@@ -1050,6 +1051,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         P.tf_width = 0;  // the TF table is not read
         occ_prefix = pi->d_prefix;
         occ_width = pi->res;
+        occ_source = pi->uid;
     } else {
         float4* table = nullptr;
         if ((st = tf_table(ctx, tf, vrc::alpha_corrected(p->compositing, p->classification), kcorr, &table)) !=
@@ -1112,6 +1114,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         const float msp = std::min(vol->desc.spacing[0], std::min(vol->desc.spacing[1], vol->desc.spacing[2]));
         P.aux_gscale = msp / dom;
     }
+    int occ_launches = 0;
     if (p->empty_space_skipping) {
         // skip cells: the requested edge if the volume holds that level, else the brick
         const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
@@ -1127,9 +1130,26 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
                 for (int i = 0; i < 3; ++i) nc[i] = lv.nc[i];
             }
         const long long n = (long long)nc[0] * nc[1] * nc[2];
+        // the occupancy bits are a function of the volume's min/max tables,
+        // the TF (or table) and the cell edge: reuse them while those stay
+        uint32_t lo_bits, hi_bits;
+        std::memcpy(&lo_bits, &tf->lo, 4);
+        std::memcpy(&hi_bits, &tf->hi, 4);
+        const uint64_t key[6] = {vol->uid, occ_source, (uint64_t)occ_width, lo_bits, hi_bits, (uint64_t)C};
+        const uint32_t* occ_before = ctx->d_occ;
+        const uint32_t* coarse_before = ctx->d_occ_coarse;
         VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, vrc::occupancy_bytes(n)));
-        VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, occ_prefix, occ_width, vol->desc.rwm_scale,
-                                            vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
+        if (C < vol->L.B)
+            VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes,
+                                 vrc::occupancy_bytes(vol->L.nbricks())));
+        const bool cached = std::memcmp(key, ctx->occ_key, sizeof(key)) == 0 && ctx->d_occ == occ_before &&
+                            (C >= vol->L.B || ctx->d_occ_coarse == coarse_before);
+        if (!cached) {
+            std::memset(ctx->occ_key, 0, sizeof(ctx->occ_key));
+            VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, occ_prefix, occ_width, vol->desc.rwm_scale,
+                                                vol->desc.rwm_offset, tf->lo, tf->hi, ctx->d_occ, s));
+            ++occ_launches;
+        }
         P.occupancy = ctx->d_occ;
         P.cshift = ilog2(C);
         for (int i = 0; i < 3; ++i) P.nc[i] = nc[i];
@@ -1138,14 +1158,17 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         if (C < vol->L.B) {
             // coarse level: whole bricks, tested first
             const long long nb = vol->L.nbricks();
-            VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes, vrc::occupancy_bytes(nb)));
-            VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width,
-                                                vol->desc.rwm_scale, vol->desc.rwm_offset, tf->lo, tf->hi,
-                                                ctx->d_occ_coarse, s));
+            if (!cached) {
+                VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width,
+                                                    vol->desc.rwm_scale, vol->desc.rwm_offset, tf->lo, tf->hi,
+                                                    ctx->d_occ_coarse, s));
+                ++occ_launches;
+            }
             P.occ_coarse = ctx->d_occ_coarse;
             P.cshift_coarse = vol->L.shift;
             for (int i = 0; i < 3; ++i) P.ncc[i] = vol->L.nb[i];
         }
+        std::memcpy(ctx->occ_key, key, sizeof(key));
     }
     if (vol->h_bricks && (vol->cache_limit > 0 || vol->lod_on)) {
         if ((st = prepare_brick_cache(ctx, const_cast<vrc_volume*>(vol), occ_prefix, occ_width, tf, P, s)) != VRC_OK)
@@ -1169,7 +1192,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         stats->samples_shaded = double(h[2]);
         stats->skip_runs = double(h[3]);
         stats->device_status = int(h[4] & 0xffffffffu);
-        stats->kernel_launches = 1 + (P.occupancy ? 1 : 0) + (P.occ_coarse ? 1 : 0);
+        stats->kernel_launches = 1 + occ_launches;
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->kernel_ms, ctx->ev[1], ctx->ev[2]));
         VRC_CUDA(ctx, cudaEventElapsedTime(&stats->total_ms, ctx->ev[0], ctx->ev[3]));
         if (stats->device_status != 0) return fail(ctx, VRC_ERR_DEVICE, "vrc_render: kernel reported an error status");

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <utility>
@@ -160,6 +161,13 @@ cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nce
                              uint32_t* occ, cudaStream_t s);
 inline size_t occupancy_bytes(long long ncells) { return (size_t)((ncells + 31) / 32) * 4; }
 
+// Process-unique id of a volume, TF or pre-integration table: identifies
+// the derived data cached for it even when an address is reused later.
+inline uint64_t next_uid() {
+    static std::atomic<uint64_t> n{1};
+    return n.fetch_add(1);
+}
+
 }  // namespace vrc
 
 // Opaque handle definitions.
@@ -181,6 +189,9 @@ struct vrc_context {
     int* d_prefix = nullptr;
     size_t prefix_bytes = 0;
     unsigned long long* d_counters = nullptr;  // 4 counters + status + tile counter
+    // what d_occ / d_occ_coarse hold: (volume uid, TF or table uid, table
+    // width, domain lo/hi bits, skip cell edge); both are pure functions of it
+    uint64_t occ_key[6] = {0, 0, 0, 0, 0, 0};
 };
 
 struct vrc_cell_level {
@@ -193,6 +204,7 @@ struct vrc_cell_level {
 
 struct vrc_volume {
     vrc_context* ctx = nullptr;
+    uint64_t uid = vrc::next_uid();
     vrc_volume_desc desc{};
     vrc::BrickLayout L{};
     void* d_bricks = nullptr;     // device address of the brick pool
@@ -238,6 +250,7 @@ struct vrc_volume {
 
 struct vrc_tf {
     vrc_context* ctx = nullptr;
+    uint64_t uid = vrc::next_uid();
     int width = 0;
     float lo = 0.f, hi = 1.f;
     uint8_t* h_rgba = nullptr;
@@ -249,6 +262,7 @@ struct vrc_tf {
 
 struct vrc_preint {
     vrc_context* ctx = nullptr;
+    uint64_t uid = vrc::next_uid();
     int res = 0;
     float step = 0.f;
     int use_integral = 0;
