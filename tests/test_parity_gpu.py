@@ -392,3 +392,26 @@ def test_occupancy_reused_across_frames(ctx):
     tfc = v.TransferFunction(ctx, v.TransferFunction.bake(keys2, w.tf_width), w.domain)
     img, st = v.render(ctx, vol, tfc, p, None, None, v.OUT_RGBA32F)
     assert st.kernel_launches == 3
+
+
+@pytest.mark.parametrize("skipping", [1, 0])
+def test_loop_cap(ctx, skipping):
+    """cpuraycaster.cpp:239: a ray stops after 255 * 255 loop iterations. At
+    rate 3000 on a 32^3 volume (step 1/96000) the rays need ~1e5 samples;
+    the cap, also inside closed-form jumps over empty cells, matches the
+    oracle bit for bit."""
+    rng = np.random.default_rng(11)
+    vox = rng.integers(0, 256, size=(32, 32, 32), dtype=np.uint8)
+    vox[:, :, :16] //= 4  # an empty half under the TF below
+    tf = v.TransferFunction.bake([(0.0, (0, 0, 0, 0)), (0.3, (0, 0, 0, 0)), (0.31, (200, 90, 40, 1)),
+                                  (1.0, (40, 90, 200, 2))], 256)
+    p = v.default_params(6, 4)
+    p.sampling_rate = 3000.0
+    p.empty_space_skipping = skipping
+    p.camera = v.make_camera((60.0, 40.0, 70.0), (16.0, 16.0, 16.0), near=1.0, far=300.0, fovy=12.0)
+    c = Case(ctx, vox, tf, (0.0, 1.0), p)
+    img, st = c.gpu()
+    o32, s32, _ = c.oracle(32)
+    assert s32.max() == 255 * 255  # some rays reach the cap
+    np.testing.assert_array_equal(_bits(img), _bits(o32))
+    assert st.samples == s32.sum()
