@@ -530,9 +530,12 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
         float skip_lim = 0.f;
         if (P.occupancy) {
             // Two skip levels: a whole empty brick-sized cell first, else an
-            // empty fine cell (8^3 by default).
+            // empty fine cell (8^3 by default); both words are loaded at once.
             float tsafe = 0.f;
             bool empty = false;
+            const int fcx = ix >> P.cshift, fcy = iy >> P.cshift, fcz = iz >> P.cshift;
+            const long long fc = ((long long)fcz * P.nc[1] + fcy) * P.nc[0] + fcx;
+            const uint32_t fine_word = __ldg(P.occupancy + (fc >> 5));
             if (P.occ_coarse) {
                 const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
                 const long long c = ((long long)cz * P.ncc[1] + cy) * P.ncc[0] + cx;
@@ -541,13 +544,9 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     empty = true;
                 }
             }
-            if (!empty) {
-                const int cx = ix >> P.cshift, cy = iy >> P.cshift, cz = iz >> P.cshift;
-                const long long c = ((long long)cz * P.nc[1] + cy) * P.nc[0] + cx;
-                if (((__ldg(P.occupancy + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
-                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift, P.nc);
-                    empty = true;
-                }
+            if (!empty && ((fine_word >> (fc & 31)) & 1u) == 0u) {
+                tsafe = cell_exit_t(P, f, dx, dy, dz, fcx, fcy, fcz, P.cshift, P.nc);
+                empty = true;
             }
             if (PI && empty && P.pi_chain && prev_empty) {
                 // This sample and the previous one lie in empty cells that
