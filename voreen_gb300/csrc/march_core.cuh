@@ -653,12 +653,33 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                         const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
                         const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
                         const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float v0 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
-                        const float v1 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
-                        const float v2 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
-                        const float v3 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
-                        const float v4 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
-                        const float v5 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
+                        // The taps lie at or beyond the sample on their axis, so
+                        // the "+" taps can only leave the apron upward and the
+                        // "-" taps downward. When all six stay inside (away from
+                        // the volume's faces, always), they are read in one
+                        // straight block whose 48 loads are in flight together.
+                        const float fxp = floorf(vxp), fyp = floorf(vyp), fzp = floorf(vzp);
+                        const float fxm = floorf(vxm), fym = floorf(vym), fzm = floorf(vzm);
+                        const int dxp = (int)fxp - ix, dyp = (int)fyp - iy, dzp = (int)fzp - iz;
+                        const int dxm = (int)fxm - ix, dym = (int)fym - iy, dzm = (int)fzm - iz;
+                        const int top = L.B + 1;
+                        float v0, v1, v2, v3, v4, v5;
+                        if ((!POOL || b) && lx + dxp <= top && ly + dyp <= top && lz + dzp <= top && lx + dxm >= 0 &&
+                            ly + dym >= 0 && lz + dzm >= 0) {
+                            v0 = tri_raw<DT>(b, o + dxp, S, S2, vxp - fxp, fy, fz);
+                            v1 = tri_raw<DT>(b, o + dyp * S, S, S2, fx, vyp - fyp, fz);
+                            v2 = tri_raw<DT>(b, o + dzp * S2, S, S2, fx, fy, vzp - fzp);
+                            v3 = tri_raw<DT>(b, o + dxm, S, S2, vxm - fxm, fy, fz);
+                            v4 = tri_raw<DT>(b, o + dym * S, S, S2, fx, vym - fym, fz);
+                            v5 = tri_raw<DT>(b, o + dzm * S2, S, S2, fx, fy, vzm - fzm);
+                        } else {
+                            v0 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
+                            v1 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
+                            v2 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
+                            v3 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
+                            v4 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
+                            v5 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
+                        }
                         g = F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
                     }
                     const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
