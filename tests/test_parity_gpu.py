@@ -415,3 +415,42 @@ def test_loop_cap(ctx, skipping):
     assert s32.max() == 255 * 255  # some rays reach the cap
     np.testing.assert_array_equal(_bits(img), _bits(o32))
     assert st.samples == s32.sum()
+
+
+@pytest.mark.parametrize("kind", ["u16_shells", "f32_signed", "u8_plateaus", "f32_negative_scale"])
+def test_mip_cell_skipping_is_exact(ctx, kind):
+    """MIP skips cells whose largest value cannot raise the ray's maximum: the
+    image and the sample count equal the render without skipping and the
+    FP32 oracle bit for bit, including negative values, a negative
+    real-world offset, plateaus (samples equal to the cell maximum) and a
+    negative scale (where that skipping is off)."""
+    rng = np.random.default_rng(21)
+    rwm = (1.0, 0.0)
+    if kind == "u16_shells":
+        w = synth.config2(size=(96, 80, 72), image=(160, 120), compositing=v.MIP)
+        vox, keys, dom, spacing = w.voxels, w.tf_keys, w.domain, w.spacing
+    else:
+        spacing = (1.0, 1.0, 1.0)
+        if kind == "u8_plateaus":
+            vox = (rng.integers(0, 6, size=(40, 48, 56)) * 40).astype(np.uint8)  # few distinct levels
+            dom = (0.0, 1.0)
+        else:
+            vox = rng.normal(0.0, 1.0, size=(40, 48, 56)).astype(np.float32)
+            rwm = (2.0, -0.5) if kind == "f32_signed" else (-1.5, 0.25)
+            dom = (-3.0, 3.0)
+        keys = [(0.0, (0, 0, 255, 0)), (0.4, (0, 255, 0, 30)), (1.0, (255, 0, 0, 200))]
+    tf = v.TransferFunction.bake(keys, 256 if vox.dtype == np.uint8 else 4096)
+    p = v.default_params(120, 90)
+    X, Y, Z = vox.shape[2], vox.shape[1], vox.shape[0]
+    d = float(np.sqrt(X * X + Y * Y + Z * Z))
+    p.camera = v.make_camera((X * 0.5 + 0.9 * d, Y * 0.5 + 0.5 * d, Z * 0.5 + 1.1 * d), (X / 2, Y / 2, Z / 2),
+                             near=0.1, far=10 * d)
+    p.compositing = v.MIP
+    c = Case(ctx, vox, tf, dom, p, spacing, rwm=rwm)
+    a, sa = c.gpu(empty_space_skipping=1)
+    b, sb = c.gpu(empty_space_skipping=0)
+    np.testing.assert_array_equal(_bits(a), _bits(b))
+    assert sa.samples == sb.samples
+    o32, s32, _ = c.oracle(32)
+    np.testing.assert_array_equal(_bits(a), _bits(o32))
+    assert (a[..., 3] > 0).mean() > 0.02

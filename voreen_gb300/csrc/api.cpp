@@ -1151,6 +1151,13 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             ++occ_launches;
         }
         P.occupancy = ctx->d_occ;
+        // MIP: cells that cannot raise a ray's maximum are skipped too; that
+        // needs a monotone real-world mapping
+        if (p->compositing == VRC_MIP && vol->desc.rwm_scale >= 0.f) {
+            P.mip_skip = 1;
+            P.cell_max = cmax;
+            P.brick_max = vol->d_bmax;
+        }
         P.cshift = ilog2(C);
         for (int i = 0; i < 3; ++i) P.nc[i] = nc[i];
         const int maxdim = std::max(vol->desc.dims[0], std::max(vol->desc.dims[1], vol->desc.dims[2]));

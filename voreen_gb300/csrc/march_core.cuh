@@ -373,6 +373,18 @@ struct Counters {
     unsigned long long samples = 0, fetched = 0, shaded = 0, runs = 0;
 };
 
+// MIP: true when no sample of a cell whose largest normalised value is `m`
+// can exceed the ray's maximum real-world intensity `max_int`, so the cell
+// changes nothing (compositeMIP replaces the result only for a larger value).
+// A trilinear sample exceeds its largest voxel by at most ~13 ulp of rounding
+// (three products, seven sums, weights summing to at most (1 + u)^3); m is
+// raised by 2e-6 relative, well above that, and the real-world mapping is
+// monotone (scale >= 0, checked on the host), so the test is exact.
+__device__ __forceinline__ bool mip_cell_below(const MarchParams& P, float m, float max_int) {
+    const float mb = m + fabsf(m) * 2e-6f;
+    return a_(m_(mb, P.rwm_scale), P.rwm_offset) <= max_int;
+}
+
 // Largest ray parameter up to which every sample's floor voxel stays in skip
 // cell (cx, cy, cz): per axis, where the unclamped voxel coordinate
 // dim * (first + t * dir) - 0.5 reaches the cell face it moves toward, pulled
@@ -536,15 +548,20 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             const int fcx = ix >> P.cshift, fcy = iy >> P.cshift, fcz = iz >> P.cshift;
             const long long fc = ((long long)fcz * P.nc[1] + fcy) * P.nc[0] + fcx;
             const uint32_t fine_word = __ldg(P.occupancy + (fc >> 5));
+            constexpr bool MIPS = COMP == VRC_MIP;
+            const bool mip_skip = MIPS && P.mip_skip;
+            const float fine_max = mip_skip ? __ldg(P.cell_max + fc) : 0.f;
             if (P.occ_coarse) {
                 const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
                 const long long c = ((long long)cz * P.ncc[1] + cy) * P.ncc[0] + cx;
-                if (((__ldg(P.occ_coarse + (c >> 5)) >> (c & 31)) & 1u) == 0u) {
+                const uint32_t coarse_word = __ldg(P.occ_coarse + (c >> 5));
+                const float coarse_max = mip_skip ? __ldg(P.brick_max + c) : 0.f;
+                if (((coarse_word >> (c & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, coarse_max, max_int))) {
                     tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift_coarse, P.ncc);
                     empty = true;
                 }
             }
-            if (!empty && ((fine_word >> (fc & 31)) & 1u) == 0u) {
+            if (!empty && (((fine_word >> (fc & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, fine_max, max_int)))) {
                 tsafe = cell_exit_t(P, f, dx, dy, dz, fcx, fcy, fcz, P.cshift, P.nc);
                 empty = true;
             }

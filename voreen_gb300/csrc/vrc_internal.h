@@ -82,6 +82,11 @@ struct MarchParams {
     const float4* pi_table;      // pre-integration table [back * pi_res + front]; nullptr = classify by the TF
     int pi_res;
     int pi_chain;                // a step moves less than 0.99 voxel per axis: empty-to-empty segments skip
+    // MIP: skip cells whose largest value cannot raise the ray's maximum
+    // (max tables of the skip level and of the bricks; mip_skip = 0: off)
+    const float* cell_max;
+    const float* brick_max;
+    int mip_skip;
     const int* brick_slot;       // brick -> slot in `bricks` (a device brick cache) or -1, nullptr = direct
     const void* host_pool;       // mapped host pool read for slot -1 (when lod_bricks is null)
     const void* lod_bricks;      // half-resolution level read for slot -1, nullptr = read the host pool
