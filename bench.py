@@ -122,13 +122,13 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def load_traffic():
-    """Per-launch DRAM bytes of the march kernel from the committed ncu
-    summary (profiles/), scaled per frame; None if absent."""
+def load_traffic(key: str = "dram_bytes_per_launch"):
+    """Per-launch DRAM (or L2) bytes of the march kernel from the committed
+    ncu summary (profiles/); None if absent."""
     p = os.path.join(ROOT, "profiles", "march_dvr_phong_512cube_u16_1080p.json")
     if os.path.exists(p):
         try:
-            return json.load(open(p)).get("dram_bytes_per_launch")
+            return json.load(open(p)).get(key)
         except (OSError, ValueError):
             return None
     return None
@@ -866,6 +866,8 @@ def main():
     peak, peak_kind = measured_peaks()
     achieved = b_alg / (k_ms * 1e-3) / 1e9
     traffic = load_traffic() if (args.workload == "ct" and not args.small) else None
+    l2_peak = v.measure_l2_read(ctx)
+    l2_traffic = load_traffic("l2_bytes_per_launch") if (args.workload == "ct" and not args.small) else None
 
     line = {"metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
             "warmup": warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -880,6 +882,10 @@ def main():
                          "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                          "algorithmic_bytes_per_launch": b_alg,
                          "note": f"algorithmic bytes = {8 * bpv} B/sample + {24 * bpv} B/shaded sample + 4 B/pixel"},
+            "roofline_l2": {"bound": "l2", "achieved": achieved, "peak": l2_peak, "unit": "GB/s",
+                            "frac": achieved / l2_peak if l2_peak > 0 else None,
+                            "peak_kind": "measured in this run: 48 MB L2-resident 16-byte reads (vrc_measure_l2_read)",
+                            "traffic": l2_traffic},
             "e2e": {"value": 1000.0 / e2e_ms * ws, "unit": "frames/s", "h2d_bytes_per_step": 2 * npix * 16,
                     "d2h_bytes_per_step": npix * 4, "kernel_ms": statistics.median(e2e_kms),
                     "note": "pinned host entry/exit read and RGBA8 frame written in place by the march (mapped)"},

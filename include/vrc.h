@@ -334,6 +334,11 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
                       const float* entry, const float* exit_pts, int ee_on_device, void* out, int out_format,
                       int out_on_device, vrc_render_stats* stats);
 
+/* Diagnostics: read bandwidth of an L2-resident buffer of `bytes` (every SM
+ * reading it `reps` times with 16-byte loads), in GB/s: the on-chip peak the
+ * march's gathers are compared with beside the HBM copy peak. */
+vrc_status vrc_measure_l2_read(vrc_context* ctx, size_t bytes, int reps, float* gbs);
+
 /* Bilinear rescale of a device RGBA image (w x h) to W x H on the context
  * stream: VolumeRaycaster::rescaleRendering (GL_LINEAR, clamp to edge) as
  * SingleVolumeRaycaster applies it after an interaction-coarseness render.

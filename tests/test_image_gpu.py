@@ -80,3 +80,12 @@ def test_processor_interaction_coarseness(ctx):
     assert np.abs(img - ref).max() < 2e-6
     assert (img[..., 3] > 0).mean() > 0.05
     r.deinitialize()
+
+
+def test_l2_read_probe(ctx):
+    """The L2 peak the bench divides by: a plausible on-chip bandwidth, above
+    any HBM figure, and errors as statuses."""
+    g = v.measure_l2_read(ctx, 32 << 20, 10)
+    assert 8000.0 < g < 200000.0
+    with pytest.raises(v.VrcError):
+        v.measure_l2_read(ctx, 1024, 1)

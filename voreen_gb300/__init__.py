@@ -370,6 +370,13 @@ def sampling_step(vol: "Volume", sampling_rate: float) -> float:
     return float(lib().vrc_sampling_step(vol.handle, sampling_rate))
 
 
+def measure_l2_read(ctx: Context, nbytes: int = 48 << 20, reps: int = 40) -> float:
+    """L2-resident read bandwidth in GB/s (vrc_measure_l2_read)."""
+    g = C.c_float()
+    _check(lib().vrc_measure_l2_read(ctx.handle, int(nbytes), int(reps), C.byref(g)), ctx, "vrc_measure_l2_read")
+    return float(g.value)
+
+
 def default_params(width: int, height: int) -> RenderParams:
     p = RenderParams()
     lib().vrc_render_params_default(C.byref(p), width, height)

@@ -34,6 +34,7 @@ SOURCES = [
     ("march_first_hit.cu", ["-fmad=false"]),
     ("preint.cu", ["-fmad=false"]),
     ("image.cu", []),
+    ("diag.cu", []),
     ("ingest.cpp", []),
     ("noalloc.cu", []),
     ("batch.cpp", []),
