@@ -186,3 +186,31 @@ def test_upload_budget_with_lod_converges(ctx):
     img, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
     np.testing.assert_array_equal(_bits(img), _bits(ref))
     assert not np.array_equal(_bits(first), _bits(ref))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_cache_settings_are_exact(ctx, seed):
+    """Random cache budgets, upload budgets, brick sizes, modes and TF changes
+    on a host-resident pool: every frame equals the device-resident one."""
+    rng = np.random.default_rng(900 + seed)
+    brick = [16, 32][seed % 2]
+    w = synth.config2(size=(72, 64, 56), image=(96, 72), dist_factor=float(rng.uniform(0.7, 1.4)),
+                      azimuth=float(rng.uniform(0, 360)))
+    host = v.Volume(ctx, w.voxels, w.spacing, placement=v.PLACE_HOST, brick_size=brick)
+    dev = v.Volume(ctx, w.voxels, w.spacing, brick_size=brick)
+    nb = int(np.prod(host.brick_minmax()[2]))
+    bb = host.host_bytes // nb
+    host.set_cache_limit(int(bb * rng.integers(1, nb + 1)))
+    host.set_cache_upload_budget(int(bb * rng.integers(1, 8)) if rng.uniform() < 0.7 else 0)
+    keys2 = [(0.0, (0, 0, 0, 0)), (float(rng.uniform(0.2, 0.6)), (0, 0, 0, 0)), (0.8, (250, 200, 90, 160)),
+             (1.0, (255, 255, 255, 255))]
+    tfs = [v.TransferFunction(ctx, v.TransferFunction.bake(k, w.tf_width), w.domain) for k in (w.tf_keys, keys2)]
+    comp = [v.DVR, v.MIP, v.ISO][int(rng.integers(0, 3))]
+    p = w.params(entry_exit_mode=v.EE_ANALYTIC, compositing=comp,
+                 shading=v.SHADE_PHONG if comp == v.DVR else v.SHADE_NONE)
+    for frame in range(5):
+        tf = tfs[int(rng.integers(0, 2))]
+        a, sa = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+        b, sb = v.render(ctx, dev, tf, p, None, None, v.OUT_RGBA32F)
+        np.testing.assert_array_equal(_bits(a), _bits(b))
+        assert sa.samples == sb.samples
