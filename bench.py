@@ -762,7 +762,9 @@ def main():
         desc = v.make_desc(v.U16, w.dims, w.spacing)
         _, _, inv = v.camera_matrices(p.camera, desc, w.width, w.height)
         e, x = oracle.entry_exit(inv, w.width, w.height)
-        per_step = max(1.0, min(args.cpu_seconds, 150.0 / (warmup + args.steps)))
+        # each step renders a band of centre rows sized so the whole run takes
+        # about 150 s of CPU time (at least 2 rows a step): a bounded sample
+        per_step = min(args.cpu_seconds, max(0.02, 150.0 / (warmup + args.steps)))
         times, rates = [], []
         for i in range(warmup + args.steps):
             dt, rows, samples, threads, lo = run_cpu(w, e, x, per_step / 2 if i < warmup else per_step)
