@@ -211,3 +211,24 @@ def test_preintegrated_interaction_frame(ctx):
     np.testing.assert_array_equal(img, full.cpu().numpy())
     assert (img[..., 3] > 0).mean() > 0.05
     r.deinitialize()
+
+
+@pytest.mark.parametrize("prop,value,msg", [
+    ("compositing", "xray", "unsupported compositing"),
+    ("shading", "toon", "unsupported compositing/shading"),
+    ("classification", "pre-integrated-magic", "unsupported classification"),
+    ("preIntegrationTableSize", 300, "unsupported classification"),
+    ("interactionCoarseness", 9, "interaction settings"),
+    ("interactionQuality", 0.0, "interaction settings"),
+    ("brickUploadBudgetMB", 0, "brick settings"),
+    ("brickBufferSizeMB", -1, "brick settings"),
+])
+def test_process_rejects_bad_settings_without_output(vrc_lib, prop, value, msg):
+    """CPURaycaster::process logs and returns without output on a bad
+    setting (cpuraycaster.cpp:125-146); no device is touched before that."""
+    r = CudaRaycaster()
+    r.volumeInport.setData(VolumeData(np.zeros((4, 4, 4), np.uint16)))
+    setattr(r, prop, value)
+    r.process(analytic_entry_exit=True)
+    assert msg in r.lastError and not r.outport.hasData()
+    r.close()
