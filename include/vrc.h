@@ -11,6 +11,7 @@
  *                       src/core/datastructures/volume/volumegl.cpp:126-168
  *                       (+ brick min/max, optimizedproxygeometry.cpp:894-987)
  *   vrc_vvd_read_header, vrc_volume_load_vvd
+ *   vrc_tf_read_tfi     TransFunc1DKeys::loadTfi (.tfi transfer-function files)
  *                       VvdVolumeReader::read, modules/core/io/vvdvolumereader.cpp,
  *                       modules/core/io/vvdformat.cpp:53-89
  *   vrc_volume_minmax   VolumeMinMax derived data used for TF domain fitting
@@ -232,6 +233,26 @@ int vrc_tf_table_width(int dtype);
 vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float domain_lo, float domain_hi,
                          vrc_tf** out);
 vrc_status vrc_tf_destroy(vrc_tf* tf);
+
+/* Voreen's .tfi transfer-function files (TransFunc1DKeys::loadTfi,
+ * src/core/datastructures/transfunc/1d/1dkeys/transfunc1dkeys.cpp:685-712):
+ * the TransFuncIntensity element's alphaMode, texDimensions, gammaValue,
+ * domain and threshold (TransFuncBase::deserialize, transfuncbase.cpp:222-232;
+ * TransFunc1D::deserialize, transfunc1d.cpp:206-212; the reference's
+ * defaults when absent) and its keys in file order (intensity, split, colorL,
+ * colorR when split: TransFuncMappingKey::deserialize,
+ * transfuncmappingkey.cpp:150-161). Writes at most max_keys keys; info->nkeys
+ * is the number in the file. VRC_ERR_NOT_READY when the file cannot be read,
+ * VRC_ERR_UNSUPPORTED when it holds no TransFuncIntensity. */
+typedef struct {
+    int width;           /* texDimensions x, 0 when absent */
+    int alpha_mode;      /* alphaMode, 1 (use alpha) when absent */
+    float gamma;         /* gammaValue, 1 when absent */
+    float domain[2];     /* domain (real-world), (0, 1) when absent */
+    float threshold[2];  /* threshold (normalised), (0, 1) when absent */
+    int nkeys;
+} vrc_tfi_info;
+vrc_status vrc_tf_read_tfi(const char* path, vrc_tfi_info* info, vrc_tf_key* keys, int max_keys);
 
 /* ---- pre-integrated classification --------------------------------------
  * PreIntegrationTable (src/core/datastructures/transfunc/1d/preintegrationtable.cpp):

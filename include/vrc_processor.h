@@ -62,6 +62,10 @@ vrc_status vrcp_set_tf_keys(vrcp_processor* p, const vrc_tf_key* keys, int nkeys
                             float threshold_hi);
 vrc_status vrcp_set_tf_domain(vrcp_processor* p, float lo, float hi, int fitted, int width);
 vrc_status vrcp_get_tf(const vrcp_processor* p, int* width, float* lo, float* hi, int* fitted);
+/* Loads a .tfi file into "transferFunction" (vrc_tf_read_tfi), as
+ * TransFunc1DKeysProperty loads one: keys, gamma, thresholds and the file's
+ * domain, which process() then keeps. */
+vrc_status vrcp_load_tf(vrcp_processor* p, const char* path);
 
 /* Ports. Data is borrowed: it must stay valid until process() returns.
  * A NULL pointer disconnects the port. A volume is uploaded again when

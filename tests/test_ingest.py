@@ -87,3 +87,92 @@ def test_shipped_volumes(vrc_lib, name):
         scale = {v.U8: 255.0, v.U16: 65535.0, v.F32: 1.0}[info.dtype]
         assert np.float32(vox.min() / scale) == pytest.approx(lo, abs=1e-7)
         assert np.float32(vox.max() / scale) == pytest.approx(hi, abs=1e-7)
+
+
+REF_TFS = os.path.join(os.path.dirname(REF_VOLUMES), "..", "voreencore", "transferfuncs")
+
+TFI = """<?xml version="1.0" ?>
+<VoreenData version="1">
+    <TransFuncIntensity type="TransFuncIntensity">
+        <texDimensions x="4096" y="1" z="1" />
+        <gammaValue value="1.5" />
+        <domain x="-100" y="3000.5" />
+        <Keys>
+            <key type="TransFuncMappingKey">
+                <intensity value="0.25" />
+                <split value="false" />
+                <colorL r="10" g="20" b="30" a="40" />
+            </key>
+            <key type="TransFuncMappingKey">
+                <intensity value="0.5" />
+                <split value="true" />
+                <colorL r="1" g="2" b="3" a="4" />
+                <colorR r="250" g="240" b="230" a="220" />
+            </key>
+        </Keys>
+    </TransFuncIntensity>
+</VoreenData>
+"""
+
+
+def test_read_tfi_fields_defaults_and_split_keys(vrc_lib, tmp_path):
+    f = tmp_path / "t.tfi"
+    f.write_text(TFI)
+    t = v.read_tfi(str(f))
+    assert t["width"] == 4096 and t["gamma"] == 1.5 and t["alpha_mode"] == 1  # alphaMode absent: 1
+    assert t["domain"] == (-100.0, 3000.5) and t["threshold"] == (0.0, 1.0)  # threshold absent: (0, 1)
+    assert t["keys"] == [(0.25, (10, 20, 30, 40), (10, 20, 30, 40)), (0.5, (1, 2, 3, 4), (250, 240, 230, 220))]
+    # the keys bake like keys given directly
+    a = v.TransferFunction.bake([(k[0], k[1], k[2]) for k in t["keys"]], 256, t["gamma"], t["threshold"])
+    b = v.TransferFunction.bake([(0.25, (10, 20, 30, 40)), (0.5, (1, 2, 3, 4), (250, 240, 230, 220))], 256, 1.5)
+    np.testing.assert_array_equal(a, b)
+    with pytest.raises(v.VrcError):
+        v.read_tfi(str(tmp_path / "missing.tfi"))
+    (tmp_path / "bad.tfi").write_text("<VoreenData><SomethingElse/></VoreenData>")
+    with pytest.raises(v.VrcError):
+        v.read_tfi(str(tmp_path / "bad.tfi"))
+
+
+def test_processor_loads_tfi(vrc_lib, tmp_path):
+    from voreen_gb300.raycaster import CudaRaycaster
+    f = tmp_path / "t.tfi"
+    f.write_text(TFI)
+    r = CudaRaycaster()
+    r.load_transfer_function(str(f))
+    assert r.transferFunction.domain == (-100.0, 3000.5) and r.transferFunction.domain_fitted
+    assert r.transferFunction.gamma == 1.5 and len(r.transferFunction.keys) == 2
+    r.close()
+
+
+def _etree_tfi(path):
+    root = ET.parse(path).getroot().find("TransFuncIntensity")
+    def xy(tag, default):
+        e = root.find(tag)
+        return (float(e.get("x")), float(e.get("y"))) if e is not None else default
+    keys = []
+    for k in root.find("Keys").findall("key"):
+        col = lambda e: tuple(int(e.get(c)) for c in "rgba")
+        cl = col(k.find("colorL"))
+        split = k.find("split").get("value") == "true"
+        keys.append((float(np.float32(float(k.find("intensity").get("value")))), cl,
+                     col(k.find("colorR")) if split else cl))
+    g = root.find("gammaValue")
+    return {"keys": keys, "domain": xy("domain", (0.0, 1.0)), "threshold": xy("threshold", (0.0, 1.0)),
+            "gamma": float(g.get("value")) if g is not None else 1.0}
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_TFS), reason="the Voreen source tree is not present")
+def test_reference_tfi_files_equal_an_independent_parse(vrc_lib):
+    """The reference's own .tfi files (sample and preset transfer functions)
+    read as Python's XML parser reads them."""
+    paths = [os.path.join(REF_TFS, f) for f in ("nucleon.tfi", "walnut.tfi")]
+    pre = os.path.join(REF_TFS, "presets", "1dkeys")
+    if os.path.isdir(pre):
+        paths += sorted(os.path.join(pre, f) for f in os.listdir(pre) if f.endswith(".tfi"))
+    assert len(paths) >= 2
+    for p in paths:
+        t, ref = v.read_tfi(p), _etree_tfi(p)
+        assert t["keys"] == ref["keys"], p
+        assert t["domain"] == tuple(np.float32(ref["domain"]).tolist()), p
+        assert t["threshold"] == tuple(np.float32(ref["threshold"]).tolist()), p
+        assert t["gamma"] == float(np.float32(ref["gamma"])), p

@@ -370,6 +370,19 @@ def sampling_step(vol: "Volume", sampling_rate: float) -> float:
     return float(lib().vrc_sampling_step(vol.handle, sampling_rate))
 
 
+def read_tfi(path: str) -> dict:
+    """A Voreen .tfi transfer function (vrc_tf_read_tfi): keys as
+    (intensity, colorL, colorR), gamma, thresholds, domain, width, alphaMode."""
+    info = _abi.TfiInfo()
+    _check(lib().vrc_tf_read_tfi(path.encode(), C.byref(info), None, 0), None, "vrc_tf_read_tfi")
+    keys = (TFKey * max(1, info.nkeys))()
+    _check(lib().vrc_tf_read_tfi(path.encode(), C.byref(info), keys, info.nkeys), None, "vrc_tf_read_tfi")
+    return {"keys": [(float(k.intensity), tuple(k.color_l), tuple(k.color_r)) for k in keys[:info.nkeys]],
+            "gamma": float(info.gamma), "threshold": (float(info.threshold[0]), float(info.threshold[1])),
+            "domain": (float(info.domain[0]), float(info.domain[1])), "width": int(info.width),
+            "alpha_mode": int(info.alpha_mode)}
+
+
 def measure_l2_read(ctx: Context, nbytes: int = 48 << 20, reps: int = 40) -> float:
     """L2-resident read bandwidth in GB/s (vrc_measure_l2_read)."""
     g = C.c_float()

@@ -40,6 +40,11 @@ class TFKey(C.Structure):
     _fields_ = [("intensity", C.c_float), ("color_l", C.c_uint8 * 4), ("color_r", C.c_uint8 * 4)]
 
 
+class TfiInfo(C.Structure):
+    _fields_ = [("width", C.c_int), ("alpha_mode", C.c_int), ("gamma", C.c_float), ("domain", C.c_float * 2),
+                ("threshold", C.c_float * 2), ("nkeys", C.c_int)]
+
+
 class Camera(C.Structure):
     _fields_ = [("position", C.c_float * 3), ("focus", C.c_float * 3), ("up", C.c_float * 3),
                 ("fovy_deg", C.c_float), ("near_dist", C.c_float), ("far_dist", C.c_float),
@@ -96,6 +101,7 @@ SIGNATURES = {
     "vrc_volume_cache_info": (C.c_int, [VP, P(C.c_longlong), P(C.c_longlong), P(C.c_longlong)]),
     "vrc_volume_set_lod": (C.c_int, [VP, C.c_int]),
     "vrc_measure_l2_read": (C.c_int, [VP, C.c_size_t, C.c_int, P(C.c_float)]),
+    "vrc_tf_read_tfi": (C.c_int, [C.c_char_p, P(TfiInfo), P(TFKey), C.c_int]),
     "vrc_volume_set_cache_upload_budget": (C.c_int, [VP, C.c_size_t]),
     "vrc_volume_minmax": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),
     "vrc_volume_brick_minmax": (C.c_int, [VP, P(C.c_int), VP, VP]),
@@ -174,6 +180,7 @@ PROC_SIGNATURES = {
     "vrcp_set_tf_keys": (C.c_int, [VP, P(TFKey), C.c_int, C.c_float, C.c_float, C.c_float]),
     "vrcp_set_tf_domain": (C.c_int, [VP, C.c_float, C.c_float, C.c_int, C.c_int]),
     "vrcp_get_tf": (C.c_int, [VP, P(C.c_int), P(C.c_float), P(C.c_float), P(C.c_int)]),
+    "vrcp_load_tf": (C.c_int, [VP, C.c_char_p]),
     "vrcp_set_volume": (C.c_int, [VP, P(VolumeDesc), VP]),
     "vrcp_set_entry_exit": (C.c_int, [VP, VP, VP, C.c_int, C.c_int]),
     "vrcp_set_output_size": (C.c_int, [VP, C.c_int, C.c_int]),

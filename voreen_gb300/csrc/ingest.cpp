@@ -191,6 +191,71 @@ vrc_status vrc_vvd_read_header(const char* vvd_path, vrc_vvd_info* info) {
     return VRC_OK;
 }
 
+vrc_status vrc_tf_read_tfi(const char* path, vrc_tfi_info* info, vrc_tf_key* keys, int max_keys) {
+    if (!path || !info || max_keys < 0 || (max_keys > 0 && !keys)) return VRC_ERR_INVALID_ARG;
+    std::memset(info, 0, sizeof(*info));
+    info->alpha_mode = 1;
+    info->gamma = 1.f;
+    info->domain[1] = 1.f;
+    info->threshold[1] = 1.f;
+    std::string s;
+    if (!read_file(path, s)) return VRC_ERR_NOT_READY;
+    size_t tb, te;
+    if (!find_tag(s, "TransFuncIntensity", 0, tb, te)) return VRC_ERR_UNSUPPORTED;
+    size_t kb = std::string::npos, ke = std::string::npos;
+    const bool have_keys = find_tag(s, "Keys", te, kb, ke);
+    const size_t keys_end = have_keys ? s.find("</Keys>", ke) : std::string::npos;
+    // a scalar element of the function (before its key list): attribute `a` of <tag>
+    auto field = [&](const char* tag, const char* a, float& out) {
+        size_t b, e;
+        std::string v;
+        if (find_tag(s, tag, te, b, e) && (!have_keys || b < kb) && attr(s, b, e, a, v)) to_float(v, out);
+    };
+    float f = 0.f;
+    f = (float)info->alpha_mode;
+    field("alphaMode", "value", f);
+    info->alpha_mode = (int)f;
+    f = 0.f;
+    field("texDimensions", "x", f);
+    info->width = (int)f;
+    field("gammaValue", "value", info->gamma);
+    field("domain", "x", info->domain[0]);
+    field("domain", "y", info->domain[1]);
+    field("threshold", "x", info->threshold[0]);
+    field("threshold", "y", info->threshold[1]);
+    int n = 0;
+    size_t p = have_keys ? ke : std::string::npos;
+    size_t b, e;
+    while (have_keys && find_tag(s, "key", p, b, e) && (keys_end == std::string::npos || b < keys_end)) {
+        const size_t end = s.find("</key>", e);
+        if (end == std::string::npos) return VRC_ERR_INVALID_ARG;
+        vrc_tf_key k{};
+        size_t xb, xe;
+        std::string v;
+        if (!find_tag(s, "intensity", e, xb, xe) || xb > end || !attr(s, xb, xe, "value", v) || !to_float(v, k.intensity))
+            return VRC_ERR_INVALID_ARG;
+        bool split = false;
+        if (find_tag(s, "split", e, xb, xe) && xb < end && attr(s, xb, xe, "value", v)) split = v == "true" || v == "1";
+        auto color = [&](const char* tag, uint8_t* c) {
+            size_t cb, ce;
+            if (!find_tag(s, tag, e, cb, ce) || cb > end) return false;
+            const char* ch[4] = {"r", "g", "b", "a"};
+            for (int i = 0; i < 4; ++i) {
+                std::string cv;
+                c[i] = attr(s, cb, ce, ch[i], cv) ? (uint8_t)std::atoi(cv.c_str()) : (uint8_t)(i == 3 ? 255 : 0);
+            }
+            return true;
+        };
+        if (!color("colorL", k.color_l)) return VRC_ERR_INVALID_ARG;
+        if (!split || !color("colorR", k.color_r)) std::memcpy(k.color_r, k.color_l, 4);
+        if (n < max_keys) keys[n] = k;
+        ++n;
+        p = end;
+    }
+    info->nkeys = n;
+    return VRC_OK;
+}
+
 vrc_status vrc_volume_load_vvd(vrc_context* ctx, const char* vvd_path, int brick_size, vrc_volume** out,
                                vrc_vvd_info* info_out) {
     if (!ctx) return VRC_ERR_INVALID_ARG;

@@ -580,6 +580,24 @@ vrc_status vrcp_get_tf(const vrcp_processor* p, int* width, float* lo, float* hi
     return VRC_OK;
 }
 
+vrc_status vrcp_load_tf(vrcp_processor* p, const char* path) {
+    if (!p || !path) return VRC_ERR_INVALID_ARG;
+    vrc_tfi_info info;
+    vrc_status st = vrc_tf_read_tfi(path, &info, nullptr, 0);
+    if (st != VRC_OK) return st;
+    std::vector<vrc_tf_key> keys((size_t)info.nkeys);
+    if ((st = vrc_tf_read_tfi(path, &info, keys.data(), info.nkeys)) != VRC_OK) return st;
+    auto& t = p->r.transferFunction;
+    t.keys = keys;
+    t.gamma = info.gamma;
+    t.threshold_lo = info.threshold[0];
+    t.threshold_hi = info.threshold[1];
+    t.domain_lo = info.domain[0];
+    t.domain_hi = info.domain[1];
+    t.domain_fitted = true;  // the file's domain is kept
+    return VRC_OK;
+}
+
 vrc_status vrcp_set_volume(vrcp_processor* p, const vrc_volume_desc* desc, const void* voxels) {
     if (!p || (voxels && !desc)) return VRC_ERR_INVALID_ARG;
     auto& v = p->r.volume;

@@ -64,7 +64,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import _abi, lib, make_camera, make_desc
+from . import _abi, lib, make_camera, make_desc, read_tfi
 from ._abi import F32, U8, U16, Camera, RenderStats, TFKey
 
 log = logging.getLogger("voreen.CudaRaycaster")
@@ -200,6 +200,19 @@ class CudaRaycaster:
             self.close()
         except Exception:
             pass
+
+    def load_transfer_function(self, path: str):
+        """Loads a Voreen .tfi file into transferFunction (keys, gamma,
+        thresholds and the file's domain, which process() keeps)."""
+        st = lib().vrcp_load_tf(self._h, path.encode())
+        if st != _abi.VRC_OK:
+            raise RuntimeError(f"vrcp_load_tf({path}): {_abi.STATUS_NAMES.get(st, st)}")
+        t = read_tfi(path)
+        self.transferFunction.keys = [(k[0], k[1], k[2]) for k in t["keys"]]
+        self.transferFunction.gamma = t["gamma"]
+        self.transferFunction.threshold = t["threshold"]
+        self.transferFunction.domain = t["domain"]
+        self.transferFunction.domain_fitted = True
 
     def isReady(self) -> bool:
         """volume + entry/exit ports, as CPURaycaster::isReady (cpuraycaster.cpp:82-84)."""
