@@ -3,7 +3,7 @@
 ctypes bindings over ``oracle/_build/liborc.so`` (oracle/cpu_raycaster.cpp),
 a C++ restatement of Voreen's CPURaycaster path plus the GLSL-only shading,
 MIP and ISO rules. Only tests, the smoke check and the benchmark's CPU
-baseline use it, as the checker; the product library never does.
+baseline use it, to compare results with; the product library never does.
 
 Parity status: the trilinear interpolation / normalisation and the camera
 matrices are pinned against the reference's own compiled code (golden

@@ -2,7 +2,8 @@
  * CPU oracle for the single-volume ray march -- TEST INFRASTRUCTURE ONLY.
  *
  * Only the tests, the smoke check and the benchmark's CPU-baseline leg load
- * this file's library, and only as the checker / the timed CPU reference. The
+ * this file's library, and only to compare results with or as the timed CPU
+ * reference. The
  * product library (voreen_gb300/csrc) never includes or links it.
  *
  * Restates, in plain C++ (reference paths are relative to the Voreen tree):
