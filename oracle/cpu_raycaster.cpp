@@ -3,8 +3,8 @@
  *
  * Only the tests, the smoke check and the benchmark's CPU-baseline leg load
  * this file's library, and only to compare results with or as the timed CPU
- * reference. The
- * product library (voreen_gb300/csrc) never includes or links it.
+ * reference. The product library (voreen_gb300/csrc) never includes or
+ * links it.
  *
  * Restates, in plain C++ (reference paths are relative to the Voreen tree):
  *   CPURaycaster::process / directRendering / apply1DTF
