@@ -4,8 +4,8 @@
  * A plain C++ restatement of Voreen's CPURaycaster path (and of the GLSL-only
  * shading / MIP / ISO rules of SingleVolumeRaycaster), used by the tests, the
  * smoke check and the CPU-baseline leg of the benchmark to compare results
- * with. The
- * product library never links, loads or calls anything in this directory.
+ * with. The product library never links, loads or calls anything in this
+ * directory.
  *
  * Parity status: the trilinear interpolation and voxel normalisation are
  * pinned against the reference's own compiled VolumeRAM code (oracle/ref_pin,
