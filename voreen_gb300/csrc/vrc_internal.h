@@ -233,6 +233,7 @@ struct vrc_volume {
     size_t pending_pos = 0;
     size_t upload_budget = 0;          // bytes gathered per render, 0 = unlimited
     bool cache_valid = false;
+    uint64_t cache_src_key[4] = {0, 0, 0, 0};  // (TF or table uid, width, domain bits) the plan was made for
     long long cache_reachable = 0;     // bricks the current TF can reach
     // refinement: bricks the last frame touched (d_used) displace bricks it
     // did not touch; h_last_used = frame that last touched a brick
