@@ -34,10 +34,14 @@ _DTYPE_NP = {U8: np.uint8, U16: np.uint16, F32: np.float32}
 
 
 def lib():
+    """The loaded libvrc.so with its ctypes signatures (raises when it is not built)."""
     return _abi.load()
 
 
 class VrcError(RuntimeError):
+    """A vrc_status other than VRC_OK, with the context's error detail; `status`
+    holds the code."""
+
     def __init__(self, status: int, message: str):
         super().__init__(f"{_abi.STATUS_NAMES.get(status, status)}: {message}")
         self.status = status
@@ -97,6 +101,8 @@ class Context:
 
 
 def make_desc(dtype: int, dims_xyz, spacing=(1.0, 1.0, 1.0), offset=(0.0, 0.0, 0.0), rwm=(1.0, 0.0)) -> VolumeDesc:
+    """vrc_volume_desc: dtype, dims (x, y, z), spacing, offset and the real-world
+    mapping (scale, offset) of a volume."""
     d = VolumeDesc()
     d.dtype = dtype
     d.dims[:] = [int(v) for v in dims_xyz]
@@ -391,12 +397,16 @@ def measure_l2_read(ctx: Context, nbytes: int = 48 << 20, reps: int = 40) -> flo
 
 
 def default_params(width: int, height: int) -> RenderParams:
+    """Render parameters with the reference processor's property defaults
+    (vrc_render_params_default) for a width x height image."""
     p = RenderParams()
     lib().vrc_render_params_default(C.byref(p), width, height)
     return p
 
 
 def make_camera(position, focus, up=(0.0, 1.0, 0.0), fovy=45.0, near=0.1, far=50.0, ratio=1.0) -> Camera:
+    """A perspective camera (tgt::Camera fields: position, focus, up, vertical
+    field of view in degrees, near/far distances, frustum ratio)."""
     c = Camera()
     c.position[:] = [float(v) for v in position]
     c.focus[:] = [float(v) for v in focus]
@@ -406,6 +416,8 @@ def make_camera(position, focus, up=(0.0, 1.0, 0.0), fovy=45.0, near=0.1, far=50
 
 
 def camera_matrices(cam: Camera, desc: VolumeDesc, width: int, height: int):
+    """(view, projection, inverse(projection * view * textureToWorld)) as
+    4 x 4 float64 arrays, computed as the reference does (vrc_camera_matrices)."""
     v = np.zeros(16, np.float64)
     p = np.zeros(16, np.float64)
     inv = np.zeros(16, np.float64)

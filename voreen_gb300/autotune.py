@@ -23,12 +23,18 @@ SKIP_CELLS = (8, 16)
 
 
 def class_key(dtype: int, dims, width: int, height: int) -> str:
+    """Request class the tuned settings are cached under: dtype, log2 of the
+    largest volume dimension, log4 of the pixel count (both rounded)."""
     vclass = int(round(math.log2(max(dims))))
     iclass = int(round(math.log2(max(1, width * height)) / 2))
     return f"dt{dtype}-v{vclass}-i{iclass}"
 
 
 class Autotuner:
+    """Times the candidate tile widths, brick sizes and skip cells on one
+    representative request per class and keeps the fastest (optionally
+    persisted as JSON at cache_path)."""
+
     def __init__(self, ctx, cache_path: str | None = None, frames: int = 3):
         self.ctx = ctx
         self.frames = frames

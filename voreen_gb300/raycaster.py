@@ -89,6 +89,8 @@ class VolumeData:
 
 
 class Port:
+    """A processor port: its id and the data it currently holds."""
+
     def __init__(self, name: str):
         self.name = name
         self.data = None
@@ -108,6 +110,9 @@ class Port:
 
 @dataclass
 class TransFunc1DKeys:
+    """The transferFunction property: keys as (intensity, colour) or
+    (intensity, colourL, colourR), domain, gamma, thresholds, and the table
+    width / domain fitting state process() maintains."""
     keys: list = field(default_factory=lambda: [(0.0, (0, 0, 0, 0)), (1.0, (255, 255, 255, 255))])
     domain: tuple = (0.0, 1.0)
     gamma: float = 1.0
@@ -121,6 +126,8 @@ def _id(name: str) -> bytes:
 
 
 class CudaRaycaster:
+    """The C++ CudaRaycaster processor (include/vrc_processor.h) with its
+    ports as attributes and its properties readable and writable by id."""
     className = "CudaRaycaster"
     category = "Raycasting"
 
@@ -279,6 +286,8 @@ class CudaRaycaster:
             object.__setattr__(self, "lastStats", st)
 
     def process(self, analytic_entry_exit: bool = False, interacting: bool = False):
+        """One frame into outport (CPURaycaster::process; interaction mode as
+        SingleVolumeRaycaster's). On failure: lastError, no new output."""
         self._push()
         lib().vrcp_process(self._h, 1 if analytic_entry_exit else 0, 1 if interacting else 0)
         self._pull()
