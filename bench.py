@@ -134,16 +134,27 @@ def load_traffic(key: str = "dram_bytes_per_launch"):
     return None
 
 
-def build_workload(small: bool, kind: str = "ct"):
+def build_workload(small: bool, kind: str = "ct", volume_fn=None):
     """ct: 512^3 u16 shaded DVR 1080p; mip: the same volume and TF under MIP;
-    blobs: 128^3 u8 plain DVR 512x512 (the CPU-runnable case)."""
+    blobs: 128^3 u8 plain DVR 512x512 (the CPU-runnable case). volume_fn:
+    the volume generator (default: the library's)."""
     from voreen_gb300 import synth
     if kind == "blobs":
-        return synth.config1()
+        return synth.config1(volume_fn=volume_fn)
     comp = synth.MIP if kind == "mip" else synth.DVR
     if small:
-        return synth.config2(size=(256, 256, 256), image=(960, 540), compositing=comp)
-    return synth.config2(compositing=comp)
+        return synth.config2(size=(256, 256, 256), image=(960, 540), compositing=comp, volume_fn=volume_fn)
+    return synth.config2(compositing=comp, volume_fn=volume_fn)
+
+
+def oracle_workload_params(w, shading=None):
+    """The oracle's render parameters for workload w (the processor defaults
+    of the library's vrc_render_params_default: iso 0.5, ERT 0.95, light
+    0.4 / 0.8 / 0.6, shininess 60)."""
+    import oracle
+    return oracle.make_params(sampling_rate=w.sampling_rate, compositing=w.compositing,
+                              shading=w.shading if shading is None else shading, iso_value=0.5, ert=0.95,
+                              light_pos=list(w.light_pos)[:3], camera_pos=list(w.camera_pos))
 
 
 def run_cpu(w, entry, exit_pts, target_s: float, start_row: int | None = None):
@@ -151,13 +162,8 @@ def run_cpu(w, entry, exit_pts, target_s: float, start_row: int | None = None):
     sized to about target_s: centred, or starting at start_row (wrapping to
     the top). Returns (seconds, rows, samples, threads, first row)."""
     import oracle
-    import numpy as np
-    p = w.params()
-    op = oracle.make_params(sampling_rate=p.sampling_rate, compositing=p.compositing, shading=p.shading,
-                            iso_value=p.iso_value, ert=p.ert_threshold, light_pos=list(p.light_position)[:3],
-                            camera_pos=list(p.camera.position))
-    import voreen_gb300 as v
-    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    op = oracle_workload_params(w)
+    tf = oracle.bake_tf(w.tf_keys, w.tf_width)
     ov = oracle.make_volume(w.voxels, w.spacing)
     H = w.height
     threads = os.cpu_count() or 1
@@ -753,9 +759,12 @@ def main():
         run_ingest(args, warmup, ws, rank, local)
         return
 
-    w = build_workload(args.small, args.workload)
+    if args.impl == "reference":
+        import oracle
+        w = build_workload(args.small, args.workload, volume_fn=oracle.synth_volume)
+    else:
+        w = build_workload(args.small, args.workload)
     shading = w.shading if args.shading == "phong" else v.SHADE_NONE
-    p = w.params(skip_cell_size=args.skip_cell, empty_space_skipping=0 if args.no_skip else 1, shading=shading)
     npix = w.width * w.height
     bpv = w.voxels.dtype.itemsize
     comp_name = {v.DVR: "dvr", v.MIP: "mip", v.ISO: "iso"}[w.compositing]
@@ -771,11 +780,12 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        from voreen_gb300 import build as vbuild
-        vbuild.build()  # host-only entry points (camera matrices, TF bake); no GPU is used on this arm
+        # the CPU arm loads nothing of the product: volume, TF bake, camera
+        # and entry/exit all come from oracle/
         import oracle
-        desc = v.make_desc(v.U16, w.dims, w.spacing)
-        _, _, inv = v.camera_matrices(p.camera, desc, w.width, w.height)
+        from oracle import camera as ocam
+        inv = ocam.inverse_mvp(w.camera_pos, w.camera_focus, (0.0, 1.0, 0.0), w.fovy, w.near, w.far, w.width,
+                               w.height, w.dims, w.spacing)
         e, x = oracle.entry_exit(inv, w.width, w.height)
         # each step renders a band of centre rows sized so the whole run takes
         # about 150 s of CPU time (at least 2 rows a step): a bounded sample
@@ -805,6 +815,7 @@ def main():
         print(json.dumps(line))
         return
 
+    p = w.params(skip_cell_size=args.skip_cell, empty_space_skipping=0 if args.no_skip else 1, shading=shading)
     import torch
     from voreen_gb300 import build as vbuild
     vbuild.build()

@@ -406,21 +406,30 @@ vrc_status vrc_batch_destroy(vrc_batch* b);
 
 /* ---- render without allocating ---------------------------------------------
  * No counterpart in the reference: an addition for callers that cannot call
- * cudaMalloc while they render -- code inside a CUDA graph capture or a
- * real-time frame loop (cudaMalloc can synchronise the device), or hosts
- * whose device memory belongs to their own fixed-budget pool or to another
- * runtime. It renders like vrc_render but keeps its scratch (sample and tile
- * counters, the per-render TF table, the empty-space cell map) in one
- * fixed-size array in device global memory that every GPU loading the
- * library holds until exit, and it allocates nothing.
+ * cudaMalloc while they render -- a real-time frame loop (cudaMalloc can
+ * synchronise the device and stall the frame), or hosts whose device memory
+ * belongs to their own fixed-budget pool or to another runtime. It renders
+ * like vrc_render but keeps its scratch (sample and tile counters, the
+ * per-render TF table, the empty-space cell map) in one fixed-size array in
+ * device global memory that every GPU loading the library holds until exit,
+ * and it allocates nothing.
  * Limits: at most VRC_NOALLOC_MAX_CELLS empty-space cells when skipping is on
  * (a 1024^3 volume at the default 8^3 cells) and TF width <= 4096; larger
- * requests return VRC_ERR_SCRATCH_LIMIT and render nothing.
- * The caller passes the inputs (an uploaded volume, a TF, device entry/exit
- * images unless analytic), the device output image and the cudaStream_t to
- * run on; the call returns after enqueueing. Its first call on a device sets
- * up the scratch address for that device: make that call before any stream
- * capture. All calls share the array: calls that overlap on the GPU race. */
+ * requests return VRC_ERR_SCRATCH_LIMIT and render nothing. TF
+ * classification only (VRC_ERR_UNSUPPORTED otherwise). Frames equal
+ * vrc_render's, but empty space is skipped at the requested cell level only
+ * (no brick-level pass, no MIP cell skipping), and a host-placed brick pool
+ * is read in place (no device brick cache, no level of detail), so some
+ * frames take longer than vrc_render's.
+ * The caller passes the inputs (an uploaded volume, a TF of the same
+ * context, device entry/exit images unless analytic), the device output
+ * image and the cudaStream_t to run on; the call returns after enqueueing
+ * (no host buffer is read afterwards) and leaves the calling thread's
+ * current device as it found it. Its first call on a device sets up the
+ * scratch address for that device. All calls share the array: calls that
+ * overlap on the GPU race. The kernel's device status word is not reported
+ * (vrc_render's stats report it); the returned status covers the arguments
+ * and the launches. */
 #define VRC_NOALLOC_MAX_CELLS 2097152
 vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                               const float* d_entry, const float* d_exit, void* d_out, int out_format, void* stream);

@@ -235,6 +235,24 @@ def half_sample_mean(vox: np.ndarray) -> np.ndarray:
     return (acc // 8).astype(vox.dtype)
 
 
+_synth = None
+
+
+def synth_volume(kind: int, dtype: int, dims_xyz, seed: int) -> np.ndarray:
+    """The seeded workload volume (the same generator source as the product's
+    vrc_synth_volume, built as oracle/_build/libsynth.so), (Z, Y, X)."""
+    global _synth
+    if _synth is None:
+        _synth = C.CDLL(_build.build_synth())
+        _synth.vrc_synth_volume.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.c_uint64, C.c_void_p]
+        _synth.vrc_synth_volume.restype = C.c_int
+    X, Y, Z = dims_xyz
+    out = np.empty((Z, Y, X), {U8: np.uint8, U16: np.uint16, F32: np.float32}[dtype])
+    if _synth.vrc_synth_volume(kind, dtype, (C.c_int * 3)(X, Y, Z), seed, _ptr(out)) != 0:
+        raise ValueError("vrc_synth_volume: invalid arguments")
+    return out
+
+
 # ---- the reference pin library (present only where the reference tree is) ----
 _ref = None
 

@@ -19,7 +19,9 @@ BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(BUILD, "liborc.so")
 REF_LIB = os.path.join(REF_OUT, "libvoreen_ref.so")
-DEFAULT_REFERENCE = "/root/reference/voreen"
+# The Voreen source tree (read only) for the reference pin library: taken from
+# VOREEN_REFERENCE when set; absent on machines without the reference.
+DEFAULT_REFERENCE = os.environ.get("VOREEN_REFERENCE", "/root/reference/voreen")
 
 
 def _cxx() -> str:
@@ -43,6 +45,24 @@ def build(force: bool = False) -> str:
         if r.returncode != 0:
             raise RuntimeError(f"oracle build failed:\n{r.stderr}")
     return LIB
+
+
+SYNTH_SRC = os.path.join(os.path.dirname(HERE), "voreen_gb300", "csrc", "synth.cpp")
+SYNTH_LIB = os.path.join(BUILD, "libsynth.so")
+
+
+def build_synth(force: bool = False) -> str:
+    """The seeded workload generator (vrc_synth_volume) built on its own, so
+    that the benchmark's CPU arm makes the same input volumes as the GPU arm
+    without loading the product library."""
+    os.makedirs(BUILD, exist_ok=True)
+    hdr = os.path.join(os.path.dirname(HERE), "include", "vrc_synth.h")
+    if force or _stale(SYNTH_LIB, [SYNTH_SRC, hdr]):
+        cmd = [_cxx(), "-O3", "-std=c++17", "-fopenmp", "-fPIC", "-shared", SYNTH_SRC, "-o", SYNTH_LIB]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"workload generator build failed:\n{r.stderr}")
+    return SYNTH_LIB
 
 
 def build_ref(reference_root: str = DEFAULT_REFERENCE, force: bool = False) -> str | None:

@@ -11,7 +11,9 @@ import pytest
 import voreen_gb300 as v
 from voreen_gb300 import _abi
 
-REF_VOLUMES = "/root/reference/voreen/resource/voreenve/volumes"
+from oracle import build as _obuild
+
+REF_VOLUMES = os.path.join(_obuild.DEFAULT_REFERENCE, "resource", "voreenve", "volumes")
 
 
 def test_synthetic_headers(vrc_lib, tmp_path):

@@ -47,3 +47,46 @@ def test_camera_matrices_match_tgt(vrc_lib):
         if asp_eff >= 1.0:
             ref[0, 0] *= asp / asp_eff  # f / aspect with the window aspect the library was given
             np.testing.assert_allclose(proj, ref, rtol=1e-5, atol=1e-6)
+
+
+def test_oracle_camera_matches_tgt(orc):
+    """The oracle's own camera chain (used by the benchmark's CPU arm) against
+    the reference's createLookAt / createPerspective outputs."""
+    from oracle import camera as ocam
+    g = np.load(os.path.join(GOLD, "camera.npz"))
+    for i in range(len(g["eye"])):
+        m = ocam.look_at(g["eye"][i].astype(np.float64), g["focus"][i].astype(np.float64),
+                         g["up"][i].astype(np.float64))
+        np.testing.assert_allclose(m.reshape(-1), g["lookat"][i].astype(np.float64), rtol=2e-5, atol=2e-4)
+    for i in range(len(g["persp"])):
+        fov, asp, n, f = [float(x) for x in g["persp_params"][i]]
+        if asp < 1.0:
+            continue  # the camera widens fovy for tall windows; createPerspective alone does not
+        m = ocam.perspective(np.degrees(fov), n, f, asp)
+        np.testing.assert_allclose(m, g["persp"][i].astype(np.float64).reshape(4, 4), rtol=1e-5, atol=1e-6)
+
+
+def test_oracle_camera_equals_library(vrc_lib):
+    import voreen_gb300 as v
+    from oracle import camera as ocam
+    rng = np.random.default_rng(7)
+    for _ in range(20):
+        dims = tuple(int(d) for d in rng.integers(1, 600, 3))
+        spacing = tuple(float(s) for s in rng.uniform(0.3, 2.0, 3))
+        pos = rng.uniform(-900, 900, 3)
+        focus = rng.uniform(0, 300, 3)
+        W, H = int(rng.integers(16, 2000)), int(rng.integers(16, 2000))
+        fovy, near, far = float(rng.uniform(10, 90)), float(rng.uniform(0.1, 5)), float(rng.uniform(2000, 5000))
+        cam = v.make_camera(pos, focus, fovy=fovy, near=near, far=far)
+        _, _, inv = v.camera_matrices(cam, v.make_desc(v.U8, dims, spacing), W, H)
+        ours = ocam.inverse_mvp(pos, focus, (0, 1, 0), fovy, near, far, W, H, dims, spacing)
+        np.testing.assert_allclose(ours, inv, rtol=1e-9, atol=1e-12 * np.abs(inv).max())
+
+
+def test_oracle_generator_equals_library(vrc_lib):
+    """The benchmark's CPU arm builds its inputs with oracle.synth_volume: the
+    same volumes as the library's generator."""
+    import oracle
+    import voreen_gb300 as v
+    for kind, dt, dims, seed in [(0, v.U8, (40, 33, 27), 5), (1, v.U16, (64, 48, 40), 2002), (0, v.F32, (17, 9, 31), 9)]:
+        np.testing.assert_array_equal(oracle.synth_volume(kind, dt, dims, seed), v.synth_volume(kind, dt, dims, seed))

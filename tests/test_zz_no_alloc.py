@@ -1,11 +1,11 @@
 """vrc_render_noalloc through the C ABI.
 
 This entry point exists for callers that cannot allocate device memory while
-they render (graph capture, real-time loops, hosts with their own fixed
-device-memory pool): it keeps its scratch in a fixed array inside the
-library. Its frames must equal vrc_render's (same kernels, same host TF
-arithmetic: bit-equal), on consecutive calls that share that array, and a
-request beyond the array's capacity must be refused with
+they render (real-time loops, hosts with their own fixed device-memory
+pool): it keeps its scratch in a fixed array inside the library. Its frames
+must equal vrc_render's (same kernels, the same TF values: bit-equal), on
+consecutive calls that share that array, also for a brick pool in host
+memory, and a request beyond the array's capacity must be refused with
 VRC_ERR_SCRATCH_LIMIT. Collected last so that a failure here leaves every
 other test already run.
 """
@@ -75,3 +75,47 @@ def test_noalloc_refuses_requests_beyond_its_scratch(ctx):
     ref, _ = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F)
     np.testing.assert_array_equal(out.cpu().numpy().view(np.uint32), ref.view(np.uint32))
     vol.close()
+
+
+def test_noalloc_host_placed_pool(ctx):
+    """A brick pool in pinned host memory is read in place: the frame equals
+    vrc_render's of the same volume (which reads it through its device brick
+    cache) and of the device-resident volume."""
+    torch = pytest.importorskip("torch")
+    w = synth.config2(size=(80, 72, 64), image=(160, 120))
+    p = w.params()
+    p.entry_exit_mode = v.EE_ANALYTIC
+    host = v.Volume(ctx, w.voxels, w.spacing, placement=v.PLACE_HOST, brick_size=16)
+    dev = v.Volume(ctx, w.voxels, w.spacing, brick_size=16)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    ref_dev, _ = v.render(ctx, dev, tf, p, None, None, v.OUT_RGBA32F)
+    ref_host, _ = v.render(ctx, host, tf, p, None, None, v.OUT_RGBA32F)
+    for _ in range(2):
+        got = torch.full((p.height, p.width, 4), 3.0, dtype=torch.float32, device="cuda")
+        v.render_noalloc(host, tf, p, None, None, got, v.OUT_RGBA32F, ctx.stream)
+        ctx.synchronize()
+        g = got.cpu().numpy()
+        assert (g[..., 3] > 0).any()
+        np.testing.assert_array_equal(g.view(np.uint32), ref_host.view(np.uint32))
+        np.testing.assert_array_equal(g.view(np.uint32), ref_dev.view(np.uint32))
+    host.close()
+    dev.close()
+
+
+def test_noalloc_rejects_handles_of_two_contexts(ctx):
+    torch = pytest.importorskip("torch")
+    other = v.Context(0)
+    try:
+        w = synth.config1(size=(32, 32, 32), image=(32, 32))
+        vol = v.Volume(ctx, w.voxels, w.spacing)
+        tf = v.TransferFunction(other, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+        p = w.params()
+        p.entry_exit_mode = v.EE_ANALYTIC
+        out = torch.zeros((32, 32, 4), dtype=torch.float32, device="cuda")
+        with pytest.raises(v.VrcError) as ei:
+            v.render_noalloc(vol, tf, p, None, None, out, v.OUT_RGBA32F, ctx.stream)
+        assert ei.value.status == 1
+        tf.close()
+        vol.close()
+    finally:
+        other.close()

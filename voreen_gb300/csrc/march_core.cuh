@@ -28,7 +28,10 @@
 //    alpha is already decided, so it changes no discrete decision; its
 //    colours differ from the CPU path by ~1e-6.
 #pragma once
+#include <algorithm>
 #include <cstdint>
+#include <mutex>
+#include <vector>
 
 #include "vrc_internal.h"
 
@@ -849,14 +852,45 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
     }
 }
 
+// Resident CTAs per SM of one kernel instantiation for a dynamic shared
+// memory size, queried once per (device, size): the attribute call and the
+// occupancy query cost more host time than a frame's launch.
+template <typename K>
+cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
+    struct Entry {
+        int dev;
+        size_t smem;
+        int per_sm;
+    };
+    static std::mutex m;
+    static std::vector<Entry> seen;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(m);
+    for (const Entry& x : seen)
+        if (x.dev == dev && x.smem == smem) {
+            *per_sm = x.per_sm;
+            return cudaSuccess;
+        }
+    // the largest table (4096 entries, 64 KB) once per device; smaller ones fit under it
+    e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)std::max(smem, (size_t)4096 * sizeof(float4)));
+    if (e != cudaSuccess) return e;
+    int n = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem);
+    if (e != cudaSuccess) return e;
+    seen.push_back(Entry{dev, smem, n});
+    *per_sm = n;
+    return cudaSuccess;
+}
+
 template <int DT, int COMP, int SHADE, int EE, bool POOL>
 cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
     auto k = march_kernel<DT, COMP, SHADE, EE, POOL>;
     const size_t smem = (size_t)p.tf_width * sizeof(float4);
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
     int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 256, smem);
+    cudaError_t e = resident_ctas(k, smem, &per_sm);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const long long tiles = (long long)p.tiles_x * p.tiles_y;

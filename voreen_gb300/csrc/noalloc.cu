@@ -1,21 +1,27 @@
 // vrc_render_noalloc: a render that allocates nothing.
 //
-// Some callers cannot call cudaMalloc while they render: code running inside
-// a CUDA graph capture or a real-time frame loop (cudaMalloc can synchronise
-// the device), or a host application whose device memory is handed out by
-// its own fixed-budget pool or by another runtime. vrc_render grows scratch
-// buffers on demand; this variant keeps the same scratch -- the sample
-// counters and tile counter, the per-render float4 TF table and the
-// empty-space cell map -- in one fixed-size array in device global memory.
+// Some callers cannot call cudaMalloc while they render: a real-time frame
+// loop (cudaMalloc can synchronise the device and stall the frame), or a
+// host application whose device memory is handed out by its own
+// fixed-budget pool or by another runtime. vrc_render grows scratch buffers
+// on demand; this variant keeps the same scratch -- the sample counters and
+// tile counter, the per-render float4 TF table and the empty-space cell map
+// -- in one fixed-size array in device global memory.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads the
 // library holds NOALLOC_SCRATCH_BYTES of it until the process exits. Host
 // code never uses the symbol as an address: at set-up (the first call on a
 // device, with that device current) cudaGetSymbolAddress resolves its device
-// address once, and that address is what the kernels receive. Make that first
-// call before any stream capture. Every call shares the array and it keeps
-// the last call's contents: the counters are cleared on each call, and calls
-// that overlap on the GPU (other streams, or threads without ordering) race.
+// address once, and that address is what the kernels receive. Every call
+// shares the array and it keeps the last call's contents: the counters are
+// cleared on each call, and calls that overlap on the GPU (other streams, or
+// threads without ordering) race.
+//
+// The TF table is built on the device by a small kernel whose by-value
+// parameters carry the RGBA8 entries and the (opacity-corrected) alpha of
+// each of the 256 alpha bytes, computed on the host with the same powf
+// vrc_render uses; so no host buffer is read after the call returns and the
+// table equals vrc_render's bit for bit.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,11 +33,29 @@
 namespace {
 
 constexpr size_t COUNTER_BYTES = 256;                        // 16 x u64 counters, padded
-constexpr size_t TF_BYTES = (size_t)4096 * sizeof(float4);    // widest TF table
+constexpr int MAX_TF = 4096;
+constexpr size_t TF_BYTES = (size_t)MAX_TF * sizeof(float4);  // widest TF table
 constexpr size_t OCC_OFFSET = COUNTER_BYTES + TF_BYTES;
 constexpr size_t SCRATCH_BYTES = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS / 8;  // one bit per cell
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
+
+// Kernel parameters of the TF table build: 16 KB of RGBA8 entries and 1 KB of
+// alpha values (17.4 KB, inside the 32 KB kernel-parameter limit).
+struct TfTableArgs {
+    uchar4 rgba[MAX_TF];
+    float alpha[256];  // alpha' for each alpha byte
+    int width;
+};
+
+__global__ void tf_table_kernel(const TfTableArgs a, float4* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.width; i += gridDim.x * blockDim.x) {
+        const uchar4 c = a.rgba[i];
+        // correctly rounded IEEE divisions: the same values as the host's
+        out[i] = make_float4(__fdiv_rn((float)c.x, 255.f), __fdiv_rn((float)c.y, 255.f), __fdiv_rn((float)c.z, 255.f),
+                             a.alpha[c.w]);
+    }
+}
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
@@ -53,24 +77,32 @@ cudaError_t setup_device(int dev) {
     return cudaSuccess;
 }
 
-// Host staging for the TF table: thread-local static storage, no allocation
-// per call.
-thread_local float4 t_tf_host[4096];
-
 vrc_status cuda_status(cudaError_t e) { return e == cudaSuccess ? VRC_OK : VRC_ERR_CUDA; }
 
-}  // namespace
+// Makes `dev` current for the call and puts the caller's device back on
+// every return path.
+struct DeviceScope {
+    int prev = -1;
+    cudaError_t enter(int dev) {
+        cudaError_t e = cudaGetDevice(&prev);
+        if (e != cudaSuccess) {
+            prev = -1;
+            return e;
+        }
+        return prev == dev ? cudaSuccess : cudaSetDevice(dev);
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
 
-extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
-                                         const float* d_entry, const float* d_exit, void* d_out, int out_format,
-                                         void* stream) {
-    if (!vol || !tf || !p || !d_out) return VRC_ERR_INVALID_ARG;
-    vrc_status st = vrc::check_params(nullptr, p);
+vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p, const float* d_entry,
+                          const float* d_exit, void* d_out, int out_format, cudaStream_t s, int dev) {
+    unsigned char* scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    vrc::MarchParams P;
+    vrc_status st = vrc::fill_params(nullptr, vol, p, P);
     if (st != VRC_OK) return st;
-    if (out_format < VRC_OUT_RGBA8 || out_format > VRC_OUT_RGBA16) return VRC_ERR_INVALID_ARG;
-    if (p->entry_exit_mode == VRC_EE_BUFFERS && (!d_entry || !d_exit)) return VRC_ERR_NOT_READY;
-    if (tf->width > 4096) return VRC_ERR_SCRATCH_LIMIT;
-    if (p->classification != VRC_CLASSIFY_TF) return VRC_ERR_UNSUPPORTED;  // TF classification only
 
     // empty-space cells: the requested level, else the brick grid (as vrc_render)
     const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
@@ -88,30 +120,21 @@ extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf
     const long long ncells = (long long)nc[0] * nc[1] * nc[2];
     if (p->empty_space_skipping && ncells > (long long)VRC_NOALLOC_MAX_CELLS) return VRC_ERR_SCRATCH_LIMIT;
 
-    const int dev = vol->ctx ? vol->ctx->device : 0;
-    if (dev < 0 || dev >= MAX_DEVICES) return VRC_ERR_INVALID_ARG;
-    cudaError_t e = cudaSetDevice(dev);
-    if (e != cudaSuccess) return cuda_status(e);
-    if ((e = setup_device(dev)) != cudaSuccess) return cuda_status(e);
-    unsigned char* scratch = static_cast<unsigned char*>(g_scratch_addr[dev]);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-
-    vrc::MarchParams P;
-    if ((st = vrc::fill_params(nullptr, vol, p, P)) != VRC_OK) return st;
-
-    // TF table (r/255, g/255, b/255, alpha') into the scratch array; the same
-    // host arithmetic as vrc_render's table, so results match it exactly
+    // TF table (r/255, g/255, b/255, alpha') into the scratch array
+    static thread_local TfTableArgs args;
     const bool corrected = vrc::alpha_corrected(p->compositing, p->classification);
     const float kcorr = P.step * 200.f;
-    for (int i = 0; i < tf->width; ++i) {
-        const uint8_t* c = tf->h_rgba + 4 * i;
-        float a = float(c[3]) / 255.f;
-        if (corrected) a = 1.f - powf(1.f - a, kcorr);
-        t_tf_host[i] = make_float4(float(c[0]) / 255.f, float(c[1]) / 255.f, float(c[2]) / 255.f, a);
+    for (int a = 0; a < 256; ++a) {
+        float x = float(a) / 255.f;
+        if (corrected) x = 1.f - powf(1.f - x, kcorr);
+        args.alpha[a] = x;
     }
+    std::memcpy(args.rgba, tf->h_rgba, (size_t)tf->width * 4);
+    args.width = tf->width;
     float4* d_tf = reinterpret_cast<float4*>(scratch + COUNTER_BYTES);
-    if ((e = cudaMemcpyAsync(d_tf, t_tf_host, tf->width * sizeof(float4), cudaMemcpyHostToDevice, s)) != cudaSuccess)
-        return cuda_status(e);
+    tf_table_kernel<<<(tf->width + 255) / 256, 256, 0, s>>>(args, d_tf);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_status(e);
     P.tf_table = d_tf;
     P.tf_width = tf->width;
     P.tf_lo = tf->lo;
@@ -141,7 +164,28 @@ extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf
     P.counters = counters;
     P.status = reinterpret_cast<int*>(counters + 4);
     P.tile_counter = reinterpret_cast<unsigned int*>(counters + 5);
-    if ((e = vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, g_num_sms[dev], s)) != cudaSuccess)
-        return cuda_status(e);
-    return VRC_OK;
+    return cuda_status(vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, g_num_sms[dev], s));
+}
+
+}  // namespace
+
+extern "C" vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
+                                         const float* d_entry, const float* d_exit, void* d_out, int out_format,
+                                         void* stream) {
+    if (!vol || !tf || !p || !d_out) return VRC_ERR_INVALID_ARG;
+    if (vol->ctx != tf->ctx) return VRC_ERR_INVALID_ARG;  // handles of two contexts (possibly two GPUs)
+    vrc_status st = vrc::check_params(nullptr, p);
+    if (st != VRC_OK) return st;
+    if (out_format < VRC_OUT_RGBA8 || out_format > VRC_OUT_RGBA16) return VRC_ERR_INVALID_ARG;
+    if (p->entry_exit_mode == VRC_EE_BUFFERS && (!d_entry || !d_exit)) return VRC_ERR_NOT_READY;
+    if (tf->width > MAX_TF) return VRC_ERR_SCRATCH_LIMIT;
+    if (p->classification != VRC_CLASSIFY_TF) return VRC_ERR_UNSUPPORTED;  // TF classification only
+
+    const int dev = vol->ctx ? vol->ctx->device : 0;
+    if (dev < 0 || dev >= MAX_DEVICES) return VRC_ERR_INVALID_ARG;
+    DeviceScope scope;
+    cudaError_t e = scope.enter(dev);
+    if (e != cudaSuccess) return cuda_status(e);
+    if ((e = setup_device(dev)) != cudaSuccess) return cuda_status(e);
+    return render_noalloc(vol, tf, p, d_entry, d_exit, d_out, out_format, static_cast<cudaStream_t>(stream), dev);
 }

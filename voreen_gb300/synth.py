@@ -103,9 +103,12 @@ def tf_keys_trapezoids(centers, seed: int, alpha_range=(0.1, 0.8), top=(0.004, 0
     return out
 
 
-def config1(seed: int = 1, size=(128, 128, 128), image=(512, 512), azimuth=30.0, elevation=20.0) -> Workload:
-    """Plain DVR, 128^3 u8 Gaussian blobs, 256-entry ramp TF, 512^2, rate 2."""
-    vox = synth_volume(BLOBS, U8, size, 1000 * 1 + seed)
+def config1(seed: int = 1, size=(128, 128, 128), image=(512, 512), azimuth=30.0, elevation=20.0,
+            volume_fn=None) -> Workload:
+    """Plain DVR, 128^3 u8 Gaussian blobs, 256-entry ramp TF, 512^2, rate 2.
+    volume_fn: the generator (kind, dtype, dims, seed) -> voxels, by default
+    the library's vrc_synth_volume."""
+    vox = (volume_fn or synth_volume)(BLOBS, U8, size, 1000 * 1 + seed)
     pos, focus, near, far = orbit_camera(size, (1, 1, 1), azimuth, elevation)
     return Workload("plain DVR 128^3 u8 512x512", vox, (1.0, 1.0, 1.0), tf_keys_c1(), 256, (0.0, 1.0), image[0],
                     image[1], 2.0, DVR, SHADE_NONE, pos, focus, near=near, far=far)
@@ -127,12 +130,12 @@ def shells_tf(vox_u16: np.ndarray, seed: int, n_peaks: int = 5, rwm=(1.0, 0.0)):
 
 
 def config2(seed: int = 1, size=(512, 512, 512), image=(1920, 1080), compositing=DVR, azimuth=35.0,
-            elevation=25.0, dist_factor=1.25) -> Workload:
+            elevation=25.0, dist_factor=1.25, volume_fn=None) -> Workload:
     """CT-like shaded DVR (or MIP): 512^3 u16 nested shells, spacing
     (0.7, 0.7, 1.0), 4096-entry 5-trapezoid TF, Phong, 1920x1080, rate 2.
     The light sits at the camera position; the camera orbits at 1.25 x the box
-    diagonal so the volume fills most of the frame."""
-    vox = synth_volume(SHELLS, U16, size, 1000 * 2 + seed)
+    diagonal so the volume fills most of the frame. volume_fn as in config1."""
+    vox = (volume_fn or synth_volume)(SHELLS, U16, size, 1000 * 2 + seed)
     spacing = (0.7, 0.7, 1.0)
     keys, domain = shells_tf(vox, 1000 * 2 + seed)
     pos, focus, near, far = orbit_camera(size, spacing, azimuth, elevation, dist_factor)
