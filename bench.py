@@ -190,6 +190,35 @@ def run_cpu(w, entry, exit_pts, target_s: float, start_row: int | None = None):
     return dt, rows, total, threads, lo
 
 
+def frame_parity(ctx, vol, tf, p, w, e_dev, x_dev, e_host, x_host, gpu_samples):
+    """The benchmarked frame (same volume, TF, camera and entry/exit points),
+    rendered as RGBA32F by the library and by the FP32 and FP64 oracles over
+    the whole image: max |d| against each, and the rays where FP32 and FP64
+    take different discrete decisions (count, their max |d|, how many of them
+    exceed 1/255). Outside the timed region."""
+    import torch
+    import oracle
+    from oracle import parity
+    import voreen_gb300 as v
+    out = torch.empty((w.height, w.width, 4), dtype=torch.float32, device=e_dev.device)
+    _, st = v.render(ctx, vol, tf, p, e_dev, x_dev, v.OUT_RGBA32F, out)
+    img = out.cpu().numpy()
+    op = oracle_workload_params(w, shading=p.shading)
+    op.compositing = p.compositing
+    ov = oracle.make_volume(w.voxels, w.spacing)
+    otf = oracle.bake_tf(w.tf_keys, w.tf_width)
+    t0 = time.perf_counter()
+    o32, s32, fh32 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 32)
+    o64, s64, fh64 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 64)
+    step = 1.0 / (max(w.dims) * w.sampling_rate)
+    r = parity.report(img, o32, s32, fh32, o64, s64, fh64, p.compositing, step, shaded=p.shading != v.SHADE_NONE)
+    r.update({"frame": f"{w.width}x{w.height} full frame, RGBA32F", "bound": 1.0 / 255.0,
+              "samples_equal_fp32": int(s32.sum()) == int(st.samples) == int(gpu_samples),
+              "bit_equal_fp32": bool(np.array_equal(img.view(np.uint32), o32.view(np.uint32))),
+              "oracle_seconds": time.perf_counter() - t0})
+    return r
+
+
 def run_batch(args, warmup, ws, rank, local):
     """64 requests (volumes 64^3..512^3, u8/u16/f32, images 256^2..2048^2,
     DVR + Phong) in one persistent launch replayed from a CUDA graph; tile
@@ -934,6 +963,7 @@ def main():
                                 "sample": f"{rows} centre rows ({s_cpu} samples) of the same frame, extrapolated "
                                           f"to {w.width}x{w.height}; FP32 CPURaycaster restatement",
                                 "gsamples_per_s": s_cpu / dt / 1e9}
+        line["parity"] = frame_parity(ctx, vol, tf, p, w, e_dev, x_dev, e_host, x_host, samples)
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:

@@ -33,3 +33,22 @@ def ctx(vrc_lib):
     c = v.Context(0)
     yield c
     c.close()
+
+
+def pytest_terminal_summary(terminalreporter, exitstatus, config):
+    """Prints the FP64 parity reports the tests recorded: per case the max |d|
+    against the FP32 and FP64 oracles, and the decision-divergent rays (count
+    and their max |d|) that the 1/255 bound leaves out."""
+    try:
+        from helpers import REPORTS
+    except ImportError:
+        return
+    if not REPORTS:
+        return
+    tr = terminalreporter
+    tr.section("parity vs FP64 oracle (|d| in 1/255 units)")
+    for label, r in REPORTS:
+        tr.write_line(f"{label}: max vs FP32 {r['max_abs_vs_fp32'] * 255:.4f}, vs FP64 {r['max_abs_vs_fp64'] * 255:.4f} "
+                      f"on agreeing rays ({r['max_abs_vs_fp64_all_rays'] * 255:.4f} on all); divergent rays "
+                      f"{r['divergent_rays']} of {r['hit_rays']} hit, their max {r['divergent_max_abs_vs_fp64'] * 255:.4f}, "
+                      f"above 1/255: {r['waived_rays']}; channels > 0.5/255: {r['channels_over_half_lsb_vs_fp64']}")

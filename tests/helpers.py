@@ -5,9 +5,13 @@ from __future__ import annotations
 import numpy as np
 
 import oracle
+from oracle import parity
 import voreen_gb300 as v
 
 TOL = 1.0 / 255.0  # spec bound per RGBA channel against the FP64 oracle
+
+# Parity reports of this session (printed by conftest's terminal summary).
+REPORTS: list = []
 
 
 def oracle_params(w_params, light=None, cam=None, preint_table=None):
@@ -62,35 +66,22 @@ class Case:
                              e, x, precision, rows)
 
 
-def sample_index(first_hit, step):
-    """Loop index of the selected sample from its ray parameter (-1: none)."""
-    fh = np.asarray(first_hit, np.float64)
-    return np.where(fh >= 0, np.rint(fh / step), -1).astype(np.int64)
-
-
-def decision_divergent(o32, s32, fh32, o64, s64, fh64, comp, step, shaded=False):
-    """Rays where FP32 and FP64 take a different discrete decision: a
-    different number of samples (ERT step or the t > tend stop), a different
-    selected sample (first hit, MIP maximum, ISO hit), or for MIP / ISO a
-    different TF entry for the selected sample (the output is that entry)."""
-    div = s32 != s64
-    div |= sample_index(fh32, step) != sample_index(fh64, step)
-    if comp in (v.MIP, v.ISO):
-        d = np.abs(o32.astype(np.float64) - o64)
-        div |= d[..., 3] > 1e-6
-        if not shaded:
-            div |= d.max(axis=-1) > 1e-5
-    return div
+sample_index = parity.sample_index
+decision_divergent = parity.decision_divergent
 
 
 def assert_fp64_parity(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded=False, max_div_frac=2e-3,
-                       tol=TOL):
+                       tol=TOL, label=None):
     """max |d| <= tol on every ray where FP32 and FP64 make the same discrete
-    decisions; the rest (reported) must be a tiny fraction of the hit rays."""
-    d = np.abs(gpu_img.astype(np.float64) - o64).max(axis=-1)
-    div = decision_divergent(o32, s32, fh32, o64, s64, fh64, comp, step, shaded)
-    hits = max(1, int((s32 > 0).sum()))
-    assert div.sum() <= max(2, max_div_frac * hits), f"{div.sum()} decision-divergent rays of {hits}"
-    ok = ~div
-    assert d[ok].max(initial=0.0) <= tol, f"max |d| on agreeing rays = {d[ok].max() * 255:.3f}/255"
-    return float(d[ok].max(initial=0.0)), int(div.sum())
+    decisions. A ray above tol is waived only if its decisions diverge, and
+    the waived rays (counted, with their max |d| reported) must be a tiny
+    fraction of the hit rays. Returns the parity report."""
+    r = parity.report(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded, tol)
+    if label is not None:
+        REPORTS.append((label, r))
+    hits = max(1, r["hit_rays"])
+    assert r["waived_rays"] <= max(2, max_div_frac * hits), \
+        f"{r['waived_rays']} decision-divergent rays above the bound of {hits} hit rays " \
+        f"(their max |d| {r['divergent_max_abs_vs_fp64'] * 255:.3f}/255)"
+    assert r["max_abs_vs_fp64"] <= tol, f"max |d| on agreeing rays = {r['max_abs_vs_fp64'] * 255:.3f}/255"
+    return r

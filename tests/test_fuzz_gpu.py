@@ -7,7 +7,7 @@ import pytest
 
 import voreen_gb300 as v
 
-from helpers import Case
+from helpers import Case, assert_fp64_parity
 
 pytestmark = pytest.mark.gpu
 
@@ -81,9 +81,12 @@ def test_random_case_matches_oracle(ctx, seed):
     p.light_position[:] = [*eye, 1.0]
     c = Case(ctx, vox, tf, domain, p, spacing, rwm=rwm, brick=brick)
     img, st = c.gpu()
-    o32, s32, _ = c.oracle(32)
+    o32, s32, fh32 = c.oracle(32)
     assert st.samples == s32.sum()
     if shaded:
         assert np.abs(img - o32).max() <= 1e-4
     else:
         np.testing.assert_array_equal(_bits(img), _bits(o32))
+    if comp in (v.DVR, v.MIP, v.ISO):
+        o64, s64, fh64 = c.oracle(64)
+        assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, shaded=shaded)
