@@ -275,3 +275,36 @@ def ref_lib(reference_root: str | None = None):
         L.ref_iround.restype = C.c_int
         _ref = L
     return _ref
+
+
+_ref_tf = None
+
+
+def ref_tf_lib(reference_root: str | None = None):
+    """The reference's own TF bake arithmetic (oracle/_ref/libvoreen_tf_ref.so), or None."""
+    global _ref_tf
+    if _ref_tf is None:
+        path = _build.build_tf_ref(reference_root or _build.DEFAULT_REFERENCE)
+        if path is None:
+            if os.path.exists(_build.REF_TF_LIB):
+                path = _build.REF_TF_LIB
+            else:
+                return None
+        L = C.CDLL(path)
+        L.ref_tf_bake.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float,
+                                  C.c_void_p]
+        _ref_tf = L
+    return _ref_tf
+
+
+def ref_bake_tf(keys, width, gamma=1.0, threshold=(0.0, 1.0), reference_root: str | None = None):
+    """The TF table as the reference's own code bakes it (None without the
+    reference tree). keys as for bake_tf."""
+    L = ref_tf_lib(reference_root)
+    if L is None:
+        return None
+    inten = np.array([k[0] for k in keys] or [0.0], np.float32)
+    cols = np.array([list(k[1]) + list(k[2] if len(k) > 2 else k[1]) for k in keys] or [[0] * 8], np.uint8)
+    out = np.zeros((width, 4), np.uint8)
+    L.ref_tf_bake(_ptr(inten), _ptr(cols), len(keys), width, gamma, threshold[0], threshold[1], _ptr(out))
+    return out

@@ -93,6 +93,46 @@ def build_ref(reference_root: str = DEFAULT_REFERENCE, force: bool = False) -> s
     return REF_LIB
 
 
+REF_TF_LIB = os.path.join(REF_OUT, "libvoreen_tf_ref.so")
+
+
+def build_tf_ref(reference_root: str = DEFAULT_REFERENCE, force: bool = False) -> str | None:
+    """Compile the reference's own TF bake arithmetic into
+    oracle/_ref/libvoreen_tf_ref.so: TransFunc1DKeys::getMappingForValueUByte
+    (transfunc1dkeys.cpp), TransFunc1D::applyGammaToIntensity (transfunc1d.cpp)
+    and TransFuncMappingKey (transfuncmappingkey.cpp), driven by
+    oracle/ref_pin/tf_driver.cpp. Hidden visibility and section garbage
+    collection keep only what the driver reaches, so the GL, shader and
+    serialisation code those files also hold is dropped at link time.
+    Returns None when the reference tree is absent."""
+    base = os.path.join(reference_root, "src/core/datastructures/transfunc/1d")
+    srcs = [os.path.join(base, "1dkeys/transfunc1dkeys.cpp"), os.path.join(base, "transfunc1d.cpp"),
+            os.path.join(base, "1dkeys/utils/transfuncmappingkey.cpp"), os.path.join(HERE, "ref_pin", "tf_driver.cpp")]
+    if not all(os.path.exists(s) for s in srcs):
+        return None
+    os.makedirs(REF_OUT, exist_ok=True)
+    if not force and not _stale(REF_TF_LIB, srcs[3:]) and os.path.exists(REF_TF_LIB):
+        return REF_TF_LIB
+    inc = []
+    for d in ("", "ext", "include", "ext/boost/include", "ext/rapidjson", "ext/tinyxml", "ext/glew/include"):
+        inc += ["-I", os.path.join(reference_root, d)]
+    flags = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-DUNIX", "-DTIXML_USE_STL",
+             "-DBOOST_SYSTEM_NO_DEPRECATED", "-w", "-fvisibility=hidden", "-ffunction-sections", "-fdata-sections"]
+    objs = []
+    for s in srcs:
+        o = os.path.join(REF_OUT, "tf_" + os.path.basename(s) + ".o")
+        r = subprocess.run([_cxx(), *flags, *inc, "-c", s, "-o", o], capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference TF pin build failed for {s}:\n{r.stderr[-4000:]}")
+        objs.append(o)
+    r = subprocess.run([_cxx(), "-shared", "-Wl,--gc-sections", "-o", REF_TF_LIB, *objs], capture_output=True,
+                       text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference TF pin link failed:\n{r.stderr[-4000:]}")
+    return REF_TF_LIB
+
+
 if __name__ == "__main__":
     print(build(force=True))
     print(build_ref(force=True))
+    print(build_tf_ref(force=True))

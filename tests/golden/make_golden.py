@@ -13,6 +13,16 @@ Outputs (small, committed):
                  (ext/tgt/matrix.h:1196-1247) for seeded cameras.
   iround.npz     tgt::iround (ext/tgt/tgt_math.h:223-225) at values near
                  rounding boundaries.
+  tf_bake.npz    the TF bake of TransFunc1D::createTextureData
+                 (transfunc1d.cpp:85-103) over the reference's own
+                 TransFunc1DKeys::getMappingForValueUByte
+                 (1dkeys/transfunc1dkeys.cpp:119-154) and applyGammaToIntensity
+                 (oracle/_ref/libvoreen_tf_ref.so) for seeded key sets (split
+                 keys, coincident keys, keys on texel values, gamma != 1,
+                 thresholds, widths 2..4096) and the keys of the Voreen sample
+                 transfer functions nucleon.tfi / walnut.tfi.
+
+    python tests/golden/make_golden.py [/path/to/voreen] [--only tf_bake]
 """
 from __future__ import annotations
 
@@ -95,7 +105,77 @@ def iround_cases(ref, rng):
     return {"x": vals, "iround": res}
 
 
-def main(reference_root=None):
+def _random_keys(rng, n):
+    xs = np.sort(rng.uniform(0, 1, n)).astype(np.float32)
+    keys = []
+    for x in xs:
+        cl = tuple(int(c) for c in rng.integers(0, 256, 4))
+        cr = cl if rng.random() < 0.6 else tuple(int(c) for c in rng.integers(0, 256, 4))
+        keys.append((float(x), cl, cr))
+    return keys
+
+
+def _tfi_keys(path):
+    """Keys of a Voreen .tfi file (TransFunc1DKeys serialisation): intensity,
+    colorL, colorR (= colorL unless split)."""
+    import xml.etree.ElementTree as ET
+    root = ET.parse(path).getroot()
+    keys = []
+    for k in root.iter("key"):
+        inten = float(k.find("intensity").get("value"))
+        split = k.find("split").get("value") in ("true", "1")
+        cl = k.find("colorL")
+        cl = tuple(int(cl.get(c)) for c in "rgba")
+        cr = k.find("colorR") if split else None
+        cr = tuple(int(cr.get(c)) for c in "rgba") if cr is not None else cl
+        keys.append((inten, cl, cr))
+    return keys
+
+
+def tf_bake_cases(rng, reference_root):
+    cases = []
+    for i in range(40):
+        keys = _random_keys(rng, int(rng.integers(1, 12)))
+        width = int(rng.choice([2, 3, 256, 1000, 4096]))
+        gamma = 1.0 if i % 3 else float(rng.uniform(0.3, 3.0))
+        thr = (0.0, 1.0) if i % 4 else (float(rng.uniform(0, 0.3)), float(rng.uniform(0.6, 1.0)))
+        cases.append((keys, width, gamma, thr))
+    # keys exactly on texel values, coincident keys, descending ramps, one key, none
+    on = [float(np.float32(k) / np.float32(255)) for k in (0, 40, 41, 128, 200, 255)]
+    cases.append(([(on[0], (0, 0, 255, 0)), (on[1], (0, 0, 255, 0)), (on[2], (9, 9, 250, 3)),
+                   (on[3], (250, 10, 10, 200)), (on[4], (30, 200, 30, 255), (200, 30, 30, 0)),
+                   (on[5], (255, 255, 255, 255))], 256, 1.0, (0.0, 1.0)))
+    cases.append(([(0.25, (255, 0, 0, 255)), (0.25, (0, 255, 0, 10)), (0.75, (0, 0, 255, 128)),
+                   (0.75, (255, 255, 0, 64), (1, 2, 3, 4))], 4096, 1.0, (0.0, 1.0)))
+    cases.append(([(0.0, (255, 255, 255, 255)), (1.0, (0, 0, 0, 0))], 1000, 0.5, (0.2, 0.9)))
+    cases.append(([(0.6, (10, 20, 30, 40), (50, 60, 70, 80))], 256, 2.0, (0.0, 1.0)))
+    cases.append(([], 64, 1.0, (0.0, 1.0)))
+    tfdir = os.path.join(reference_root, "resource", "voreencore", "transferfuncs")
+    for name in ("nucleon.tfi", "walnut.tfi"):
+        keys = _tfi_keys(os.path.join(tfdir, name))
+        for width in (256, 4096):
+            cases.append((keys, width, 1.0, (0.0, 1.0)))
+    out = {"n": np.array(len(cases))}
+    for i, (keys, width, gamma, thr) in enumerate(cases):
+        table = oracle.ref_bake_tf(keys, width, gamma, thr, reference_root)
+        out[f"c{i}_intensity"] = np.array([k[0] for k in keys], np.float32)
+        out[f"c{i}_colors"] = np.array([list(k[1]) + list(k[2] if len(k) > 2 else k[1]) for k in keys],
+                                       np.uint8).reshape(-1, 8)
+        out[f"c{i}_params"] = np.array([width, gamma, thr[0], thr[1]], np.float64)
+        out[f"c{i}_table"] = table
+    return out
+
+
+def main(reference_root=None, only=None):
+    from oracle import build as obuild
+    reference_root = reference_root or obuild.DEFAULT_REFERENCE
+    if only == "tf_bake":
+        if oracle.ref_tf_lib(reference_root) is None:
+            raise SystemExit("reference sources not found: cannot build oracle/_ref")
+        np.savez_compressed(os.path.join(HERE, "tf_bake.npz"),
+                            **tf_bake_cases(np.random.default_rng(20261204), reference_root))
+        print("tf_bake.npz written to", HERE)
+        return
     ref = oracle.ref_lib(reference_root)
     if ref is None:
         raise SystemExit("reference sources not found: cannot build oracle/_ref")
@@ -103,8 +183,15 @@ def main(reference_root=None):
     np.savez_compressed(os.path.join(HERE, "trilinear.npz"), **trilinear_cases(ref, rng))
     np.savez_compressed(os.path.join(HERE, "camera.npz"), **camera_cases(ref, rng))
     np.savez_compressed(os.path.join(HERE, "iround.npz"), **iround_cases(ref, rng))
+    np.savez_compressed(os.path.join(HERE, "tf_bake.npz"),
+                        **tf_bake_cases(np.random.default_rng(20261204), reference_root))
     print("golden vectors written to", HERE)
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else None)
+    import argparse
+    ap = argparse.ArgumentParser()
+    ap.add_argument("reference_root", nargs="?", default=None)
+    ap.add_argument("--only", choices=["tf_bake"], default=None)
+    a = ap.parse_args()
+    main(a.reference_root, a.only)

@@ -30,7 +30,13 @@ def test_synthetic_headers(vrc_lib, tmp_path):
         '<MetaItem name="Offset"', '<MetaItem name="Ignored"').replace('<MetaItem name="Spacing"', '<MetaItem name="X"'))
     i = v.read_vvd_header(str(tmp_path / "b.vvd"))
     assert i.dtype == v.U16 and tuple(i.spacing) == (1.0, 1.0, 1.0) and tuple(i.offset) == (0.0, 0.0, 0.0)
-    assert (i.rwm_scale, i.rwm_offset) == (1.0, 0.0)
+    # no RealWorldMapping item: the denormalizing mapping of the format, as
+    # VvdVolumeReader sets it (vvdvolumereader.cpp:102-120)
+    assert (i.rwm_scale, i.rwm_offset) == (65535.0, 0.0)
+    for dt, scale in ((np.uint8, 255.0), (np.float32, 1.0)):
+        v.write_vvd(str(tmp_path / "d.vvd"), vox.astype(dt))
+        j = v.read_vvd_header(str(tmp_path / "d.vvd"))
+        assert (j.rwm_scale, j.rwm_offset) == (scale, 0.0)
     assert i.raw_path.decode() == str(tmp_path / "b.raw")
 
 
@@ -76,6 +82,11 @@ def test_shipped_volumes(vrc_lib, name):
         item = root.find(f".//MetaItem[@name='{key}']/value")
         if item is not None:
             assert tuple(field) == tuple(np.float32(item.get(k)) for k in "xyz")
+    rwm = root.find(".//MetaItem[@name='RealWorldMapping']/value")
+    if rwm is not None:
+        assert (info.rwm_scale, info.rwm_offset) == (np.float32(rwm.get("scale")), np.float32(rwm.get("offset")))
+    else:
+        assert (info.rwm_scale, info.rwm_offset) == ({"uint8": 255.0, "uint16": 65535.0, "float": 1.0}[fmt], 0.0)
     # Voreen's own VolumeMinMax against the raw voxels normalised as vrc normalises them
     mm = root.find(".//DerivedItem[@type='VolumeMinMax']")
     if mm is not None and os.path.exists(info.raw_path.decode()):

@@ -40,3 +40,32 @@ def test_bake_ramp_values(vrc_lib):
 def test_bake_rejects_unsorted(vrc_lib):
     with pytest.raises(v.VrcError):
         v.TransferFunction.bake([(0.5, (0, 0, 0, 0)), (0.2, (1, 1, 1, 1))], 256)
+
+
+def _golden_cases():
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "tf_bake.npz"))
+    for i in range(int(g["n"])):
+        inten, cols = g[f"c{i}_intensity"], g[f"c{i}_colors"]
+        width, gamma, lo, hi = g[f"c{i}_params"]
+        keys = [(float(inten[k]), tuple(int(c) for c in cols[k, :4]), tuple(int(c) for c in cols[k, 4:]))
+                for k in range(len(inten))]
+        yield i, keys, int(width), float(gamma), (float(lo), float(hi)), g[f"c{i}_table"]
+
+
+def test_bake_matches_reference_code(vrc_lib, orc):
+    """Pinned: the library's bake (vrc_tf_bake_keys) and the oracle's equal
+    the tables the reference's own TransFunc1DKeys::getMappingForValueUByte and
+    applyGammaToIntensity produce (tests/golden/tf_bake.npz, made by
+    tests/golden/make_golden.py from the Voreen sources), byte for byte; the
+    cases include split and coincident keys, keys on texel values, gamma,
+    thresholds and the keys of the sample transfer functions nucleon.tfi and
+    walnut.tfi."""
+    n = 0
+    for i, keys, width, gamma, thr, table in _golden_cases():
+        np.testing.assert_array_equal(orc.bake_tf(keys, width, gamma, thr), table, err_msg=f"oracle, case {i}")
+        if keys:  # the library's C ABI takes at least one key
+            np.testing.assert_array_equal(v.TransferFunction.bake(keys, width, gamma, thr), table,
+                                          err_msg=f"library, case {i}")
+        n += 1
+    assert n >= 49

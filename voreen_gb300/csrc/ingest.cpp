@@ -149,7 +149,13 @@ vrc_status vrc_vvd_read_header(const char* vvd_path, vrc_vvd_info* info) {
         info->spacing[i] = 1.f;
         info->offset[i] = 0.f;
     }
-    info->rwm_scale = 1.f;
+    // No RealWorldMapping item: VvdVolumeReader gives the volume the
+    // denormalizing mapping of its format (modules/core/io/vvdvolumereader.cpp:
+    // 102-120, RealWorldMapping::createDenormalizingMapping): scale = the
+    // largest value of an unsigned integer type, 1 for float, offset 0. The
+    // file's VolumeMinMax items are normalised values, which the mapping does
+    // not change.
+    info->rwm_scale = info->dtype == VRC_U8 ? 255.f : (info->dtype == VRC_U16 ? 65535.f : 1.f);
     info->rwm_offset = 0.f;
     const char* axes[3] = {"x", "y", "z"};
     if (meta_value(s, "Spacing", b, e))
