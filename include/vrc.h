@@ -397,6 +397,18 @@ typedef struct {
 /* Builds device descriptors and TF tables (allocating), orders requests
  * longest first and captures the launch sequence. Items are copied. */
 vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n, vrc_batch** out);
+/* As vrc_batch_create, with each request isolated from the others: a request
+ * that fails its checks (null or foreign handles, invalid parameters, a
+ * singular camera, an unsupported mode, or compositing / shading other than
+ * the first valid request's) is left out of the launch instead of failing
+ * the batch, and status[i] (n entries, required) receives each request's
+ * vrc_status -- VRC_OK for the requests that run. Returns an error only when
+ * no request is valid or on a batch-wide failure (allocation, capture).
+ * Stats report latency -1 for requests left out. The per-job isolation of
+ * SIMDRaycaster's job queue (modules/staging/processors/simdraycaster/
+ * simdraycaster.cpp:401-414) at request granularity. */
+vrc_status vrc_batch_create_isolated(vrc_context* ctx, const vrc_batch_item* items, int n, int* status,
+                                     vrc_batch** out);
 /* Enqueues one replay of the captured graph on the context's stream. */
 vrc_status vrc_batch_launch(vrc_batch* b);
 /* Synchronizes the context stream, then reports the last launch:

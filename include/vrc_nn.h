@@ -81,10 +81,21 @@ int vrc_nn_tile_alpha(const float* rgba, int H, int W, int tile, int ny, int nx,
  * C1 and n_split (Cout / n_split output channels per CTA, a multiple of 16, at
  * most 128). out_mode 0: BF16 NHWC with act (0 none, 1 ReLU, 2 leaky); 1:
  * FP32 NHWC (act applied likewise). d_err (nullable): set non-zero by a CTA
- * whose bounded wait gave up (the output is then incomplete). */
+ * whose bounded wait gave up (the output is then incomplete); the value names
+ * the wait (1 weights, 2 free stage, 3 filled stage, 4 free accumulator,
+ * 5 filled accumulator), and every non-zero value is a timeout
+ * (VRC_ERR_TIMEOUT). The CTA then waits for its own copies and MMAs in flight,
+ * frees its tensor memory and returns: no trap, and the next launch runs
+ * normally. */
 int vrc_nn_conv3x3_tc(const void* in0, int C0, const void* in1, int C1, int N, int H, int W, const void* wtc,
                       const float* bias, int Cout, int n_split, int act, void* out, int out_mode, int* d_err,
                       void* stream);
+/* Limit of vrc_nn_conv3x3_tc's pipeline waits in nanoseconds of the global
+ * timer, for launches made after the call (0 restores the default, 200 ms).
+ * The waits for a CTA's own copies and MMAs in flight keep their fixed
+ * 200 ms. A short limit makes the waits give up (d_err); used to exercise
+ * that path. Returns 0. */
+int vrc_nn_set_wait_limit(unsigned long long ns);
 /* w BF16 [Cout][3][3][C0 + C1] -> the shared-memory operand image that
  * vrc_nn_conv3x3_tc loads (same size): per output-channel slice, tap and
  * channel chunk, a block of rows swizzled as the tensor cores read them. */

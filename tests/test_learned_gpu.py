@@ -217,3 +217,40 @@ def test_infer_tc_matches_infer(vrc_lib):
     assert int(err.item()) == 0
     assert rel_err(b.cpu().numpy(), a.cpu().numpy()) < 1e-2
     assert float((a - b).abs().max()) < 5e-2
+
+
+def test_conv_tc_wait_timeout_is_reported_and_recovers(vrc_lib):
+    """The bounded-wait path of the tcgen05 convolution: with a pipeline wait
+    limit of 1 ns the waits give up, the kernel reports it through its error
+    word (a wait code 1..5, a timeout) and returns -- no trap, no hang, the
+    context stays usable -- and the next launch at the default limit is
+    bit-equal to a launch before it."""
+    from voreen_gb300.learned import _call, _p, _stream
+    rng = np.random.default_rng(77)
+    c0, cout, H, W = 64, 128, 64, 512
+    x, _ = bf16(rng.standard_normal((1, H, W, c0)))
+    w, _ = bf16(rng.standard_normal((cout, 3, 3, c0)) / np.sqrt(9 * c0))
+    b = torch.zeros(cout, dtype=torch.float32, device="cuda")
+    wtc = torch.empty_like(w)
+    _call("vrc_nn_weights_tc", _p(w), cout, c0, 0, 1, _p(wtc), _stream())
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def run():
+        err.zero_()
+        y = torch.full((1, H, W, cout), 3.0, dtype=torch.float32, device="cuda")
+        _call("vrc_nn_conv3x3_tc", _p(x), c0, None, 0, 1, H, W, _p(wtc), _p(b), cout, 1, 0, _p(y), 1, _p(err),
+              _stream())
+        torch.cuda.synchronize()
+        return y, int(err.item())
+
+    ref, e0 = run()
+    assert e0 == 0
+    try:
+        _call("vrc_nn_set_wait_limit", 1)
+        _, e1 = run()
+        assert 1 <= e1 <= 5, f"error word {e1}"
+    finally:
+        _call("vrc_nn_set_wait_limit", 0)
+    y, e2 = run()
+    assert e2 == 0
+    assert torch.equal(y, ref)

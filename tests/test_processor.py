@@ -232,3 +232,24 @@ def test_process_rejects_bad_settings_without_output(vrc_lib, prop, value, msg):
     r.process(analytic_entry_exit=True)
     assert msg in r.lastError and not r.outport.hasData()
     r.close()
+
+
+def test_autotuner_cache_round_trip_on_host(tmp_path):
+    """The tuner's JSON cache (no GPU needed): class keys group requests by
+    dtype, volume size and image size, and a loaded cache answers without
+    timing."""
+    import numpy as np
+    from voreen_gb300 import autotune
+    assert autotune.class_key(1, (512, 512, 512), 1920, 1080) == autotune.class_key(1, (500, 480, 512), 1900, 1000)
+    assert autotune.class_key(1, (512, 512, 512), 1920, 1080) != autotune.class_key(0, (512, 512, 512), 1920, 1080)
+    path = str(tmp_path / "t.json")
+    t = autotune.Autotuner(None, cache_path=path)
+    vox = np.zeros((64, 64, 64), np.uint16)
+    key = autotune.class_key(1, (64, 64, 64), 256, 256)
+    t.table[key] = {"tile_width": 16, "brick": 16, "skip_cell": 8, "kernel_ms": 0.5}
+    t.save()
+    u = autotune.Autotuner(None, cache_path=path)
+
+    class P:
+        width, height = 256, 256
+    assert u.tune(vox, (1, 1, 1), None, (0, 1), P()) == t.table[key]

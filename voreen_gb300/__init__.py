@@ -469,20 +469,31 @@ class Batch:
     """Many requests in one persistent launch replayed from a captured CUDA
     graph (vrc_batch_*). items: [(Volume, TransferFunction, RenderParams,
     out CUDA tensor, out_format)]; params must use analytic entry/exit and
-    share compositing and shading."""
+    share compositing and shading. Volume / TransferFunction may be None.
+    isolate=True (vrc_batch_create_isolated): invalid requests are left out
+    and `status` holds each request's vrc_status; otherwise any invalid
+    request raises."""
 
-    def __init__(self, ctx: Context, items):
+    def __init__(self, ctx: Context, items, isolate: bool = False):
         self.ctx = ctx
         self.items = list(items)
         arr = (_abi.BatchItem * len(self.items))()
         for i, (vol, tf, p, out, fmt) in enumerate(self.items):
-            arr[i].volume = vol.handle.value
-            arr[i].tf = tf.handle.value
+            arr[i].volume = vol.handle.value if vol is not None else None
+            arr[i].tf = tf.handle.value if tf is not None else None
             arr[i].params = p
-            arr[i].out = out.data_ptr()
+            arr[i].out = out.data_ptr() if out is not None else None
             arr[i].out_format = fmt
         self.handle = C.c_void_p()
-        _check(lib().vrc_batch_create(ctx.handle, arr, len(self.items), C.byref(self.handle)), ctx, "vrc_batch_create")
+        if isolate:
+            st = (C.c_int * len(self.items))()
+            _check(lib().vrc_batch_create_isolated(ctx.handle, arr, len(self.items), st, C.byref(self.handle)), ctx,
+                   "vrc_batch_create_isolated")
+            self.status = [int(x) for x in st]
+        else:
+            _check(lib().vrc_batch_create(ctx.handle, arr, len(self.items), C.byref(self.handle)), ctx,
+                   "vrc_batch_create")
+            self.status = [0] * len(self.items)
 
     def launch(self):
         _check(lib().vrc_batch_launch(self.handle), self.ctx, "vrc_batch_launch")

@@ -116,6 +116,7 @@ SIGNATURES = {
     "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
     "vrc_render_aux": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP, P(RenderStats)]),
     "vrc_batch_create": (C.c_int, [VP, P(BatchItem), C.c_int, P(VP)]),
+    "vrc_batch_create_isolated": (C.c_int, [VP, P(BatchItem), C.c_int, P(C.c_int), P(VP)]),
     "vrc_batch_launch": (C.c_int, [VP]),
     "vrc_batch_stats_get": (C.c_int, [VP, VP, P(BatchStats)]),
     "vrc_batch_destroy": (C.c_int, [VP]),
@@ -156,6 +157,7 @@ NN_SIGNATURES = {
     "vrc_nn_tile_alpha": [VP, _I, _I, _I, _I, _I, VP, VP],
     "vrc_nn_conv3x3_tc": [VP, _I, VP, _I, _I, _I, _I, VP, VP, _I, _I, _I, VP, _I, VP, VP],
     "vrc_nn_weights_tc": [VP, _I, _I, _I, _I, VP, VP],
+    "vrc_nn_set_wait_limit": [C.c_ulonglong],
 }
 
 # include/vrc_processor.h: the CudaRaycaster processor shim

@@ -40,6 +40,8 @@ class Autotuner:
         self.frames = frames
         self.cache_path = cache_path
         self.table: dict[str, dict] = {}
+        # per class, every candidate timed in this session: (tile_width, brick, skip_cell, kernel_ms)
+        self.timings: dict[str, list] = {}
         if cache_path and os.path.exists(cache_path):
             with open(cache_path) as f:
                 self.table = json.load(f)
@@ -71,6 +73,7 @@ class Autotuner:
         if key in self.table:
             return self.table[key]
         best = None
+        timed = self.timings.setdefault(key, [])
         bricks = BRICKS if tune_bricks else (32,)
         params.entry_exit_mode = EE_ANALYTIC
         for brick in bricks:
@@ -82,6 +85,7 @@ class Autotuner:
                 params.tile_width = tw
                 params.skip_cell_size = cell
                 ms = self._time(vol, tf, params)
+                timed.append((tw, brick, cell, ms))
                 if best is None or ms < best["kernel_ms"]:
                     best = {"tile_width": tw, "brick": brick, "skip_cell": cell, "kernel_ms": ms}
             tf.close()

@@ -13,7 +13,8 @@
 
 struct vrc_batch {
     vrc_context* ctx = nullptr;
-    int n = 0;
+    int n = 0;                              // requests in the launch
+    int n_items = 0;                        // items given (requests left out included)
     int compositing = 0, shading = 0;
     std::vector<int> order;                 // launch position -> item index
     vrc::BatchReq* d_reqs = nullptr;
@@ -61,33 +62,58 @@ void pick_level(const vrc_volume* vol, int want, const float** mn, const float**
 
 }  // namespace
 
-extern "C" {
+namespace {
 
-vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n, vrc_batch** out) {
-    if (!ctx || !items || !out || n < 1) return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: bad arguments");
+// Checks one request against the batch's rules; `first` is the first valid
+// request (its compositing and shading are the batch's), or null.
+vrc_status check_item(vrc_context* ctx, const vrc_batch_item& it, int i, const vrc_batch_item* first) {
+    if (!it.volume || !it.tf || !it.out || it.volume->ctx != ctx || it.tf->ctx != ctx)
+        return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: item " + std::to_string(i) + " is incomplete");
+    vrc_status st = vrc::check_params(ctx, &it.params);
+    if (st != VRC_OK) return st;
+    if (it.params.entry_exit_mode != VRC_EE_ANALYTIC)
+        return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: batched requests use analytic entry/exit");
+    if (it.params.compositing > VRC_ISO || it.params.classification != VRC_CLASSIFY_TF)
+        return bfail(ctx, VRC_ERR_UNSUPPORTED,
+                     "vrc_batch_create: batches take dvr / mip / iso compositing with TF classification");
+    if (first && (it.params.compositing != first->params.compositing || it.params.shading != first->params.shading))
+        return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: all requests must share compositing and shading");
+    if (it.out_format < VRC_OUT_RGBA8 || it.out_format > VRC_OUT_RGBA16)
+        return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: unknown output format");
+    vrc::MarchParams P;  // camera and region checks
+    return vrc::fill_params(ctx, it.volume, &it.params, P);
+}
+
+// status == nullptr: any invalid request fails the batch. Otherwise invalid
+// requests are left out and status[i] holds each request's vrc_status.
+vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items, int* status, vrc_batch** out) {
+    if (!ctx || !all || !out || n_items < 1) return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: bad arguments");
     *out = nullptr;
-    for (int i = 0; i < n; ++i) {
-        const vrc_batch_item& it = items[i];
-        if (!it.volume || !it.tf || !it.out || it.volume->ctx != ctx || it.tf->ctx != ctx)
-            return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: item " + std::to_string(i) + " is incomplete");
-        vrc_status st = vrc::check_params(ctx, &it.params);
-        if (st != VRC_OK) return st;
-        if (it.params.entry_exit_mode != VRC_EE_ANALYTIC)
-            return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: batched requests use analytic entry/exit");
-        if (it.params.compositing > VRC_ISO || it.params.classification != VRC_CLASSIFY_TF)
-            return bfail(ctx, VRC_ERR_UNSUPPORTED,
-                         "vrc_batch_create: batches take dvr / mip / iso compositing with TF classification");
-        if (it.params.compositing != items[0].params.compositing || it.params.shading != items[0].params.shading)
-            return bfail(ctx, VRC_ERR_UNSUPPORTED, "vrc_batch_create: all requests must share compositing and shading");
-        if (it.out_format < VRC_OUT_RGBA8 || it.out_format > VRC_OUT_RGBA16)
-            return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: unknown output format");
+    std::vector<int> valid;  // launch requests -> item index
+    const vrc_batch_item* first = nullptr;
+    std::string first_error;
+    for (int i = 0; i < n_items; ++i) {
+        const vrc_status st = check_item(ctx, all[i], i, first);
+        if (status) status[i] = st;
+        if (st != VRC_OK) {
+            if (!status) return st;
+            if (first_error.empty()) first_error = ctx->last_error;
+            continue;
+        }
+        if (!first) first = &all[i];
+        valid.push_back(i);
     }
+    if (valid.empty()) return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create: no valid request (" + first_error + ")");
+    const int n = (int)valid.size();
+    std::vector<vrc_batch_item> items(n);
+    for (int k = 0; k < n; ++k) items[k] = all[valid[k]];
     cudaError_t e = cudaSetDevice(ctx->device);
     if (e != cudaSuccess) return bfail(ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
     vrc_batch* b = new (std::nothrow) vrc_batch();
     if (!b) return VRC_ERR_OUT_OF_MEMORY;
     b->ctx = ctx;
     b->n = n;
+    b->n_items = n_items;
     b->compositing = items[0].params.compositing;
     b->shading = items[0].params.shading;
 
@@ -167,6 +193,7 @@ vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n
     std::vector<unsigned> prefix(n + 1, 0);
     for (int k = 0; k < n; ++k) {
         ordered[k] = reqs[b->order[k]];
+        b->order[k] = valid[b->order[k]];  // launch position -> item index
         const unsigned long long t = (unsigned long long)ordered[k].P.tiles_x * ordered[k].P.tiles_y;
         if (prefix[k] + t > 0xffffffffULL) {
             release(b);
@@ -215,6 +242,20 @@ vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n
     return VRC_OK;
 }
 
+}  // namespace
+
+extern "C" {
+
+vrc_status vrc_batch_create(vrc_context* ctx, const vrc_batch_item* items, int n, vrc_batch** out) {
+    return create_batch(ctx, items, n, nullptr, out);
+}
+
+vrc_status vrc_batch_create_isolated(vrc_context* ctx, const vrc_batch_item* items, int n, int* status,
+                                     vrc_batch** out) {
+    if (!status) return bfail(ctx, VRC_ERR_INVALID_ARG, "vrc_batch_create_isolated: null status array");
+    return create_batch(ctx, items, n, status, out);
+}
+
 vrc_status vrc_batch_launch(vrc_batch* b) {
     if (!b) return VRC_ERR_INVALID_ARG;
     cudaError_t e = cudaGraphLaunch(b->exec, b->ctx->stream);
@@ -231,6 +272,8 @@ vrc_status vrc_batch_stats_get(vrc_batch* b, float* latency_ms, vrc_batch_stats*
     if (e != cudaSuccess) return bfail(b->ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
     std::vector<float> lat(b->n);
     float mx = 0.f;
+    if (latency_ms)
+        for (int i = 0; i < b->n_items; ++i) latency_ms[i] = -1.f;  // requests left out of the launch
     for (int k = 0; k < b->n; ++k) {
         const unsigned long long end = h[3 + k];
         lat[k] = end > h[1] ? float(double(end - h[1]) * 1e-6) : 0.f;

@@ -852,12 +852,15 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
     }
 }
 
-// Resident CTAs per SM of one kernel instantiation for a dynamic shared
-// memory size, queried once per (device, size): the attribute call and the
-// occupancy query cost more host time than a frame's launch.
+// Resident CTAs per SM of one kernel for a dynamic shared memory size,
+// queried once per (kernel, device, size): the attribute call and the
+// occupancy query cost more host time than a frame's launch. Every march
+// instantiation has the same function type, so entries are keyed by the
+// kernel's address.
 template <typename K>
 cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
     struct Entry {
+        const void* fn;
         int dev;
         size_t smem;
         int per_sm;
@@ -867,9 +870,10 @@ cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
+    const void* fn = reinterpret_cast<const void*>(k);
     std::lock_guard<std::mutex> lock(m);
     for (const Entry& x : seen)
-        if (x.dev == dev && x.smem == smem) {
+        if (x.fn == fn && x.dev == dev && x.smem == smem) {
             *per_sm = x.per_sm;
             return cudaSuccess;
         }
@@ -880,7 +884,7 @@ cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
     int n = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem);
     if (e != cudaSuccess) return e;
-    seen.push_back(Entry{dev, smem, n});
+    seen.push_back(Entry{fn, dev, smem, n});
     *per_sm = n;
     return cudaSuccess;
 }

@@ -19,15 +19,18 @@
 // per tile rather than three times. Warp roles: 0 = TMA producer, 1 = MMA
 // issuer and tensor-memory owner, 2..5 = epilogue (tensor memory -> bias,
 // activation -> global). Two sets of R accumulators let the epilogue of one
-// tile overlap the MMAs of the next. Every wait is bounded (200 ms of
-// %globaltimer): on a timeout the CTA records an error code, waits for its own
-// copies and MMAs in flight (again bounded), frees its tensor memory and
-// returns.
+// tile overlap the MMAs of the next. Every wait is bounded by %globaltimer:
+// the pipeline waits by a host-settable limit (vrc_nn_set_wait_limit, 200 ms
+// by default); on a timeout the CTA records an error code, waits for its own
+// copies and MMAs in flight (bounded by a fixed 200 ms, whatever the pipeline
+// limit, so no copy or MMA is left writing to memory the CTA gives back),
+// frees its tensor memory and returns.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <mutex>
 
 #include "../../include/vrc_nn.h"
@@ -61,6 +64,7 @@ struct TcParams {
     const uint8_t* wtc;
     void* out;
     int* err;
+    unsigned long long wait_ns;  // limit of the pipeline waits
 };
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -81,12 +85,13 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Wait for the phase of parity `parity` to complete; false after WAIT_NS or
+// Wait for the phase of parity `parity` to complete; false after limit_ns or
 // once another role has given up (abort flag in shared memory). sleep_ns > 0
 // backs off between polls, leaving issue slots to the warps sharing the
 // scheduler (the epilogue warps share theirs with the producer and the MMA
 // issuer).
-__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, unsigned sleep_ns = 0) {
+__device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag, unsigned long long limit_ns,
+                          unsigned sleep_ns = 0) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = gtime();
     for (;;) {
@@ -95,7 +100,7 @@ __device__ bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_fla
             if (sleep_ns) __nanosleep(sleep_ns);
         }
         if (abort_flag && *abort_flag) return false;
-        if (gtime() - t0 > WAIT_NS) return false;
+        if (gtime() - t0 > limit_ns) return false;
     }
 }
 
@@ -241,7 +246,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int r = 0; ok && r < R + 2; ++r) {
                 for (int c = 0; c < p.nchunks; ++c, ++it) {
                     const int s = it % S;
-                    if (!mbar_wait(empty0 + 8 * s, ((it / S) & 1) ^ 1, s_abort)) {
+                    if (!mbar_wait(empty0 + 8 * s, ((it / S) & 1) ^ 1, s_abort, p.wait_ns)) {
                         record_error(p.err, s_abort, 2);
                         ok = false;
                         break;
@@ -255,8 +260,8 @@ __global__ void __launch_bounds__(THREADS, 1)
             }
         }
         // drain: the last copy into every stage, and the weights, have landed
-        for (int i = it - S < 0 ? 0 : it - S; i < it; ++i) mbar_wait(full0 + 8 * (i % S), (i / S) & 1, nullptr);
-        mbar_wait(wbar, 0, nullptr);
+        for (int i = it - S < 0 ? 0 : it - S; i < it; ++i) mbar_wait(full0 + 8 * (i % S), (i / S) & 1, nullptr, WAIT_NS);
+        mbar_wait(wbar, 0, nullptr, WAIT_NS);
     } else if (warp == 1 && lane == 0) {
         // ---- MMA issuer ----
         const uint32_t idesc = instr_desc(TM, p.n_tile);
@@ -264,7 +269,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         constexpr uint32_t LAYOUT = CK == 64 ? 2u : (CK == 32 ? 4u : 6u);
         const uint32_t b_block = (uint32_t)p.n_tile * RB;  // bytes of one (tap, chunk) block of weights
         const int nkb = p.nchunks;
-        bool ok = mbar_wait(wbar, 0, s_abort);
+        bool ok = mbar_wait(wbar, 0, s_abort, p.wait_ns);
         if (!ok) record_error(p.err, s_abort, 1);
         tc_fence_after();
         // descriptors are built once and advanced by adding (byte offset >> 4)
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int it = 0, tl = 0;
         for (int t = cta; ok && t < p.pix_tiles; t += ncta, ++tl) {
             const int acc = tl & 1;
-            if (!mbar_wait(tempty0 + 8 * acc, ((tl >> 1) & 1) ^ 1, s_abort)) {
+            if (!mbar_wait(tempty0 + 8 * acc, ((tl >> 1) & 1) ^ 1, s_abort, p.wait_ns)) {
                 record_error(p.err, s_abort, 4);
                 ok = false;
                 break;
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             for (int r = 0; ok && r < R + 2; ++r) {
                 for (int c = 0; c < nkb; ++c, ++it) {
                     const int s = it % S;
-                    if (!mbar_wait(full0 + 8 * s, (it / S) & 1, s_abort)) {
+                    if (!mbar_wait(full0 + 8 * s, (it / S) & 1, s_abort, p.wait_ns)) {
                         record_error(p.err, s_abort, 3);
                         ok = false;
                         break;
@@ -319,7 +324,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         }
         // every MMA issued by this thread has completed before tensor memory is freed
         mma_commit(dbar);
-        mbar_wait(dbar, 0, nullptr);
+        mbar_wait(dbar, 0, nullptr, WAIT_NS);
     } else if (warp >= 2) {
         // ---- epilogue: tensor memory -> bias + activation -> global ----
         const int q = warp & 3;  // this warp's tensor-memory lane quarter
@@ -328,7 +333,7 @@ __global__ void __launch_bounds__(THREADS, 1)
         int tl = 0;
         for (int t = cta; t < p.pix_tiles; t += ncta, ++tl) {
             const int acc = tl & 1;
-            if (!mbar_wait(tfull0 + 8 * acc, (tl >> 1) & 1, s_abort, 256)) {
+            if (!mbar_wait(tfull0 + 8 * acc, (tl >> 1) & 1, s_abort, p.wait_ns, 256)) {
                 record_error(p.err, s_abort, 5);
                 break;
             }
@@ -447,11 +452,18 @@ bool nhwc_map(CUtensorMap* m, const void* base, int N, int H, int W, int C, int 
 int chunk_of(int C0, int C1) { return (C0 % 64 == 0 && C1 % 64 == 0) ? 64 : ((C0 % 32 == 0 && C1 % 32 == 0) ? 32 : 16); }
 
 int status(cudaError_t e) { return e == cudaSuccess ? 0 : 2; }
+
+std::atomic<unsigned long long> g_wait_ns{WAIT_NS};
 uint32_t align1024(uint32_t x) { return (x + 1023u) & ~1023u; }
 
 }  // namespace
 
 extern "C" {
+
+int vrc_nn_set_wait_limit(unsigned long long ns) {
+    g_wait_ns.store(ns == 0 ? WAIT_NS : ns);
+    return 0;
+}
 
 int vrc_nn_weights_tc(const void* w, int Cout, int C0, int C1, int n_split, void* wtc, void* stream) {
     const int Cin = C0 + C1;
@@ -516,6 +528,7 @@ int vrc_nn_conv3x3_tc(const void* in0, int C0, const void* in1, int C1, int N, i
     p.wtc = static_cast<const uint8_t*>(wtc);
     p.out = out;
     p.err = d_err;
+    p.wait_ns = g_wait_ns.load();
     const size_t smem = fixed + (size_t)p.stages * p.a_stride;
     CUtensorMap m0, m1;
     if (!nhwc_map(&m0, in0, N, H, W, C0, CK)) return 2;
