@@ -208,10 +208,13 @@ def frame_parity(ctx, vol, tf, p, w, e_dev, x_dev, e_host, x_host, gpu_samples):
     ov = oracle.make_volume(w.voxels, w.spacing)
     otf = oracle.bake_tf(w.tf_keys, w.tf_width)
     t0 = time.perf_counter()
-    o32, s32, fh32 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 32)
-    o64, s64, fh64 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 64)
+    g32 = np.zeros((w.height, w.width), np.uint32)
+    g64 = np.zeros((w.height, w.width), np.uint32)
+    o32, s32, fh32 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 32, signature=g32)
+    o64, s64, fh64 = oracle.render(ov, otf, w.domain, op, e_host, x_host, 64, signature=g64)
     step = 1.0 / (max(w.dims) * w.sampling_rate)
-    r = parity.report(img, o32, s32, fh32, o64, s64, fh64, p.compositing, step, shaded=p.shading != v.SHADE_NONE)
+    r = parity.report(img, o32, s32, fh32, o64, s64, fh64, p.compositing, step, shaded=p.shading != v.SHADE_NONE,
+                      sig32=g32, sig64=g64)
     r.update({"frame": f"{w.width}x{w.height} full frame, RGBA32F", "bound": 1.0 / 255.0,
               "samples_equal_fp32": int(s32.sum()) == int(st.samples) == int(gpu_samples),
               "bit_equal_fp32": bool(np.array_equal(img.view(np.uint32), o32.view(np.uint32))),

@@ -67,7 +67,8 @@ def lib():
                                             C.c_void_p, C.c_void_p]
         for name in ("oracle_render_f32", "oracle_render_f64"):
             getattr(L, name).argtypes = [P(OrcVolume), P(OrcTF), P(OrcParams), C.c_void_p, C.c_void_p, C.c_int,
-                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+                                         C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.c_void_p]
         L.oracle_trilinear_f32.argtypes = [P(OrcVolume), C.c_void_p, C.c_int, C.c_void_p]
         L.oracle_brick_minmax.argtypes = [P(OrcVolume), C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         _lib = L
@@ -175,8 +176,10 @@ def entry_exit(inv_mvp: np.ndarray, width: int, height: int, quantize16: bool = 
 
 
 def render(vol: OrcVolume, tf_rgba: np.ndarray, domain, params: OrcParams, entry: np.ndarray, exit_pts: np.ndarray,
-           precision: int = 32, rows=None, nthreads: int = 0):
-    """Returns (rgba (H,W,4), samples (H,W) int32, first_hit (H,W))."""
+           precision: int = 32, rows=None, nthreads: int = 0, signature: np.ndarray | None = None):
+    """Returns (rgba (H,W,4), samples (H,W) int32, first_hit (H,W)).
+    signature: optional (H, W) uint32 array that receives each ray's decision
+    signature (a hash of the TF entries with alpha > 0 it picked, by sample)."""
     H, W = entry.shape[:2]
     tf_rgba = np.ascontiguousarray(tf_rgba, dtype=np.uint8)
     tf = OrcTF()
@@ -191,8 +194,10 @@ def render(vol: OrcVolume, tf_rgba: np.ndarray, domain, params: OrcParams, entry
     fh = np.full((H, W), -1, ft)
     r0, r1 = (0, H) if rows is None else rows
     fn = lib().oracle_render_f32 if precision == 32 else lib().oracle_render_f64
+    if signature is not None:
+        assert signature.dtype == np.uint32 and signature.shape == (H, W) and signature.flags.c_contiguous
     fn(C.byref(vol), C.byref(tf), C.byref(params), _ptr(e), _ptr(x), W, H, r0, r1, nthreads, _ptr(out),
-       _ptr(samples), _ptr(fh))
+       _ptr(samples), _ptr(fh), _ptr(signature) if signature is not None else None)
     return out, samples, fh
 
 

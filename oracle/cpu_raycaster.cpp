@@ -236,9 +236,20 @@ template <typename R> V3<R> phong(const Ctx<R>& c, V3<R> n, V3<R> pos, V3<R> col
     return out;
 }
 
+/* Decision signature of a ray: a hash of (loop index, TF entry) over the
+ * samples whose TF entry has alpha > 0 (for pre-integration, the table
+ * entry (front, back)). Two evaluations of a ray that pick the same entries
+ * at the same samples have the same signature; test infrastructure uses it
+ * to tell rounding differences from different discrete decisions. */
+inline uint32_t sig_mix(uint32_t h, uint32_t loop, uint32_t entry) {
+    h ^= loop * 0x9E3779B1u + entry * 0x85EBCA77u + 0x27D4EB2Fu;
+    h *= 0x01000193u;
+    return h ^ (h >> 15);
+}
+
 /* One ray. Returns the loop iteration count. */
 template <typename R>
-int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4], R* first_hit) {
+int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4], R* first_hit, uint32_t* sig_out) {
     const OrcParams* p = c.p;
     const OrcVolume* v = c.vol;
     const OrcTF* tf = c.tf;
@@ -269,6 +280,7 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
     R res[4] = {0, 0, 0, 0};
     R depth_t = R(-1);
     R max_int = R(0);
+    uint32_t sig = 0x811C9DC5u;
     bool finished = false;
     int loop = 0;
     for (loop = 0; !finished && loop < 255 * 255; ++loop) {
@@ -283,10 +295,12 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
             const float* e = p->preint + 4 * (size_t(i2) * size_t(pres) + size_t(i1));
             for (int k = 0; k < 4; ++k) col[k] = R(e[k]);
             last_int = cur;
+            if (e[3] > 0.f) sig = sig_mix(sig, uint32_t(loop), uint32_t(i2) * uint32_t(pres) + uint32_t(i1));
         } else {
             const int idx = tf_index<R>(rw_to_tf<R>(rw, lo, hi), tf->width);
             const uint8_t* e = tf->rgba + 4 * idx;
             for (int k = 0; k < 4; ++k) col[k] = R(e[k]) / R(255);
+            if (e[3] > 0) sig = sig_mix(sig, uint32_t(loop), uint32_t(idx));
         }
         if (col[3] > R(0)) {
             V3<R> g = v3<R>(0, 0, 0);
@@ -386,12 +400,14 @@ int march_ray(const Ctx<R>& c, V3<R> first, V3<R> last, int px, int py, R out[4]
     }
     out[0] = res[0]; out[1] = res[1]; out[2] = res[2]; out[3] = res[3];
     if (first_hit) *first_hit = depth_t;
+    if (sig_out) *sig_out = sig;
     return loop;
 }
 
 template <typename R>
 void render(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p, const float* entry, const float* exitp,
-            int W, int H, int row_begin, int row_end, int nthreads, R* out, int32_t* samples, R* first_hit) {
+            int W, int H, int row_begin, int row_end, int nthreads, R* out, int32_t* samples, R* first_hit,
+            uint32_t* sig) {
     Ctx<R> c;
     c.vol = vol; c.tf = tf; c.p = p; c.entry = entry; c.W = W; c.H = H;
     const int maxdim = std::max(vol->dims[0], std::max(vol->dims[1], vol->dims[2]));
@@ -421,15 +437,18 @@ void render(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p, const flo
             const float* l = exitp + 4 * pix;
             R res[4] = {0, 0, 0, 0};
             R fh = R(-1);
+            uint32_t sg = 0;
             int n = 0;
             const bool bg = f[0] == 0.f && f[1] == 0.f && f[2] == 0.f && f[3] == 0.f &&
                             l[0] == 0.f && l[1] == 0.f && l[2] == 0.f && l[3] == 0.f;
             if (!bg) {
-                n = march_ray<R>(c, v3<R>(R(f[0]), R(f[1]), R(f[2])), v3<R>(R(l[0]), R(l[1]), R(l[2])), x, y, res, &fh);
+                n = march_ray<R>(c, v3<R>(R(f[0]), R(f[1]), R(f[2])), v3<R>(R(l[0]), R(l[1]), R(l[2])), x, y, res, &fh,
+                                 &sg);
             }
             for (int k = 0; k < 4; ++k) out[4 * pix + k] = res[k];
             if (samples) samples[pix] = n;
             if (first_hit) first_hit[pix] = fh;
+            if (sig) sig[pix] = sg;
         }
     }
 }
@@ -631,14 +650,14 @@ void oracle_entry_exit_box(const double* m, int W, int H, int quantize16, const 
 
 void oracle_render_f32(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p, const float* entry,
                        const float* exitp, int W, int H, int row_begin, int row_end, int nthreads, float* out,
-                       int32_t* samples, float* first_hit) {
-    render<float>(vol, tf, p, entry, exitp, W, H, row_begin, row_end, nthreads, out, samples, first_hit);
+                       int32_t* samples, float* first_hit, uint32_t* signature) {
+    render<float>(vol, tf, p, entry, exitp, W, H, row_begin, row_end, nthreads, out, samples, first_hit, signature);
 }
 
 void oracle_render_f64(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p, const float* entry,
                        const float* exitp, int W, int H, int row_begin, int row_end, int nthreads, double* out,
-                       int32_t* samples, double* first_hit) {
-    render<double>(vol, tf, p, entry, exitp, W, H, row_begin, row_end, nthreads, out, samples, first_hit);
+                       int32_t* samples, double* first_hit, uint32_t* signature) {
+    render<double>(vol, tf, p, entry, exitp, W, H, row_begin, row_end, nthreads, out, samples, first_hit, signature);
 }
 
 void oracle_trilinear_f32(const OrcVolume* vol, const float* pos, int n, float* out) {

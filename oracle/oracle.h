@@ -106,16 +106,19 @@ void oracle_entry_exit_box(const double* inv_mvp, int width, int height, int qua
 /* Full-frame march. entry/exit: W*H float4. out: W*H float4 (RGBA, not
  * clamped). samples_out (nullable): per-pixel loop iteration count.
  * first_hit_out (nullable): per-pixel first-hit ray parameter (-1 if none).
+ * signature_out (nullable): per-pixel hash of (loop index, TF entry) over the
+ * samples whose TF entry has alpha > 0 -- equal in two precisions exactly
+ * when they take the same TF-entry decisions at the same samples.
  * row_begin/row_end restrict the rows marched (others untouched).
  * nthreads <= 0 uses all OpenMP threads. */
 void oracle_render_f32(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p,
                        const float* entry, const float* exit_pts, int width, int height,
                        int row_begin, int row_end, int nthreads,
-                       float* out, int32_t* samples_out, float* first_hit_out);
+                       float* out, int32_t* samples_out, float* first_hit_out, uint32_t* signature_out);
 void oracle_render_f64(const OrcVolume* vol, const OrcTF* tf, const OrcParams* p,
                        const float* entry, const float* exit_pts, int width, int height,
                        int row_begin, int row_end, int nthreads,
-                       double* out, int32_t* samples_out, double* first_hit_out);
+                       double* out, int32_t* samples_out, double* first_hit_out, uint32_t* signature_out);
 
 /* Single trilinear lookup at a (clamped) voxel position, FP32 path. Used to
  * check the restatement against the reference's compiled VolumeRAM code. */

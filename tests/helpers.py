@@ -48,6 +48,7 @@ class Case:
             entry, exit_pts = oracle_entry_exit(self.vol.desc, params)
         self.entry, self.exit = entry, exit_pts
         self.ovol = oracle.make_volume(self.vox, spacing, offset, rwm)
+        self.sig = {}  # precision -> the last oracle render's decision signatures
 
     def gpu(self, out_format=v.OUT_RGBA32F, **over):
         p = self.params
@@ -62,8 +63,16 @@ class Case:
     def oracle(self, precision=32, rows=None, entry=None, exit_pts=None, preint_table=None):
         e = self.entry if entry is None else entry
         x = self.exit if exit_pts is None else exit_pts
-        return oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params, preint_table=preint_table),
-                             e, x, precision, rows)
+        sig = np.zeros(e.shape[:2], np.uint32)
+        r = oracle.render(self.ovol, self.tf_rgba, self.domain, oracle_params(self.params, preint_table=preint_table),
+                          e, x, precision, rows, signature=sig)
+        self.sig[precision] = sig
+        return r
+
+    @property
+    def sigs(self):
+        """(FP32, FP64) decision signatures of the last oracle renders."""
+        return self.sig.get(32), self.sig.get(64)
 
 
 sample_index = parity.sample_index
@@ -71,12 +80,12 @@ decision_divergent = parity.decision_divergent
 
 
 def assert_fp64_parity(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded=False, max_div_frac=2e-3,
-                       tol=TOL, label=None):
+                       tol=TOL, label=None, sigs=(None, None)):
     """max |d| <= tol on every ray where FP32 and FP64 make the same discrete
     decisions. A ray above tol is waived only if its decisions diverge, and
     the waived rays (counted, with their max |d| reported) must be a tiny
     fraction of the hit rays. Returns the parity report."""
-    r = parity.report(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded, tol)
+    r = parity.report(gpu_img, o32, s32, fh32, o64, s64, fh64, comp, step, shaded, tol, sigs[0], sigs[1])
     if label is not None:
         REPORTS.append((label, r))
     hits = max(1, r["hit_rays"])

@@ -98,15 +98,17 @@ def test_batch_requests_match_oracle(ctx, shading):
         p_buf.entry_exit_mode = v.EE_BUFFERS
         e, x = v.entry_exit(ctx, vol, p_buf)
         ov = oracle.make_volume(vox)
-        o32, s32, fh32 = oracle.render(ov, rgba, dom, oracle_params(p), e, x, 32)
-        assert (got[..., 3] > 0).mean() > 0.05
+        g32 = np.zeros(e.shape[:2], np.uint32)
+        g64 = np.zeros(e.shape[:2], np.uint32)
+        o32, s32, fh32 = oracle.render(ov, rgba, dom, oracle_params(p), e, x, 32, signature=g32)
+        assert (got[..., 3] > 0).mean() > 0.01
         if shading == v.SHADE_NONE:
             np.testing.assert_array_equal(got.view(np.uint32), o32.view(np.uint32))
         else:
             assert np.abs(got - o32).max() <= 1e-4
-        o64, s64, fh64 = oracle.render(ov, rgba, dom, oracle_params(p), e, x, 64)
+        o64, s64, fh64 = oracle.render(ov, rgba, dom, oracle_params(p), e, x, 64, signature=g64)
         assert_fp64_parity(got, o32, s32, fh32, o64, s64, fh64, v.DVR, 1.0 / (max(vox.shape) * p.sampling_rate),
-                           shaded=shading != v.SHADE_NONE)
+                           shaded=shading != v.SHADE_NONE, sigs=(g32, g64))
     b.close()
 
 

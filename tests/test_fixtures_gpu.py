@@ -77,7 +77,9 @@ def _check(ctx, vol, tf, tf_rgba, domain, vox, spacing, offset, rwm, p, label, e
     img, st = v.render(ctx, vol, tf, p, entry, exit_pts, v.OUT_RGBA32F)
     ov = oracle.make_volume(vox, spacing, offset, rwm)
     op = oracle_params(p, preint_table=preint)
-    o32, s32, fh32 = oracle.render(ov, tf_rgba, domain, op, entry, exit_pts, 32)
+    g32 = np.zeros(entry.shape[:2], np.uint32)
+    g64 = np.zeros(entry.shape[:2], np.uint32)
+    o32, s32, fh32 = oracle.render(ov, tf_rgba, domain, op, entry, exit_pts, 32, signature=g32)
     assert st.samples == s32.sum() and s32.sum() > 0
     if p.shading == v.SHADE_NONE:
         np.testing.assert_array_equal(_bits(img), _bits(o32))
@@ -85,9 +87,10 @@ def _check(ctx, vol, tf, tf_rgba, domain, vox, spacing, offset, rwm, p, label, e
         assert np.abs(img - o32).max() <= 1e-4
     assert (img[..., 3] > 0).mean() > 0.02
     if preint is None:
-        o64, s64, fh64 = oracle.render(ov, tf_rgba, domain, op, entry, exit_pts, 64)
+        o64, s64, fh64 = oracle.render(ov, tf_rgba, domain, op, entry, exit_pts, 64, signature=g64)
         assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, p.compositing,
-                           1.0 / (max(vox.shape) * p.sampling_rate), shaded=p.shading != v.SHADE_NONE, label=label)
+                           1.0 / (max(vox.shape) * p.sampling_rate), shaded=p.shading != v.SHADE_NONE, label=label,
+                           sigs=(g32, g64))
     return img
 
 

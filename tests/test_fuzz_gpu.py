@@ -89,4 +89,4 @@ def test_random_case_matches_oracle(ctx, seed):
         np.testing.assert_array_equal(_bits(img), _bits(o32))
     if comp in (v.DVR, v.MIP, v.ISO):
         o64, s64, fh64 = c.oracle(64)
-        assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, shaded=shaded)
+        assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, shaded=shaded, sigs=c.sigs)

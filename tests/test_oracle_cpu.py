@@ -82,3 +82,37 @@ def test_fp32_vs_fp64_compositing_modes(comp, gamma):
                                               iso_value=0.3)
     assert s32.sum() > 10000
     assert_fp64_parity(o32, o32, s32, f32, o64, s64, f64, comp, 1.0 / (max(w.dims) * w.sampling_rate))
+
+
+def test_decision_signature_explains_fp32_fp64_gaps():
+    """The oracle's per-ray decision signature: on the reference's
+    CPURaycaster workspace (nucleon, its 12-key TF and camera) FP32 and FP64
+    differ by more than 1/255 only on rays whose decisions differ -- here a
+    TF entry picked on the other side of an index rounding tie."""
+    import json
+    import os
+    from oracle import camera as ocam
+    from oracle import parity
+    fix = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "fixtures")
+    case = json.load(open(os.path.join(fix, "cpuraycaster_vws.json")))
+    vox = np.fromfile(os.path.join(fix, "nucleon.raw"), np.uint8).reshape(41, 41, 41)
+    sp, off = (0.04878049,) * 3, (-0.99999994,) * 3
+    cam = case["camera"]
+    W, H = case["canvas"]
+    inv = ocam.inverse_mvp(cam["position"], cam["focus"], cam["up"], cam["fovy"], cam["near"], cam["far"], W, H,
+                           (41, 41, 41), sp, off)
+    e, x = oracle.entry_exit(inv, W, H, True)
+    t = [c for c in case["raycasters"] if c["classification"] == "transfer-function"][0]["tf"]
+    tf = oracle.bake_tf([(k[0], tuple(k[1]), tuple(k[2])) for k in t["keys"]], t["width"])
+    ov = oracle.make_volume(vox, sp, off, (255.0, 0.0))
+    op = oracle.make_params(sampling_rate=2.0)
+    g32, g64 = np.zeros((H, W), np.uint32), np.zeros((H, W), np.uint32)
+    o32, s32, f32 = oracle.render(ov, tf, tuple(t["domain"]), op, e, x, 32, signature=g32)
+    o64, s64, f64 = oracle.render(ov, tf, tuple(t["domain"]), op, e, x, 64, signature=g64)
+    step = 1.0 / (41 * 2.0)
+    d = np.abs(o32.astype(np.float64) - o64).max(axis=-1)
+    div = parity.decision_divergent(o32, s32, f32, o64, s64, f64, v.DVR, step, sig32=g32, sig64=g64)
+    assert (d > 1.0 / 255.0).any()               # this view has such rays
+    assert not (d[~div] > 1.0 / 255.0).any()      # and every one of them diverges in its decisions
+    assert div.sum() < 0.002 * (s32 > 0).sum()    # a handful of the hit rays
+    assert (g32[s32 > 0] != 0x811C9DC5).any()     # the signatures record the entries taken

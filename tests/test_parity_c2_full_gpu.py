@@ -39,7 +39,7 @@ def test_c2_phong_dvr_full_frame(c2):
     assert np.abs(img - o32).max() <= 1e-4
     o64, s64, fh64 = c.oracle(64)
     assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, v.DVR, c.step, shaded=True,
-                       label="C2 512^3 u16 1920x1080 Phong DVR (full frame)")
+                       label="C2 512^3 u16 1920x1080 Phong DVR (full frame)", sigs=c.sigs)
 
 
 def test_c2_mip_full_frame(c2):
@@ -51,4 +51,4 @@ def test_c2_mip_full_frame(c2):
     np.testing.assert_array_equal(np.ascontiguousarray(img).view(np.uint32), o32.view(np.uint32))
     o64, s64, fh64 = c.oracle(64)
     assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, v.MIP, c.step,
-                       label="C2 512^3 u16 1920x1080 MIP (full frame)")
+                       label="C2 512^3 u16 1920x1080 MIP (full frame)", sigs=c.sigs)

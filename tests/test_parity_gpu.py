@@ -32,7 +32,7 @@ def test_config1_full_size_bit_exact(ctx):
     np.testing.assert_array_equal(_bits(img), _bits(o32))
     assert st.samples == s32.sum()
     o64, s64, fh64 = c.oracle(64)
-    assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, v.DVR, c.step, label="C1 128^3 u8 512x512 DVR")
+    assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, v.DVR, c.step, label="C1 128^3 u8 512x512 DVR", sigs=c.sigs)
 
 
 @pytest.mark.parametrize("comp", [v.DVR, v.MIP, v.ISO])
@@ -46,7 +46,7 @@ def test_ct_shells_unshaded_bit_exact(ctx, comp):
     np.testing.assert_array_equal(_bits(img), _bits(o32))
     assert st.samples == s32.sum()
     o64, s64, fh64 = c.oracle(64)
-    assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, label=f"shells 96x80x72 mode {comp}")
+    assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, label=f"shells 96x80x72 mode {comp}", sigs=c.sigs)
 
 
 @pytest.mark.parametrize("comp", [v.DVR, v.ISO])
@@ -65,7 +65,7 @@ def test_ct_shells_phong(ctx, comp):
     assert np.abs(img - o32).max() <= 1e-4
     o64, s64, fh64 = c.oracle(64)
     assert_fp64_parity(img, o32, s32, fh32, o64, s64, fh64, comp, c.step, shaded=True,
-                       label=f"shells 96x96x80 Phong mode {comp}")
+                       label=f"shells 96x96x80 Phong mode {comp}", sigs=c.sigs)
 
 
 def test_float_volume_and_rwm(ctx):
