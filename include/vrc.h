@@ -177,16 +177,21 @@ vrc_status vrc_volume_set_cache_upload_budget(vrc_volume* vol, size_t bytes_per_
  * vrc_volume_cache_info: bricks held by the cache, bricks the last TF could
  * reach, and bricks the last tracked render read without a slot. */
 vrc_status vrc_volume_cache_info(const vrc_volume* vol, long long* cached, long long* reachable, long long* missed);
-/* Level of detail for a VRC_PLACE_HOST pool: a device-resident
- * half-resolution level (each voxel the mean of 2x2x2 voxels, clamped at
- * the volume's edges: VolumeOctree's HalfSampleMean parent bricks,
- * volumeoctree.cpp:188-202), built on the first enable. While enabled, a
- * brick without a cache slot is sampled from that level at the same
- * texture-space point instead of from the host pool -- the coarser node
- * Voreen's octree raycaster reads where a brick is not on the GPU -- so
- * frames stay fast and approach the full-resolution image as refinement
- * fills the cache. VRC_ERR_UNSUPPORTED for device-resident pools. */
-vrc_status vrc_volume_set_lod(vrc_volume* vol, int enable);
+/* Level of detail for a VRC_PLACE_HOST pool: a device-resident coarser
+ * level of the pyramid VolumeOctree builds (each voxel the mean of 2x2x2
+ * voxels of the level above, clamped at that level's edges: HalfSampleMean
+ * parent bricks, volumeoctree.cpp:188-202). `level` k = 1 is half
+ * resolution, k = 2 quarter, ..., up to VRC_MAX_LOD_LEVEL; 0 turns the level
+ * of detail off. Built on enable (again when k changes; only level k stays
+ * on the device, 8^-k of the volume). While enabled, a brick without a cache
+ * slot is sampled from level k at the same texture-space point instead of
+ * from the host pool -- the coarser node Voreen's octree raycaster reads
+ * where a brick is not on the GPU -- so frames stay fast, degrade by level
+ * when the cache budget is below the view's working set, and approach the
+ * full-resolution image as refinement fills the cache. VRC_ERR_UNSUPPORTED
+ * for device-resident pools. */
+#define VRC_MAX_LOD_LEVEL 6
+vrc_status vrc_volume_set_lod(vrc_volume* vol, int level);
 
 /* ---- volume ingest (.vvd) ------------------------------------------------
  * Voreen's .vvd volume files (VvdVolumeReader, modules/core/io/vvdvolumereader.cpp,

@@ -214,3 +214,38 @@ def test_random_cache_settings_are_exact(ctx, seed):
         b, sb = v.render(ctx, dev, tf, p, None, None, v.OUT_RGBA32F)
         np.testing.assert_array_equal(_bits(a), _bits(b))
         assert sa.samples == sb.samples
+
+
+@pytest.mark.parametrize("level,dims,brick", [(2, (96, 80, 64), 16), (3, (96, 72, 40), 8), (2, (76, 42, 58), 8)])
+def test_deeper_lod_level_equals_oracle_pyramid(ctx, level, dims, brick):
+    """Level k of the pyramid: with no cache every sample comes from the
+    2^-k level, which must equal the oracle's render of the volume
+    half-sampled k times (HalfSampleMean applied level by level, each with
+    its own edge clamping) at 2^k times the sampling rate -- the same step in
+    texture space (the largest dimension is a multiple of 2^k). Switching
+    the level rebuilds it; level 1 afterwards is the half-resolution level
+    again."""
+    w = synth.config2(size=dims, image=(120, 96))
+    host = v.Volume(ctx, w.voxels, w.spacing, placement=v.PLACE_HOST, brick_size=brick)
+    tf_rgba = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    tf = v.TransferFunction(ctx, tf_rgba, w.domain)
+    host.set_cache_limit(0)
+    p = w.params(shading=v.SHADE_NONE, empty_space_skipping=0)
+    e, x = v.entry_exit(ctx, host, p)
+    for k in (level, 1):
+        host.set_lod(k)
+        img, st = v.render(ctx, host, tf, p, e, x, v.OUT_RGBA32F)
+        vox = w.voxels
+        for _ in range(k):
+            vox = oracle.half_sample_mean(vox)
+        ov = oracle.make_volume(np.ascontiguousarray(vox), w.spacing)
+        op = oracle_params(p)
+        op.sampling_rate = (2 ** k) * p.sampling_rate
+        o32, s32, _ = oracle.render(ov, tf_rgba, w.domain, op, e, x, 32)
+        np.testing.assert_array_equal(_bits(img), _bits(o32), err_msg=f"level {k}")
+        assert st.samples == s32.sum()
+        assert (img[..., 3] > 0).mean() > 0.02
+    host.set_lod(0)
+    with pytest.raises(v.VrcError):
+        host.set_lod(7)
+    host.close()

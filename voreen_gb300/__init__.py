@@ -200,10 +200,12 @@ class Volume:
         _check(lib().vrc_volume_set_cache_upload_budget(self.handle, int(nbytes)), self.ctx,
                "vrc_volume_set_cache_upload_budget")
 
-    def set_lod(self, enable: bool = True):
-        """Sample bricks without a cache slot from a device-resident
-        half-resolution level (host-placed pools only)."""
-        _check(lib().vrc_volume_set_lod(self.handle, 1 if enable else 0), self.ctx, "vrc_volume_set_lod")
+    def set_lod(self, level=True):
+        """Sample bricks without a cache slot from a device-resident coarser
+        level (host-placed pools only): True or 1 = half resolution, k = the
+        level 2^-k of the 2x2x2-mean pyramid, False or 0 = off."""
+        k = int(level) if not isinstance(level, bool) else (1 if level else 0)
+        _check(lib().vrc_volume_set_lod(self.handle, k), self.ctx, "vrc_volume_set_lod")
 
     def close(self):
         if self.handle:

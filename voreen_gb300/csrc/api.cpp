@@ -283,6 +283,12 @@ vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* des
     const int bpv = vrc::dtype_bytes(desc->dtype);
     const size_t nvox = (size_t)desc->dims[0] * desc->dims[1] * desc->dims[2];
     const size_t brick_bytes = (size_t)L.nbricks() * L.brick_stride * bpv;
+    // the march indexes bricks and skip cells with 32-bit integers (2^31
+    // bricks of 8^3 voxels are 1.1e12 voxels, more than any memory holds)
+    if (L.nbricks() >= (1LL << 31)) {
+        delete v;
+        return fail(ctx, VRC_ERR_UNSUPPORTED, "vrc_volume_upload: more than 2^31 bricks");
+    }
     void* staging = nullptr;
     const void* registered = nullptr;  // caller's host voxels registered for direct device reads
     cudaError_t e = cudaSuccess;
@@ -335,6 +341,10 @@ vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* des
         vrc_cell_level& lv = v->levels[li];
         lv.C = C;
         for (int i = 0; i < 3; ++i) lv.nc[i] = (desc->dims[i] + C - 1) / C;
+        if (lv.count() >= (1LL << 32)) {  // beyond the march's 32-bit cell index: skip by bricks
+            lv.C = 0;
+            continue;
+        }
         if ((e = cudaMalloc((void**)&lv.d_min, lv.count() * sizeof(float))) != cudaSuccess ||
             (e = cudaMalloc((void**)&lv.d_max, lv.count() * sizeof(float))) != cudaSuccess)
             return cleanup(VRC_ERR_OUT_OF_MEMORY, "vrc_volume_upload: cell table allocation failed");
@@ -460,35 +470,57 @@ vrc_status vrc_volume_cache_info(const vrc_volume* v, long long* cached, long lo
     return VRC_OK;
 }
 
-vrc_status vrc_volume_set_lod(vrc_volume* v, int enable) {
+vrc_status vrc_volume_set_lod(vrc_volume* v, int level) {
     if (!v || !v->ctx) return VRC_ERR_INVALID_ARG;
     vrc_context* ctx = v->ctx;
+    if (level < 0 || level > VRC_MAX_LOD_LEVEL)
+        return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_volume_set_lod: level out of range");
     if (!v->h_bricks) return fail(ctx, VRC_ERR_UNSUPPORTED, "vrc_volume_set_lod: the volume's brick pool is in device memory");
-    if (enable && !v->d_lod) {
+    if (level > 0 && (!v->d_lod || v->lod_level != level)) {
+        // level k: the 2x2x2 mean of level k - 1 (level 0 = the host pool),
+        // each intermediate level freed once the next is built
         VRC_CUDA(ctx, cudaSetDevice(ctx->device));
-        BrickLayout& H = v->lod_L;
-        H = v->L;
-        for (int i = 0; i < 3; ++i) {
-            H.dims[i] = (v->L.dims[i] + 1) / 2;
-            H.nb[i] = (H.dims[i] + H.B - 1) / H.B;
-        }
         const int bpv = vrc::dtype_bytes(v->desc.dtype);
-        const size_t n1 = (size_t)H.dims[0] * H.dims[1] * H.dims[2];
-        void* lin = nullptr;
-        cudaError_t e = cudaMalloc(&lin, n1 * bpv);
-        if (e == cudaSuccess) e = cudaMalloc(&v->d_lod, (size_t)H.nbricks() * H.brick_stride * bpv);
-        if (e == cudaSuccess) e = vrc::launch_half_sample(v->d_bricks, v->desc.dtype, v->L, H.dims, lin, ctx->stream);
-        if (e == cudaSuccess) e = vrc::launch_brick_build(lin, v->desc.dtype, H, v->d_lod, ctx->stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-        cudaFree(lin);
-        if (e != cudaSuccess) {
+        if (v->d_lod) {
+            v->bytes -= (size_t)v->lod_L.nbricks() * v->lod_L.brick_stride * bpv;
             cudaFree(v->d_lod);
             v->d_lod = nullptr;
+            v->lod_level = 0;
+        }
+        const void* src = v->d_bricks;
+        BrickLayout srcL = v->L;
+        void* prev = nullptr;  // the device level being halved (never the pool)
+        cudaError_t e = cudaSuccess;
+        for (int k = 1; k <= level && e == cudaSuccess; ++k) {
+            BrickLayout H = srcL;
+            for (int i = 0; i < 3; ++i) {
+                H.dims[i] = (srcL.dims[i] + 1) / 2;
+                H.nb[i] = (H.dims[i] + H.B - 1) / H.B;
+            }
+            const size_t n1 = (size_t)H.dims[0] * H.dims[1] * H.dims[2];
+            void* lin = nullptr;
+            void* bricks = nullptr;
+            e = cudaMalloc(&lin, n1 * bpv);
+            if (e == cudaSuccess) e = cudaMalloc(&bricks, (size_t)H.nbricks() * H.brick_stride * bpv);
+            if (e == cudaSuccess) e = vrc::launch_half_sample(src, v->desc.dtype, srcL, H.dims, lin, ctx->stream);
+            if (e == cudaSuccess) e = vrc::launch_brick_build(lin, v->desc.dtype, H, bricks, ctx->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+            cudaFree(lin);
+            cudaFree(prev);
+            prev = bricks;
+            src = bricks;
+            srcL = H;
+        }
+        if (e != cudaSuccess) {
+            cudaFree(prev);
             return cuda_fail(ctx, e, "vrc_volume_set_lod");
         }
-        v->bytes += (size_t)H.nbricks() * H.brick_stride * bpv;
+        v->d_lod = prev;
+        v->lod_L = srcL;
+        v->lod_level = level;
+        v->bytes += (size_t)srcL.nbricks() * srcL.brick_stride * bpv;
     }
-    v->lod_on = enable != 0;
+    v->lod_on = level > 0;
     return VRC_OK;
 }
 

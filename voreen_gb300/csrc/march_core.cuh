@@ -162,6 +162,16 @@ __device__ __forceinline__ float tri_raw(const typename Vox<DT>::T* __restrict__
     return __fmaf_rn(fz, y1 - y0, y0);
 }
 
+// tri_raw on voxel values already in registers (v<x><y><z>), the same
+// arithmetic in the same order.
+__device__ __forceinline__ float tri_regs(float v000, float v100, float v010, float v110, float v001, float v101,
+                                          float v011, float v111, float fx, float fy, float fz) {
+    const float x00 = __fmaf_rn(fx, v100 - v000, v000), x10 = __fmaf_rn(fx, v110 - v010, v010);
+    const float x01 = __fmaf_rn(fx, v101 - v001, v001), x11 = __fmaf_rn(fx, v111 - v011, v011);
+    const float y0 = __fmaf_rn(fy, x10 - x00, x00), y1 = __fmaf_rn(fy, x11 - x01, x01);
+    return __fmaf_rn(fz, y1 - y0, y0);
+}
+
 // Start of brick `brick`: in the pool directly, or, for a host-resident pool
 // with a device cache (brick_slot != nullptr), in the cache slot the table
 // names. A brick the cache does not hold (slot -1) is read in the mapped
@@ -532,6 +542,10 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
     float t = 0.f;
     float hit_t = -1.f, hit_g = 0.f;  // first sample with alpha > 0 (auxiliary output)
     long long marked = -1;             // last brick recorded as read (cache refinement)
+    // the brick of the last fetched sample and its start: consecutive samples
+    // mostly stay in one brick
+    int cached_brick = -1;
+    const T* cached_base = nullptr;
     bool finished = false;
     int loop = 0;
     while (!finished && loop < LOOP_CAP) {
@@ -548,15 +562,16 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
             // empty fine cell (8^3 by default); both words are loaded at once.
             float tsafe = 0.f;
             bool empty = false;
+            // cell and brick indices fit 32 bits (checked when the volume is uploaded)
             const int fcx = ix >> P.cshift, fcy = iy >> P.cshift, fcz = iz >> P.cshift;
-            const long long fc = ((long long)fcz * P.nc[1] + fcy) * P.nc[0] + fcx;
+            const unsigned fc = ((unsigned)fcz * (unsigned)P.nc[1] + (unsigned)fcy) * (unsigned)P.nc[0] + (unsigned)fcx;
             const uint32_t fine_word = __ldg(P.occupancy + (fc >> 5));
             constexpr bool MIPS = COMP == VRC_MIP;
             const bool mip_skip = MIPS && P.mip_skip;
             const float fine_max = mip_skip ? __ldg(P.cell_max + fc) : 0.f;
             if (P.occ_coarse) {
                 const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
-                const long long c = ((long long)cz * P.ncc[1] + cy) * P.ncc[0] + cx;
+                const unsigned c = ((unsigned)cz * (unsigned)P.ncc[1] + (unsigned)cy) * (unsigned)P.ncc[0] + (unsigned)cx;
                 const uint32_t coarse_word = __ldg(P.occ_coarse + (c >> 5));
                 const float coarse_max = mip_skip ? __ldg(P.brick_max + c) : 0.f;
                 if (((coarse_word >> (c & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, coarse_max, max_int))) {
@@ -623,10 +638,14 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
         }
         {
             const int bx = ix >> L.shift, by = iy >> L.shift, bz = iz >> L.shift;
-            const long long brick = ((long long)bz * L.nb[1] + by) * L.nb[0] + bx;
+            const int brick = (bz * L.nb[1] + by) * L.nb[0] + bx;
+            if (brick != cached_brick) {
+                cached_brick = brick;
+                cached_base = brick_base<POOL>(P, bricks, (long long)brick);
+            }
             ++cnt.fetched;
             const float fx = s_(vx, flx), fy = s_(vy, fly), fz = s_(vz, flz);
-            const T* __restrict__ b = brick_base<POOL>(P, bricks, brick);
+            const T* __restrict__ b = cached_base;
             if (POOL && P.brick_used && brick != marked) {
                 marked = brick;
                 mark_used(P, brick);
@@ -684,8 +703,38 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                         const int dxm = (int)fxm - ix, dym = (int)fym - iy, dzm = (int)fzm - iz;
                         const int top = L.B + 1;
                         float v0, v1, v2, v3, v4, v5;
-                        if ((!POOL || b) && lx + dxp <= top && ly + dyp <= top && lz + dzp <= top && lx + dxm >= 0 &&
-                            ly + dym >= 0 && lz + dzm >= 0) {
+                        if ((!POOL || b) && dxp == 1 && dyp == 1 && dzp == 1 && dxm == -1 && dym == -1 && dzm == -1 &&
+                            lx + 1 <= top && ly + 1 <= top && lz + 1 <= top && lx >= 1 && ly >= 1 && lz >= 1) {
+                            // The usual case, each tap one voxel from the sample's floor
+                            // voxel: the six stencils cover 32 voxels (the centre 2^3 and
+                            // 4 more on each side), read once and interpolated from
+                            // registers in tri_raw's order. r<axis><side><a><b>: the
+                            // extension voxels on that side, (a, b) along the other two axes.
+#define VRC_R(X, Y, Z) ((float)__ldg(b + o + (X) + (Y) * S + (Z) * S2))
+                            const float c000 = VRC_R(0, 0, 0), c100 = VRC_R(1, 0, 0), c010 = VRC_R(0, 1, 0),
+                                        c110 = VRC_R(1, 1, 0), c001 = VRC_R(0, 0, 1), c101 = VRC_R(1, 0, 1),
+                                        c011 = VRC_R(0, 1, 1), c111 = VRC_R(1, 1, 1);
+                            const float rxm00 = VRC_R(-1, 0, 0), rxm10 = VRC_R(-1, 1, 0), rxm01 = VRC_R(-1, 0, 1),
+                                        rxm11 = VRC_R(-1, 1, 1);
+                            const float rxp00 = VRC_R(2, 0, 0), rxp10 = VRC_R(2, 1, 0), rxp01 = VRC_R(2, 0, 1),
+                                        rxp11 = VRC_R(2, 1, 1);
+                            const float rym00 = VRC_R(0, -1, 0), rym10 = VRC_R(1, -1, 0), rym01 = VRC_R(0, -1, 1),
+                                        rym11 = VRC_R(1, -1, 1);
+                            const float ryp00 = VRC_R(0, 2, 0), ryp10 = VRC_R(1, 2, 0), ryp01 = VRC_R(0, 2, 1),
+                                        ryp11 = VRC_R(1, 2, 1);
+                            const float rzm00 = VRC_R(0, 0, -1), rzm10 = VRC_R(1, 0, -1), rzm01 = VRC_R(0, 1, -1),
+                                        rzm11 = VRC_R(1, 1, -1);
+                            const float rzp00 = VRC_R(0, 0, 2), rzp10 = VRC_R(1, 0, 2), rzp01 = VRC_R(0, 1, 2),
+                                        rzp11 = VRC_R(1, 1, 2);
+#undef VRC_R
+                            v0 = tri_regs(c100, rxp00, c110, rxp10, c101, rxp01, c111, rxp11, vxp - fxp, fy, fz);
+                            v1 = tri_regs(c010, c110, ryp00, ryp10, c011, c111, ryp01, ryp11, fx, vyp - fyp, fz);
+                            v2 = tri_regs(c001, c101, c011, c111, rzp00, rzp10, rzp01, rzp11, fx, fy, vzp - fzp);
+                            v3 = tri_regs(rxm00, c000, rxm10, c010, rxm01, c001, rxm11, c011, vxm - fxm, fy, fz);
+                            v4 = tri_regs(rym00, rym10, c000, c100, rym01, rym11, c001, c101, fx, vym - fym, fz);
+                            v5 = tri_regs(rzm00, rzm10, rzm01, rzm11, c000, c100, c010, c110, fx, fy, vzm - fzm);
+                        } else if ((!POOL || b) && lx + dxp <= top && ly + dyp <= top && lz + dzp <= top &&
+                                   lx + dxm >= 0 && ly + dym >= 0 && lz + dzm >= 0) {
                             v0 = tri_raw<DT>(b, o + dxp, S, S2, vxp - fxp, fy, fz);
                             v1 = tri_raw<DT>(b, o + dyp * S, S, S2, fx, vyp - fyp, fz);
                             v2 = tri_raw<DT>(b, o + dzp * S2, S, S2, fx, fy, vzp - fzp);

@@ -242,10 +242,11 @@ struct vrc_volume {
     uint32_t frame = 0;
     bool used_pending = false;         // d_used holds the last frame's bits
     long long last_misses = 0;         // bricks touched without a slot in the last frame
-    // half-resolution level (2x2x2 mean), device resident, sampled for
-    // bricks without a slot when lod_on
+    // a coarser level (2x2x2 means applied lod_level times), device
+    // resident, sampled for bricks without a slot when lod_on
     void* d_lod = nullptr;
     vrc::BrickLayout lod_L{};
+    int lod_level = 0;                 // level d_lod holds: 1 = half resolution, k = 2^-k
     bool lod_on = false;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
