@@ -427,7 +427,7 @@ vrc_status vrc_batch_destroy(vrc_batch* b);
  * synchronise the device and stall the frame), or hosts whose device memory
  * belongs to their own fixed-budget pool or to another runtime. It renders
  * like vrc_render but keeps its scratch (sample and tile counters, the
- * per-render TF table, the empty-space cell map) in one fixed-size array in
+ * per-render alpha table, the empty-space cell map) in one fixed-size array in
  * device global memory that every GPU loading the library holds until exit,
  * and it allocates nothing.
  * Limits: at most VRC_NOALLOC_MAX_CELLS empty-space cells when skipping is on
@@ -459,6 +459,17 @@ vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc
 vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                           const float* d_entry, const float* d_exit, void* d_out, int out_format, float* d_aux,
                           vrc_render_stats* stats);
+/* vrc_render_aux with each ray cut into four segments of whole sample steps,
+ * marched by four lanes at once and composited front to back (early ray
+ * termination applied after every segment). No counterpart in the reference,
+ * and not its loop: an approximation for the learned upsampler's
+ * half-resolution input march, whose frames are judged by PSNR against the
+ * plain render. It shortens the serial sample chain of the longest rays,
+ * which bounds a half-resolution frame. Analytic entry/exit, DVR with TF
+ * classification and device-resident volumes; VRC_ERR_UNSUPPORTED otherwise. */
+vrc_status vrc_render_aux_segments(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
+                                   const vrc_render_params* p, void* d_out, int out_format, float* d_aux,
+                                   vrc_render_stats* stats);
 
 /* Analytic entry/exit points (texture space) for `p->camera`, written as
  * float4 images, host or device destination. */

@@ -132,6 +132,7 @@ class Volume:
             dt = _NP_DTYPE[voxels.dtype]
             shape = voxels.shape
         self.desc = make_desc(dt, (shape[2], shape[1], shape[0]), spacing, offset, rwm)
+        self.placement = placement
         self.handle = C.c_void_p()
         _check(lib().vrc_volume_upload_placed(ctx.handle, C.byref(self.desc), _ptr(voxels),
                                               1 if _is_device(voxels) else 0, brick_size, placement,
@@ -143,6 +144,7 @@ class Volume:
         (vrc_volume_load_vvd); the header is in `.vvd_info`."""
         self = cls.__new__(cls)
         self.ctx = ctx
+        self.placement = PLACE_DEVICE
         self.handle = C.c_void_p()
         info = _abi.VvdInfo()
         _check(lib().vrc_volume_load_vvd(ctx.handle, path.encode(), brick_size, C.byref(self.handle), C.byref(info)),

@@ -32,6 +32,7 @@ SOURCES = [
     ("march_mip_iso.cu", ["-fmad=false"]),
     ("march_mop_mida.cu", ["-fmad=false"]),
     ("march_first_hit.cu", ["-fmad=false"]),
+    ("march_segments.cu", ["-fmad=false"]),
     ("preint.cu", ["-fmad=false"]),
     ("image.cu", []),
     ("diag.cu", []),

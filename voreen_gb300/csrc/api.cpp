@@ -593,6 +593,8 @@ vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float
     for (int i = 0; i < width; ++i) prefix[i + 1] = prefix[i] + (rgba[4 * i + 3] > 0 ? 1 : 0);
     cudaError_t e = cudaMalloc(&t->d_prefix, (width + 1) * sizeof(int));
     if (e == cudaSuccess) e = cudaMemcpy(t->d_prefix, prefix.data(), (width + 1) * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&t->d_rgba8, (size_t)width * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(t->d_rgba8, rgba, (size_t)width * 4, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         vrc_tf_destroy(t);
         return cuda_fail(ctx, e, "vrc_tf_create");
@@ -604,7 +606,8 @@ vrc_status vrc_tf_create(vrc_context* ctx, const uint8_t* rgba, int width, float
 vrc_status vrc_tf_destroy(vrc_tf* t) {
     if (!t) return VRC_ERR_INVALID_ARG;
     if (t->ctx) cudaSetDevice(t->ctx->device);
-    for (auto& kv : t->tables) cudaFree(kv.second);
+    for (auto& kv : t->alpha_tables) cudaFree(kv.second);
+    cudaFree(t->d_rgba8);
     cudaFree(t->d_prefix);
     delete[] t->h_rgba;
     delete t;
@@ -676,34 +679,38 @@ namespace {
 
 namespace vrc {
 
-// Float4 TF table for a render: (r/255, g/255, b/255, alpha') with alpha' the
-// opacity-corrected alpha for DVR (cpuraycaster.cpp:291) and the plain alpha
-// for MIP / ISO.
-vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float4** out) {
+// Alpha per alpha byte for a render: the opacity-corrected alpha
+// 1 - (1 - a/255)^(step * 200) for DVR (cpuraycaster.cpp:291) and the plain
+// a/255 for MIP / ISO -- the values CPURaycaster computes per sample, here
+// once per byte with the same float arithmetic and powf.
+void tf_alpha_values(bool corrected, float kcorr, float out[256]) {
+    for (int a = 0; a < 256; ++a) {
+        float x = float(a) / 255.f;
+        if (corrected) x = 1.f - powf(1.f - x, kcorr);
+        out[a] = x;
+    }
+}
+
+vrc_status tf_alpha(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float** out) {
     uint32_t bits = 0;
     std::memcpy(&bits, &kcorr, 4);
     const auto key = std::make_pair(corrected ? 1 : 0, corrected ? bits : 0u);
-    auto it = tf->tables.find(key);
-    if (it != tf->tables.end()) {
+    auto it = tf->alpha_tables.find(key);
+    if (it != tf->alpha_tables.end()) {
         *out = it->second;
         return VRC_OK;
     }
-    std::vector<float4> h(tf->width);
-    for (int i = 0; i < tf->width; ++i) {
-        const uint8_t* c = tf->h_rgba + 4 * i;
-        float a = float(c[3]) / 255.f;
-        if (corrected) a = 1.f - powf(1.f - a, kcorr);
-        h[i] = make_float4(float(c[0]) / 255.f, float(c[1]) / 255.f, float(c[2]) / 255.f, a);
-    }
-    float4* d = nullptr;
-    cudaError_t e0 = cudaMalloc(&d, tf->width * sizeof(float4));
-    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "tf table allocation");
-    cudaError_t e = cudaMemcpy(d, h.data(), tf->width * sizeof(float4), cudaMemcpyHostToDevice);
+    float h[256];
+    tf_alpha_values(corrected, kcorr, h);
+    float* d = nullptr;
+    cudaError_t e0 = cudaMalloc(&d, sizeof(h));
+    if (e0 != cudaSuccess) return cuda_fail(ctx, e0, "tf alpha table allocation");
+    cudaError_t e = cudaMemcpy(d, h, sizeof(h), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         cudaFree(d);
-        return cuda_fail(ctx, e, "tf table upload");
+        return cuda_fail(ctx, e, "tf alpha table upload");
     }
-    tf->tables[key] = d;
+    tf->alpha_tables[key] = d;
     *out = d;
     return VRC_OK;
 }
@@ -814,7 +821,7 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
 
 using vrc::check_params;
 using vrc::fill_params;
-using vrc::tf_table;
+using vrc::tf_alpha;
 
 
 extern "C" {
@@ -1065,7 +1072,7 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
 
 vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
                        const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
-                       int out_on_device, float* aux, vrc_render_stats* stats) {
+                       int out_on_device, float* aux, vrc_render_stats* stats, bool segments = false) {
     if (!ctx) return VRC_ERR_INVALID_ARG;
     if (!vol || !tf_c) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: volume and transfer function are required");
     if (vol->ctx != ctx || tf_c->ctx != ctx) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: handle from another context");
@@ -1076,6 +1083,11 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown output format");
     if (p->entry_exit_mode == VRC_EE_BUFFERS && (!entry || !exitp))
         return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: entry/exit points are required in buffer mode");
+    if (segments && (p->entry_exit_mode != VRC_EE_ANALYTIC || p->compositing != VRC_DVR ||
+                     p->classification != VRC_CLASSIFY_TF || vol->h_bricks))
+        return fail(ctx, VRC_ERR_UNSUPPORTED,
+                    "vrc_render_aux_segments: analytic entry/exit, DVR, TF classification and a device-resident "
+                    "volume only");
     vrc_tf* tf = const_cast<vrc_tf*>(tf_c);
     VRC_CUDA(ctx, cudaSetDevice(ctx->device));
     MarchParams P;
@@ -1095,17 +1107,19 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             const int* d = vol->desc.dims;
             P.pi_chain = P.step * float(std::max(d[0], std::max(d[1], d[2]))) <= 0.99f ? 1 : 0;
         }
-        P.tf_table = nullptr;
+        P.tf_rgba8 = nullptr;
+        P.tf_alpha = nullptr;
         P.tf_width = 0;  // the TF table is not read
         occ_prefix = pi->d_prefix;
         occ_width = pi->res;
         occ_source = pi->uid;
     } else {
-        float4* table = nullptr;
-        if ((st = tf_table(ctx, tf, vrc::alpha_corrected(p->compositing, p->classification), kcorr, &table)) !=
+        float* alpha = nullptr;
+        if ((st = tf_alpha(ctx, tf, vrc::alpha_corrected(p->compositing, p->classification), kcorr, &alpha)) !=
             VRC_OK)
             return st;
-        P.tf_table = table;
+        P.tf_rgba8 = tf->d_rgba8;
+        P.tf_alpha = alpha;
         P.tf_width = tf->width;
     }
     P.tf_lo = tf->lo;
@@ -1235,7 +1249,10 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     P.status = reinterpret_cast<int*>(ctx->d_counters + 4);
     P.tile_counter = reinterpret_cast<unsigned int*>(ctx->d_counters + 5);
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-    VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
+    if (segments)
+        VRC_CUDA(ctx, vrc::launch_march_segments(P, vol->desc.dtype, p->shading, ctx->num_sms, s));
+    else
+        VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     if (!out_on_device && !mout) VRC_CUDA(ctx, cudaMemcpyAsync(out, P.out, npix * px_bytes, cudaMemcpyDeviceToHost, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
@@ -1271,6 +1288,13 @@ vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf*
                           vrc_render_stats* stats) {
     if (!d_aux) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render_aux: null aux image");
     return render_impl(ctx, vol, tf, p, d_entry, d_exit, 1, d_out, out_format, 1, d_aux, stats);
+}
+
+vrc_status vrc_render_aux_segments(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
+                                   const vrc_render_params* p, void* d_out, int out_format, float* d_aux,
+                                   vrc_render_stats* stats) {
+    if (!d_aux) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render_aux_segments: null aux image");
+    return render_impl(ctx, vol, tf, p, nullptr, nullptr, 1, d_out, out_format, 1, d_aux, stats, true);
 }
 
 vrc_status vrc_entry_exit(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, float* entry,

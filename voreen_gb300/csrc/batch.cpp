@@ -137,13 +137,14 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
             return st;
         }
         R.dtype = it.volume->desc.dtype;
-        float4* table = nullptr;
-        if ((st = vrc::tf_table(ctx, const_cast<vrc_tf*>(it.tf), it.params.compositing == VRC_DVR, R.P.step * 200.f,
-                                &table)) != VRC_OK) {
+        float* alpha = nullptr;
+        if ((st = vrc::tf_alpha(ctx, const_cast<vrc_tf*>(it.tf), it.params.compositing == VRC_DVR, R.P.step * 200.f,
+                                &alpha)) != VRC_OK) {
             release(b);
             return st;
         }
-        R.P.tf_table = table;
+        R.P.tf_rgba8 = it.tf->d_rgba8;
+        R.P.tf_alpha = alpha;
         R.P.tf_width = it.tf->width;
         R.P.tf_lo = it.tf->lo;
         R.P.tf_hi = it.tf->hi;

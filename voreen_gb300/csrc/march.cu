@@ -108,10 +108,10 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS)
             if (!bg) {
                 const int dt = s_dtype[wib];
                 if (dt == VRC_U8)
-                    res = march_ray<VRC_U8, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
+                    res = march_ray<VRC_U8, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_rgba8, P.tf_alpha, f, l, px, py, cnt, ax);
                 else if (dt == VRC_U16)
-                    res = march_ray<VRC_U16, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
-                else res = march_ray<VRC_F32, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_table, f, l, px, py, cnt, ax);
+                    res = march_ray<VRC_U16, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_rgba8, P.tf_alpha, f, l, px, py, cnt, ax);
+                else res = march_ray<VRC_F32, COMP, SHADE, VRC_EE_ANALYTIC>(P, P.tf_rgba8, P.tf_alpha, f, l, px, py, cnt, ax);
             }
             write_out(P, (size_t)py * P.W + px, res);
             if (P.aux) P.aux[(size_t)py * P.W + px] = ax;

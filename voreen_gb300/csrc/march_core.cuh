@@ -6,9 +6,12 @@
 //  * persistent grid (a few CTAs per SM); each warp pulls 8x4 ray tiles from
 //    a global counter, so a warp's 32 rays are adjacent on screen and walk
 //    the same bricks;
-//  * the transfer function sits in shared memory as float4 (r, g, b, alpha')
-//    where alpha' already carries the opacity correction 1-(1-a)^(step*200)
-//    (computed on the host with the same powf the CPU path calls);
+//  * the transfer function sits in shared memory as its RGBA8 entries plus
+//    a table of 256 alphas (one per alpha byte) that already carry the
+//    opacity correction 1-(1-a)^(step*200), computed on the host with the
+//    same powf the CPU path calls; r/255, g/255, b/255 are the exact 8-bit
+//    normalisation. 17 KB per CTA at 4096 entries, so most of the SM's
+//    unified L1 / shared array stays L1 for the voxel gathers;
 //  * voxels come from the bricked layout (32^3 core + apron), so a stencil
 //    never crosses a brick; empty bricks (per-brick min/max against the TF)
 //    are skipped without reading voxels while t still advances sample by
@@ -505,9 +508,92 @@ __device__ __forceinline__ float4 mida_step(float4 r, float v, float4 c, float m
                        a_(m_(beta, r.w), wa));
 }
 
+// calcGradientA (mod_gradients.frag:202-214) of the sample at texture point
+// (sx, sy, sz): six lookups at +-1/dim in texture space, each clamped like
+// the intensity sample, interpolated on raw values. (vx, vy, vz): the
+// sample's clamped voxel position, (ix, iy, iz) its floor, (fx, fy, fz) the
+// fractions, b / o / (lx, ly, lz) its brick start, offset and brick-local
+// voxel. The same function runs wherever a sample is shaded, so its bits do
+// not depend on where.
+template <int DT, bool POOL>
+__device__ __forceinline__ F3 central_gradient(const MarchParams& P, const typename Vox<DT>::T* __restrict__ bricks,
+                                               const typename Vox<DT>::T* __restrict__ b, int o, int lx, int ly,
+                                               int lz, int ix, int iy, int iz, float vx, float vy, float vz, float fx,
+                                               float fy, float fz, float sx, float sy, float sz) {
+    const BrickLayout& L = P.L;
+    const int S = L.S, S2 = L.S * L.S;
+    // calcGradientA: six lookups at +-1/dim in texture space, each
+    // clamped like the intensity sample; interpolated on raw values
+    const float vxp = clampf_(s_(m_(P.dimf[0], a_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
+    const float vyp = clampf_(s_(m_(P.dimf[1], a_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
+    const float vzp = clampf_(s_(m_(P.dimf[2], a_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
+    const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
+    const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
+    const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
+    // The taps lie at or beyond the sample on their axis, so
+    // the "+" taps can only leave the apron upward and the
+    // "-" taps downward. When all six stay inside (away from
+    // the volume's faces, always), they are read in one
+    // straight block whose 48 loads are in flight together.
+    const float fxp = floorf(vxp), fyp = floorf(vyp), fzp = floorf(vzp);
+    const float fxm = floorf(vxm), fym = floorf(vym), fzm = floorf(vzm);
+    const int dxp = (int)fxp - ix, dyp = (int)fyp - iy, dzp = (int)fzp - iz;
+    const int dxm = (int)fxm - ix, dym = (int)fym - iy, dzm = (int)fzm - iz;
+    const int top = L.B + 1;
+    float v0, v1, v2, v3, v4, v5;
+    if ((!POOL || b) && dxp == 1 && dyp == 1 && dzp == 1 && dxm == -1 && dym == -1 && dzm == -1 &&
+        lx + 1 <= top && ly + 1 <= top && lz + 1 <= top && lx >= 1 && ly >= 1 && lz >= 1) {
+        // The usual case, each tap one voxel from the sample's floor
+        // voxel: the six stencils cover 32 voxels (the centre 2^3 and
+        // 4 more on each side), read once and interpolated from
+        // registers in tri_raw's order. r<axis><side><a><b>: the
+        // extension voxels on that side, (a, b) along the other two axes.
+#define VRC_R(X, Y, Z) ((float)__ldg(b + o + (X) + (Y) * S + (Z) * S2))
+        const float c000 = VRC_R(0, 0, 0), c100 = VRC_R(1, 0, 0), c010 = VRC_R(0, 1, 0),
+                    c110 = VRC_R(1, 1, 0), c001 = VRC_R(0, 0, 1), c101 = VRC_R(1, 0, 1),
+                    c011 = VRC_R(0, 1, 1), c111 = VRC_R(1, 1, 1);
+        const float rxm00 = VRC_R(-1, 0, 0), rxm10 = VRC_R(-1, 1, 0), rxm01 = VRC_R(-1, 0, 1),
+                    rxm11 = VRC_R(-1, 1, 1);
+        const float rxp00 = VRC_R(2, 0, 0), rxp10 = VRC_R(2, 1, 0), rxp01 = VRC_R(2, 0, 1),
+                    rxp11 = VRC_R(2, 1, 1);
+        const float rym00 = VRC_R(0, -1, 0), rym10 = VRC_R(1, -1, 0), rym01 = VRC_R(0, -1, 1),
+                    rym11 = VRC_R(1, -1, 1);
+        const float ryp00 = VRC_R(0, 2, 0), ryp10 = VRC_R(1, 2, 0), ryp01 = VRC_R(0, 2, 1),
+                    ryp11 = VRC_R(1, 2, 1);
+        const float rzm00 = VRC_R(0, 0, -1), rzm10 = VRC_R(1, 0, -1), rzm01 = VRC_R(0, 1, -1),
+                    rzm11 = VRC_R(1, 1, -1);
+        const float rzp00 = VRC_R(0, 0, 2), rzp10 = VRC_R(1, 0, 2), rzp01 = VRC_R(0, 1, 2),
+                    rzp11 = VRC_R(1, 1, 2);
+#undef VRC_R
+        v0 = tri_regs(c100, rxp00, c110, rxp10, c101, rxp01, c111, rxp11, vxp - fxp, fy, fz);
+        v1 = tri_regs(c010, c110, ryp00, ryp10, c011, c111, ryp01, ryp11, fx, vyp - fyp, fz);
+        v2 = tri_regs(c001, c101, c011, c111, rzp00, rzp10, rzp01, rzp11, fx, fy, vzp - fzp);
+        v3 = tri_regs(rxm00, c000, rxm10, c010, rxm01, c001, rxm11, c011, vxm - fxm, fy, fz);
+        v4 = tri_regs(rym00, rym10, c000, c100, rym01, rym11, c001, c101, fx, vym - fym, fz);
+        v5 = tri_regs(rzm00, rzm10, rzm01, rzm11, c000, c100, c010, c110, fx, fy, vzm - fzm);
+    } else if ((!POOL || b) && lx + dxp <= top && ly + dyp <= top && lz + dzp <= top &&
+               lx + dxm >= 0 && ly + dym >= 0 && lz + dzm >= 0) {
+        v0 = tri_raw<DT>(b, o + dxp, S, S2, vxp - fxp, fy, fz);
+        v1 = tri_raw<DT>(b, o + dyp * S, S, S2, fx, vyp - fyp, fz);
+        v2 = tri_raw<DT>(b, o + dzp * S2, S, S2, fx, fy, vzp - fzp);
+        v3 = tri_raw<DT>(b, o + dxm, S, S2, vxm - fxm, fy, fz);
+        v4 = tri_raw<DT>(b, o + dym * S, S, S2, fx, vym - fym, fz);
+        v5 = tri_raw<DT>(b, o + dzm * S2, S, S2, fx, fy, vzm - fzm);
+    } else {
+        v0 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
+        v1 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
+        v2 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
+        v3 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
+        v4 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
+        v5 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
+    }
+    return F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
+}
+
 // One ray: the loop of cpuraycaster.cpp:239-317 with the GLSL compositing.
 template <int DT, int COMP, int SHADE, int EE, bool POOL = false>
-__device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_tf, float4 f, float4 l, int px,
+__device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_tf, const float* __restrict__ s_alpha,
+                            float4 f, float4 l, int px,
                             int py, Counters& cnt, float2& aux) {
     using T = typename Vox<DT>::T;
     const T* __restrict__ bricks = reinterpret_cast<const T*>(P.bricks);
@@ -675,7 +761,10 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                 c = __ldg(P.pi_table + (size_t)tf_index(cur, P.pi_res) * P.pi_res + tf_index(last, P.pi_res));
                 last = cur;
             } else {
-                c = s_tf[tf_index(rw_to_tf(rw, P.tf_lo, P.tf_hi), P.tf_width)];
+                // apply1DTF: the entry's bytes / 255 (exact), alpha from the per-byte table
+                const uchar4 e8 = s_tf[tf_index(rw_to_tf(rw, P.tf_lo, P.tf_hi), P.tf_width)];
+                c = make_float4(Vox<VRC_U8>::norm(e8.x), Vox<VRC_U8>::norm(e8.y), Vox<VRC_U8>::norm(e8.z),
+                                s_alpha[e8.w]);
             }
             if (c.w > 0.f) {
                 if (SHADE == VRC_SHADE_PHONG) {
@@ -684,72 +773,8 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
                     if (t == 0.f) {
                         g = clip_border_gradient<EE>(P, F3{sx, sy, sz}, F3{dx, dy, dz}, px, py);
                     } else {
-                        // calcGradientA: six lookups at +-1/dim in texture space, each
-                        // clamped like the intensity sample; interpolated on raw values
-                        const float vxp = clampf_(s_(m_(P.dimf[0], a_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
-                        const float vyp = clampf_(s_(m_(P.dimf[1], a_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
-                        const float vzp = clampf_(s_(m_(P.dimf[2], a_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        const float vxm = clampf_(s_(m_(P.dimf[0], s_(sx, P.offs[0])), 0.5f), 0.f, P.dim_m1[0]);
-                        const float vym = clampf_(s_(m_(P.dimf[1], s_(sy, P.offs[1])), 0.5f), 0.f, P.dim_m1[1]);
-                        const float vzm = clampf_(s_(m_(P.dimf[2], s_(sz, P.offs[2])), 0.5f), 0.f, P.dim_m1[2]);
-                        // The taps lie at or beyond the sample on their axis, so
-                        // the "+" taps can only leave the apron upward and the
-                        // "-" taps downward. When all six stay inside (away from
-                        // the volume's faces, always), they are read in one
-                        // straight block whose 48 loads are in flight together.
-                        const float fxp = floorf(vxp), fyp = floorf(vyp), fzp = floorf(vzp);
-                        const float fxm = floorf(vxm), fym = floorf(vym), fzm = floorf(vzm);
-                        const int dxp = (int)fxp - ix, dyp = (int)fyp - iy, dzp = (int)fzp - iz;
-                        const int dxm = (int)fxm - ix, dym = (int)fym - iy, dzm = (int)fzm - iz;
-                        const int top = L.B + 1;
-                        float v0, v1, v2, v3, v4, v5;
-                        if ((!POOL || b) && dxp == 1 && dyp == 1 && dzp == 1 && dxm == -1 && dym == -1 && dzm == -1 &&
-                            lx + 1 <= top && ly + 1 <= top && lz + 1 <= top && lx >= 1 && ly >= 1 && lz >= 1) {
-                            // The usual case, each tap one voxel from the sample's floor
-                            // voxel: the six stencils cover 32 voxels (the centre 2^3 and
-                            // 4 more on each side), read once and interpolated from
-                            // registers in tri_raw's order. r<axis><side><a><b>: the
-                            // extension voxels on that side, (a, b) along the other two axes.
-#define VRC_R(X, Y, Z) ((float)__ldg(b + o + (X) + (Y) * S + (Z) * S2))
-                            const float c000 = VRC_R(0, 0, 0), c100 = VRC_R(1, 0, 0), c010 = VRC_R(0, 1, 0),
-                                        c110 = VRC_R(1, 1, 0), c001 = VRC_R(0, 0, 1), c101 = VRC_R(1, 0, 1),
-                                        c011 = VRC_R(0, 1, 1), c111 = VRC_R(1, 1, 1);
-                            const float rxm00 = VRC_R(-1, 0, 0), rxm10 = VRC_R(-1, 1, 0), rxm01 = VRC_R(-1, 0, 1),
-                                        rxm11 = VRC_R(-1, 1, 1);
-                            const float rxp00 = VRC_R(2, 0, 0), rxp10 = VRC_R(2, 1, 0), rxp01 = VRC_R(2, 0, 1),
-                                        rxp11 = VRC_R(2, 1, 1);
-                            const float rym00 = VRC_R(0, -1, 0), rym10 = VRC_R(1, -1, 0), rym01 = VRC_R(0, -1, 1),
-                                        rym11 = VRC_R(1, -1, 1);
-                            const float ryp00 = VRC_R(0, 2, 0), ryp10 = VRC_R(1, 2, 0), ryp01 = VRC_R(0, 2, 1),
-                                        ryp11 = VRC_R(1, 2, 1);
-                            const float rzm00 = VRC_R(0, 0, -1), rzm10 = VRC_R(1, 0, -1), rzm01 = VRC_R(0, 1, -1),
-                                        rzm11 = VRC_R(1, 1, -1);
-                            const float rzp00 = VRC_R(0, 0, 2), rzp10 = VRC_R(1, 0, 2), rzp01 = VRC_R(0, 1, 2),
-                                        rzp11 = VRC_R(1, 1, 2);
-#undef VRC_R
-                            v0 = tri_regs(c100, rxp00, c110, rxp10, c101, rxp01, c111, rxp11, vxp - fxp, fy, fz);
-                            v1 = tri_regs(c010, c110, ryp00, ryp10, c011, c111, ryp01, ryp11, fx, vyp - fyp, fz);
-                            v2 = tri_regs(c001, c101, c011, c111, rzp00, rzp10, rzp01, rzp11, fx, fy, vzp - fzp);
-                            v3 = tri_regs(rxm00, c000, rxm10, c010, rxm01, c001, rxm11, c011, vxm - fxm, fy, fz);
-                            v4 = tri_regs(rym00, rym10, c000, c100, rym01, rym11, c001, c101, fx, vym - fym, fz);
-                            v5 = tri_regs(rzm00, rzm10, rzm01, rzm11, c000, c100, c010, c110, fx, fy, vzm - fzm);
-                        } else if ((!POOL || b) && lx + dxp <= top && ly + dyp <= top && lz + dzp <= top &&
-                                   lx + dxm >= 0 && ly + dym >= 0 && lz + dzm >= 0) {
-                            v0 = tri_raw<DT>(b, o + dxp, S, S2, vxp - fxp, fy, fz);
-                            v1 = tri_raw<DT>(b, o + dyp * S, S, S2, fx, vyp - fyp, fz);
-                            v2 = tri_raw<DT>(b, o + dzp * S2, S, S2, fx, fy, vzp - fzp);
-                            v3 = tri_raw<DT>(b, o + dxm, S, S2, vxm - fxm, fy, fz);
-                            v4 = tri_raw<DT>(b, o + dym * S, S, S2, fx, vym - fym, fz);
-                            v5 = tri_raw<DT>(b, o + dzm * S2, S, S2, fx, fy, vzm - fzm);
-                        } else {
-                            v0 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxp, vx, vy, vz, fx, fy, fz);
-                            v1 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vyp, vx, vy, vz, fx, fy, fz);
-                            v2 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzp, vx, vy, vz, fx, fy, fz);
-                            v3 = grad_tap<DT, 0, POOL>(P, bricks, b, o, lx, ix, vxm, vx, vy, vz, fx, fy, fz);
-                            v4 = grad_tap<DT, 1, POOL>(P, bricks, b, o, ly, iy, vym, vx, vy, vz, fx, fy, fz);
-                            v5 = grad_tap<DT, 2, POOL>(P, bricks, b, o, lz, iz, vzm, vx, vy, vz, fx, fy, fz);
-                        }
-                        g = F3{(v3 - v0) * P.gscale[0], (v4 - v1) * P.gscale[1], (v5 - v2) * P.gscale[2]};
+                        g = central_gradient<DT, POOL>(P, bricks, b, o, lx, ly, lz, ix, iy, iz, vx, vy, vz, fx, fy,
+                                                       fz, sx, sy, sz);
                     }
                     const F3 pos{a_(m_(s_(m_(sx, P.dimf[0]), 0.5f), P.spacing[0]), P.vol_offset[0]),
                                  a_(m_(s_(m_(sy, P.dimf[1]), 0.5f), P.spacing[1]), P.vol_offset[1]),
@@ -851,8 +876,16 @@ __device__ float4 march_ray(const MarchParams& P, const float4* __restrict__ s_t
 
 template <int DT, int COMP, int SHADE, int EE, bool POOL>
 __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchParams P) {
-    extern __shared__ float4 s_tf[];
-    for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_table[i];
+    // the TF in shared memory: 256 alphas, then the RGBA8 entries (17 KB at
+    // 4096 entries, leaving most of the SM's 256 KB to the L1 that serves the
+    // voxel gathers)
+    extern __shared__ float4 s_raw[];
+    float* s_alpha = reinterpret_cast<float*>(s_raw);
+    uchar4* s_tf = reinterpret_cast<uchar4*>(s_alpha + 256);
+    if (P.tf_width > 0) {
+        for (int i = threadIdx.x; i < P.tf_width; i += blockDim.x) s_tf[i] = P.tf_rgba8[i];
+        for (int i = threadIdx.x; i < 256; i += blockDim.x) s_alpha[i] = P.tf_alpha[i];
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int ntiles = P.tiles_x * P.tiles_y;
@@ -879,7 +912,7 @@ __global__ void __launch_bounds__(256, VRC_MARCH_MIN_BLOCKS) march_kernel(MarchP
                             l.z == 0.f && l.w == 0.f;
             float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
             float2 ax = make_float2(1.f, 0.f);
-            if (!bg) r = march_ray<DT, COMP, SHADE, EE, POOL>(P, s_tf, f, l, px, py, cnt, ax);
+            if (!bg) r = march_ray<DT, COMP, SHADE, EE, POOL>(P, s_tf, s_alpha, f, l, px, py, cnt, ax);
             write_out(P, pix, r);
             if (P.aux) P.aux[pix] = ax;
         }
@@ -926,9 +959,9 @@ cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
             *per_sm = x.per_sm;
             return cudaSuccess;
         }
-    // the largest table (4096 entries, 64 KB) once per device; smaller ones fit under it
+    // the largest table (4096 entries) once per device; smaller ones fit under it
     e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)std::max(smem, (size_t)4096 * sizeof(float4)));
+                             (int)std::max(smem, 256 * sizeof(float) + (size_t)4096 * sizeof(uchar4)));
     if (e != cudaSuccess) return e;
     int n = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, 256, smem);
@@ -941,7 +974,7 @@ cudaError_t resident_ctas(K k, size_t smem, int* per_sm) {
 template <int DT, int COMP, int SHADE, int EE, bool POOL>
 cudaError_t launch_t(const MarchParams& p, int num_sms, cudaStream_t s) {
     auto k = march_kernel<DT, COMP, SHADE, EE, POOL>;
-    const size_t smem = (size_t)p.tf_width * sizeof(float4);
+    const size_t smem = 256 * sizeof(float) + (size_t)p.tf_width * sizeof(uchar4);
     int per_sm = 0;
     cudaError_t e = resident_ctas(k, smem, &per_sm);
     if (e != cudaSuccess) return e;

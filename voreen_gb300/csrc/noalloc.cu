@@ -17,11 +17,12 @@
 // cleared on each call, and calls that overlap on the GPU (other streams, or
 // threads without ordering) race.
 //
-// The TF table is built on the device by a small kernel whose by-value
-// parameters carry the RGBA8 entries and the (opacity-corrected) alpha of
-// each of the 256 alpha bytes, computed on the host with the same powf
-// vrc_render uses; so no host buffer is read after the call returns and the
-// table equals vrc_render's bit for bit.
+// The march reads the TF's RGBA8 entries where the TF object keeps them on
+// the device, and a table of the (opacity-corrected) alpha of each of the 256
+// alpha bytes, computed on the host with the same powf vrc_render uses and
+// written into the scratch array by a small kernel whose by-value parameters
+// carry it; so no host buffer is read after the call returns and the frame
+// equals vrc_render's bit for bit.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -34,28 +35,19 @@ namespace {
 
 constexpr size_t COUNTER_BYTES = 256;                        // 16 x u64 counters, padded
 constexpr int MAX_TF = 4096;
-constexpr size_t TF_BYTES = (size_t)MAX_TF * sizeof(float4);  // widest TF table
-constexpr size_t OCC_OFFSET = COUNTER_BYTES + TF_BYTES;
+constexpr size_t ALPHA_BYTES = 256 * sizeof(float);           // alpha per alpha byte of the TF
+constexpr size_t OCC_OFFSET = COUNTER_BYTES + ALPHA_BYTES;
 constexpr size_t SCRATCH_BYTES = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS / 8;  // one bit per cell
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
-// Kernel parameters of the TF table build: 16 KB of RGBA8 entries and 1 KB of
-// alpha values (17.4 KB, inside the 32 KB kernel-parameter limit).
-struct TfTableArgs {
-    uchar4 rgba[MAX_TF];
+// Kernel parameters of the alpha table build: the 256 alphas by value, so no
+// host buffer is read after the launch.
+struct AlphaArgs {
     float alpha[256];  // alpha' for each alpha byte
-    int width;
 };
 
-__global__ void tf_table_kernel(const TfTableArgs a, float4* out) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.width; i += gridDim.x * blockDim.x) {
-        const uchar4 c = a.rgba[i];
-        // correctly rounded IEEE divisions: the same values as the host's
-        out[i] = make_float4(__fdiv_rn((float)c.x, 255.f), __fdiv_rn((float)c.y, 255.f), __fdiv_rn((float)c.z, 255.f),
-                             a.alpha[c.w]);
-    }
-}
+__global__ void alpha_table_kernel(const AlphaArgs a, float* out) { out[threadIdx.x] = a.alpha[threadIdx.x]; }
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_setup_mutex;
@@ -120,22 +112,17 @@ vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_ren
     const long long ncells = (long long)nc[0] * nc[1] * nc[2];
     if (p->empty_space_skipping && ncells > (long long)VRC_NOALLOC_MAX_CELLS) return VRC_ERR_SCRATCH_LIMIT;
 
-    // TF table (r/255, g/255, b/255, alpha') into the scratch array
-    static thread_local TfTableArgs args;
-    const bool corrected = vrc::alpha_corrected(p->compositing, p->classification);
-    const float kcorr = P.step * 200.f;
-    for (int a = 0; a < 256; ++a) {
-        float x = float(a) / 255.f;
-        if (corrected) x = 1.f - powf(1.f - x, kcorr);
-        args.alpha[a] = x;
-    }
-    std::memcpy(args.rgba, tf->h_rgba, (size_t)tf->width * 4);
-    args.width = tf->width;
-    float4* d_tf = reinterpret_cast<float4*>(scratch + COUNTER_BYTES);
-    tf_table_kernel<<<(tf->width + 255) / 256, 256, 0, s>>>(args, d_tf);
+    // The TF's RGBA8 entries are read where the TF object keeps them on the
+    // device; its alpha per alpha byte (vrc_render's host arithmetic) goes into
+    // the scratch array.
+    AlphaArgs args;
+    vrc::tf_alpha_values(vrc::alpha_corrected(p->compositing, p->classification), P.step * 200.f, args.alpha);
+    float* d_alpha = reinterpret_cast<float*>(scratch + COUNTER_BYTES);
+    alpha_table_kernel<<<1, 256, 0, s>>>(args, d_alpha);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_status(e);
-    P.tf_table = d_tf;
+    P.tf_rgba8 = tf->d_rgba8;
+    P.tf_alpha = d_alpha;
     P.tf_width = tf->width;
     P.tf_lo = tf->lo;
     P.tf_hi = tf->hi;

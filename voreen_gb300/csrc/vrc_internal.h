@@ -47,7 +47,13 @@ struct MarchParams {
     const uint32_t* occ_coarse; // optional coarser skip level (one bit per brick); nullptr = single level
     int cshift_coarse;
     int ncc[3];
-    const float4* tf_table;     // (r, g, b, alpha') per TF entry
+    // TF classification: the RGBA8 entries (the CPU path's texel bytes) and,
+    // per alpha byte, the alpha the march composites -- 1-(1-a/255)^(step*200)
+    // for DVR / MIDA, a/255 otherwise (computed on the host with the same powf
+    // the CPU path calls). r/255, g/255, b/255 are formed in the kernel with
+    // the exact 8-bit normalisation.
+    const uchar4* tf_rgba8;
+    const float* tf_alpha;      // 256 entries
     int tf_width;
     BrickLayout L;
     float dimf[3], dim_m1[3], offs[3];
@@ -117,9 +123,11 @@ struct BatchReq {
 // Host helpers shared by the render entry points (api.cpp).
 vrc_status check_params(vrc_context* ctx, const vrc_render_params* p);
 vrc_status fill_params(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, MarchParams& P);
-// Device float4 TF table (r/255, g/255, b/255, alpha'), cached on the TF per
-// (opacity-corrected, correction exponent).
-vrc_status tf_table(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float4** out);
+// Device alpha table of a TF (256 floats, alpha' per alpha byte), cached on
+// the TF per (opacity-corrected, correction exponent).
+vrc_status tf_alpha(vrc_context* ctx, vrc_tf* tf, bool corrected, float kcorr, float** out);
+// The 256 alphas themselves (host): a/255, opacity-corrected when `corrected`.
+void tf_alpha_values(bool corrected, float kcorr, float out[256]);
 
 // Kernel launchers (march.cu / volume.cu). Return cudaError_t.
 cudaError_t launch_march(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
@@ -131,6 +139,9 @@ cudaError_t launch_march_mip_iso(const MarchParams& p, int dtype, int compositin
 cudaError_t launch_march_mop_mida(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                                   cudaStream_t s);
 cudaError_t launch_march_first_hit(const MarchParams& p, int dtype, int compositing, int num_sms, cudaStream_t s);
+// Segmented DVR march (march_segments.cu): four lanes per ray, one segment
+// each, composited front to back; analytic entry/exit, TF classification.
+cudaError_t launch_march_segments(const MarchParams& p, int dtype, int shading, int num_sms, cudaStream_t s);
 // Exact pre-integration table: one thread per (back, front) entry.
 // tb: res float4 TF entries; a8: their alpha bytes; corr[k * 256 + a] =
 // 1 - (1 - a/255)^(step * 200 / (k + 1)).
@@ -261,8 +272,9 @@ struct vrc_tf {
     int width = 0;
     float lo = 0.f, hi = 1.f;
     uint8_t* h_rgba = nullptr;
-    // device float4 tables keyed by (opacity-corrected?, correction exponent bits)
-    std::map<std::pair<int, uint32_t>, float4*> tables;
+    uchar4* d_rgba8 = nullptr;  // the entries on the device
+    // device alpha tables (256 floats) keyed by (opacity-corrected?, correction exponent bits)
+    std::map<std::pair<int, uint32_t>, float*> alpha_tables;
     int* d_prefix = nullptr;  // prefix count of entries with alpha > 0 (width + 1 ints)
     const vrc_preint* preint = nullptr;  // attached pre-integration table (not owned)
 };

@@ -441,13 +441,20 @@ class LearnedRenderer:
     error spread over the frame's content tiles, and below `psnr_bound` the
     frame is rendered by the plain kernel instead (the fallback). The network
     runs on the tcgen05 convolutions (tensor_cores=True) or the mma.sync ones.
-    Everything runs on the context's stream; the only host synchronisation
-    per frame reads the probe's error words and the content map."""
+    The probe tile renders on a side stream through vrc_render_noalloc, in
+    parallel with the low-resolution march and the network (so a caller must
+    not run vrc_render_noalloc concurrently with render()); everything else
+    runs on the context's stream, and the only host synchronisation per frame
+    reads the probe's error words and the content map."""
 
-    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0, tensor_cores: bool = True):
+    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0, tensor_cores: bool = True,
+                 segments: bool = True):
         import torch
         self.ctx, self.net, self.probe, self.bound = ctx, net, probe, psnr_bound
         self.tensor_cores = tensor_cores
+        # the half-resolution input march: each ray in four segments marched
+        # in parallel (vrc_render_aux_segments) or the exact march (vrc_render_aux)
+        self.segments = segments
         self.stream = torch.cuda.ExternalStream(ctx.stream)
         # [probe squared error, probe max |d|, convolution timeout word, unused]
         self.err = torch.zeros(4, dtype=torch.float32, device="cuda")
@@ -455,6 +462,9 @@ class LearnedRenderer:
         self.fallbacks = 0
         self._bufs = {}
         self._scores = None   # per probe-tile mean alpha of the previous frame (host)
+        self._side = None     # stream of the probe tile
+        self._graphs = {}     # (h, w, tensor cores, weights step) -> captured network
+        self.use_graphs = True
 
     def _buf(self, key, shape, dtype):
         import torch
@@ -488,32 +498,99 @@ class LearnedRenderer:
         _check(lib().vrc_render(self.ctx.handle, vol.handle, tf.handle, C.byref(q), None, None, 0, _p(out),
                                 OUT_RGBA32F, 1, None), self.ctx, "vrc_render")
 
+    def _start_probe(self, vol, tf, params, ref, region):
+        """The probe tile of the plain render, started on a side stream so
+        that it runs beside the low-resolution march and the network (it needs
+        only the volume, the TF and the window, known before the frame).
+        vrc_render_noalloc takes the stream explicitly and renders the same
+        pixels as vrc_render; pre-integrated classification, which it does not
+        take, renders the tile on the context stream instead. Returns the
+        event the frame waits for, or None."""
+        import torch
+        from . import CLASSIFY_TF, EE_ANALYTIC, OUT_RGBA32F, render_noalloc
+        if params.classification != CLASSIFY_TF:
+            return None
+        q = low_params(params, 1)
+        q.entry_exit_mode = EE_ANALYTIC
+        q.region[:] = list(region)
+        if self._side is None:
+            self._side = torch.cuda.Stream()
+        # the side stream must not start before the work already queued on
+        # the context stream that produced the volume and TF
+        self._side.wait_stream(self.stream)
+        render_noalloc(vol, tf, q, None, None, ref, OUT_RGBA32F, self._side.cuda_stream)
+        ev = torch.cuda.Event()
+        ev.record(self._side)
+        return ev
+
+    def _network(self, x0, rgba, out, lp):
+        """The U-Net on fixed buffers. The first frame of a size runs it
+        eagerly (which also lays the tcgen05 weights out), the second
+        captures its ~15 launches in a CUDA graph, later frames replay it on
+        the context stream. Capture failure falls back to eager launches."""
+        import torch
+        tc = self.tensor_cores and lp.height % 4 == 0 and lp.width % 4 == 0
+
+        def run():
+            if tc:
+                self.net.infer_tc(x0, rgba, out, err=self.err[2:3])
+            else:
+                self.net.infer(x0, rgba, out)
+
+        key = (lp.height, lp.width, tc, self.net.step)
+        g = self._graphs.get(key)
+        if g == "eager" or not self.use_graphs:
+            run()
+        elif g is None:
+            run()
+            self._graphs[key] = "warm"
+        elif g == "warm":
+            graph = torch.cuda.CUDAGraph()
+            try:
+                torch.cuda.current_stream().synchronize()
+                with torch.cuda.graph(graph):
+                    run()
+                self._graphs[key] = graph
+            except RuntimeError:
+                self._graphs[key] = "eager"
+            if self._graphs[key] == "eager":
+                run()
+            else:
+                graph.replay()
+        else:
+            g.replay()
+
     def render(self, vol, tf, params):
         """Returns (frame (H, W, 4) FP32 device tensor, info dict)."""
         import torch
-        from . import OUT_RGBA32F, _check, lib
+        from . import CLASSIFY_TF, OUT_RGBA32F, PLACE_DEVICE, _check, lib
         lp = low_params(params, 2)
         H, W = params.height, params.width
+        x, y, w, h, content = self.probe_window(W, H)
+        ref = self._buf("probe", (H, W, 4), torch.float32)
+        probe_done = self._start_probe(vol, tf, params, ref, (x, y, w, h))
         with torch.cuda.stream(self.stream):
             rgba = self._buf("rgba", (1, lp.height, lp.width, 4), torch.float32)
             aux = self._buf("aux", (1, lp.height, lp.width, 2), torch.float32)
-            _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None, _p(rgba),
-                                        OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
+            if self.segments and vol.placement == PLACE_DEVICE and params.classification == CLASSIFY_TF:
+                _check(lib().vrc_render_aux_segments(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), _p(rgba),
+                                                     OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux_segments")
+            else:
+                _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None,
+                                            _p(rgba), OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
             out = self._buf("out", (1, H, W, 4), torch.float32)
             self.err.zero_()
             x0 = self._buf("x0", (1, lp.height, lp.width, 16), torch.bfloat16)
             _call("vrc_nn_pack_input", _p(rgba), _p(aux), lp.height * lp.width, _p(x0), _stream())
-            if self.tensor_cores and lp.height % 4 == 0 and lp.width % 4 == 0:
-                self.net.infer_tc(x0, rgba, out, err=self.err[2:3])
-            else:
-                self.net.infer(x0, rgba, out)
+            self._network(x0, rgba, out, lp)
             # content map of this frame (for the next frame's probe), read back with the error words
             ny, nx = max(1, H // self.probe), max(1, W // self.probe)
             scores = self._buf("scores", (ny, nx), torch.float32)
             _call("vrc_nn_tile_alpha", _p(rgba), lp.height, lp.width, self.probe // 2, ny, nx, _p(scores), _stream())
-            x, y, w, h, content = self.probe_window(W, H)
-            ref = self._buf("probe", (H, W, 4), torch.float32)
-            self._render_plain(vol, tf, params, ref, region=(x, y, w, h))
+            if probe_done is None:
+                self._render_plain(vol, tf, params, ref, region=(x, y, w, h))
+            else:
+                self.stream.wait_event(probe_done)
             _call("vrc_nn_probe_error", _p(out), _p(ref), W, x, y, w, h, _p(self.err), _stream())
             host = torch.cat([self.err, scores.reshape(-1)]).cpu()  # the one synchronisation
             se, mx = float(host[0]), float(host[1])
