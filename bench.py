@@ -561,6 +561,7 @@ def run_learned(args, warmup, ws, rank, local):
     end.record(stream)
     end.synchronize()
     ms_plain = start.elapsed_time(end) / steps
+    stages = lr.stage_times(vol, tf, p, steps)
     # quality on a few held-out views of the same volume
     prng = random.Random(4242)
     quality = []
@@ -583,6 +584,7 @@ def run_learned(args, warmup, ws, rank, local):
             "plain_frames_per_s": 1000.0 / ms_plain, "speedup_vs_plain": ms_plain / ms_learned,
             "fallback_rate": sum(1 for i in infos if i["fallback"]) / len(infos),
             "probe_psnr_median": statistics.median(i["probe_psnr"] for i in infos),
+            "stage_ms": stages,
             "quality_held_out": quality}
     if rank == 0:
         print(json.dumps(line))

@@ -459,17 +459,6 @@ vrc_status vrc_render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc
 vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf, const vrc_render_params* p,
                           const float* d_entry, const float* d_exit, void* d_out, int out_format, float* d_aux,
                           vrc_render_stats* stats);
-/* vrc_render_aux with each ray cut into four segments of whole sample steps,
- * marched by four lanes at once and composited front to back (early ray
- * termination applied after every segment). No counterpart in the reference,
- * and not its loop: an approximation for the learned upsampler's
- * half-resolution input march, whose frames are judged by PSNR against the
- * plain render. It shortens the serial sample chain of the longest rays,
- * which bounds a half-resolution frame. Analytic entry/exit, DVR with TF
- * classification and device-resident volumes; VRC_ERR_UNSUPPORTED otherwise. */
-vrc_status vrc_render_aux_segments(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
-                                   const vrc_render_params* p, void* d_out, int out_format, float* d_aux,
-                                   vrc_render_stats* stats);
 
 /* Analytic entry/exit points (texture space) for `p->camera`, written as
  * float4 images, host or device destination. */

@@ -115,7 +115,6 @@ SIGNATURES = {
     "vrc_render": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, C.c_int, VP, C.c_int, C.c_int, P(RenderStats)]),
     "vrc_entry_exit": (C.c_int, [VP, VP, P(RenderParams), VP, VP, C.c_int]),
     "vrc_render_aux": (C.c_int, [VP, VP, VP, P(RenderParams), VP, VP, VP, C.c_int, VP, P(RenderStats)]),
-    "vrc_render_aux_segments": (C.c_int, [VP, VP, VP, P(RenderParams), VP, C.c_int, VP, P(RenderStats)]),
     "vrc_batch_create": (C.c_int, [VP, P(BatchItem), C.c_int, P(VP)]),
     "vrc_batch_create_isolated": (C.c_int, [VP, P(BatchItem), C.c_int, P(C.c_int), P(VP)]),
     "vrc_batch_launch": (C.c_int, [VP]),

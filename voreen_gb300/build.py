@@ -32,7 +32,6 @@ SOURCES = [
     ("march_mip_iso.cu", ["-fmad=false"]),
     ("march_mop_mida.cu", ["-fmad=false"]),
     ("march_first_hit.cu", ["-fmad=false"]),
-    ("march_segments.cu", ["-fmad=false"]),
     ("preint.cu", ["-fmad=false"]),
     ("image.cu", []),
     ("diag.cu", []),
@@ -72,21 +71,28 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compile and link libvrc.so. Environment tuning knobs for the march
     kernel: VRC_MARCH_MIN_BLOCKS (minimum resident CTAs per SM, bounds the
-    registers) and VRC_MARCH_ROUND (loop iterations per lane between refills)."""
+    registers), VRC_MARCH_ROUND (loop iterations per lane between refills)
+    and VRC_MARCH_DEFER (0: shade inline instead of through the per-warp
+    shading queue)."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
     jobs = []
     objs = []
+    stamps = []
     for src, extra in SOURCES:
         path = os.path.join(CSRC, src)
         obj = os.path.join(BUILD, src.replace(".", "_") + ".o")
         objs.append(obj)
-        tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS", "VRC_MARCH_ROUND")
+        tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS", "VRC_MARCH_ROUND", "VRC_MARCH_DEFER")
                 if src.startswith("march") and os.environ.get(k)]
         extra = extra + tune
-        force_this = bool(tune)
+        # an object is rebuilt when its tuning flags differ from the last build's
+        stamp = obj + ".flags"
+        flags = " ".join(tune)
+        force_this = (open(stamp).read() if os.path.exists(stamp) else "") != flags
         if force or force_this or _stale(obj, [path] + hdrs):
+            stamps.append((stamp, flags))
             cmd = [cc, *ARCH, *COMMON, *extra, "-c", path, "-o", obj]
             if src.endswith(".cpp"):
                 cmd.insert(1, "-x")
@@ -105,6 +111,9 @@ def build(verbose: bool = False, force: bool = False) -> str:
         for err in ex.map(run, jobs):
             if verbose and err:
                 print(err)
+    for stamp, flags in stamps:
+        with open(stamp, "w") as f:
+            f.write(flags)
     if force or jobs or _stale(LIB, objs):
         run([cc, *ARCH, "-shared", "-o", LIB, *objs, "-Xcompiler", "-fopenmp", "-lgomp"])
     return LIB

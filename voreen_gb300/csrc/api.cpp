@@ -1072,7 +1072,7 @@ vrc_status prepare_brick_cache(vrc_context* ctx, vrc_volume* vol, const int* occ
 
 vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf_c, const vrc_render_params* p,
                        const float* entry, const float* exitp, int ee_on_device, void* out, int out_format,
-                       int out_on_device, float* aux, vrc_render_stats* stats, bool segments = false) {
+                       int out_on_device, float* aux, vrc_render_stats* stats) {
     if (!ctx) return VRC_ERR_INVALID_ARG;
     if (!vol || !tf_c) return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: volume and transfer function are required");
     if (vol->ctx != ctx || tf_c->ctx != ctx) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: handle from another context");
@@ -1083,11 +1083,6 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: unknown output format");
     if (p->entry_exit_mode == VRC_EE_BUFFERS && (!entry || !exitp))
         return fail(ctx, VRC_ERR_NOT_READY, "vrc_render: entry/exit points are required in buffer mode");
-    if (segments && (p->entry_exit_mode != VRC_EE_ANALYTIC || p->compositing != VRC_DVR ||
-                     p->classification != VRC_CLASSIFY_TF || vol->h_bricks))
-        return fail(ctx, VRC_ERR_UNSUPPORTED,
-                    "vrc_render_aux_segments: analytic entry/exit, DVR, TF classification and a device-resident "
-                    "volume only");
     vrc_tf* tf = const_cast<vrc_tf*>(tf_c);
     VRC_CUDA(ctx, cudaSetDevice(ctx->device));
     MarchParams P;
@@ -1249,10 +1244,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     P.status = reinterpret_cast<int*>(ctx->d_counters + 4);
     P.tile_counter = reinterpret_cast<unsigned int*>(ctx->d_counters + 5);
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[1], s));
-    if (segments)
-        VRC_CUDA(ctx, vrc::launch_march_segments(P, vol->desc.dtype, p->shading, ctx->num_sms, s));
-    else
-        VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
+    VRC_CUDA(ctx, vrc::launch_march(P, vol->desc.dtype, p->compositing, p->shading, ctx->num_sms, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[2], s));
     if (!out_on_device && !mout) VRC_CUDA(ctx, cudaMemcpyAsync(out, P.out, npix * px_bytes, cudaMemcpyDeviceToHost, s));
     VRC_CUDA(ctx, cudaEventRecord(ctx->ev[3], s));
@@ -1288,13 +1280,6 @@ vrc_status vrc_render_aux(vrc_context* ctx, const vrc_volume* vol, const vrc_tf*
                           vrc_render_stats* stats) {
     if (!d_aux) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render_aux: null aux image");
     return render_impl(ctx, vol, tf, p, d_entry, d_exit, 1, d_out, out_format, 1, d_aux, stats);
-}
-
-vrc_status vrc_render_aux_segments(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
-                                   const vrc_render_params* p, void* d_out, int out_format, float* d_aux,
-                                   vrc_render_stats* stats) {
-    if (!d_aux) return fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render_aux_segments: null aux image");
-    return render_impl(ctx, vol, tf, p, nullptr, nullptr, 1, d_out, out_format, 1, d_aux, stats, true);
 }
 
 vrc_status vrc_entry_exit(vrc_context* ctx, const vrc_volume* vol, const vrc_render_params* p, float* entry,

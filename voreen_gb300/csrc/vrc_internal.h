@@ -139,9 +139,6 @@ cudaError_t launch_march_mip_iso(const MarchParams& p, int dtype, int compositin
 cudaError_t launch_march_mop_mida(const MarchParams& p, int dtype, int compositing, int shading, int num_sms,
                                   cudaStream_t s);
 cudaError_t launch_march_first_hit(const MarchParams& p, int dtype, int compositing, int num_sms, cudaStream_t s);
-// Segmented DVR march (march_segments.cu): four lanes per ray, one segment
-// each, composited front to back; analytic entry/exit, TF classification.
-cudaError_t launch_march_segments(const MarchParams& p, int dtype, int shading, int num_sms, cudaStream_t s);
 // Exact pre-integration table: one thread per (back, front) entry.
 // tb: res float4 TF entries; a8: their alpha bytes; corr[k * 256 + a] =
 // 1 - (1 - a/255)^(step * 200 / (k + 1)).

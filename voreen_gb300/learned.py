@@ -447,14 +447,10 @@ class LearnedRenderer:
     runs on the context's stream, and the only host synchronisation per frame
     reads the probe's error words and the content map."""
 
-    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0, tensor_cores: bool = True,
-                 segments: bool = True):
+    def __init__(self, ctx, net: UNet, probe: int = 64, psnr_bound: float = 40.0, tensor_cores: bool = True):
         import torch
         self.ctx, self.net, self.probe, self.bound = ctx, net, probe, psnr_bound
         self.tensor_cores = tensor_cores
-        # the half-resolution input march: each ray in four segments marched
-        # in parallel (vrc_render_aux_segments) or the exact march (vrc_render_aux)
-        self.segments = segments
         self.stream = torch.cuda.ExternalStream(ctx.stream)
         # [probe squared error, probe max |d|, convolution timeout word, unused]
         self.err = torch.zeros(4, dtype=torch.float32, device="cuda")
@@ -563,7 +559,7 @@ class LearnedRenderer:
     def render(self, vol, tf, params):
         """Returns (frame (H, W, 4) FP32 device tensor, info dict)."""
         import torch
-        from . import CLASSIFY_TF, OUT_RGBA32F, PLACE_DEVICE, _check, lib
+        from . import OUT_RGBA32F, _check, lib
         lp = low_params(params, 2)
         H, W = params.height, params.width
         x, y, w, h, content = self.probe_window(W, H)
@@ -572,12 +568,8 @@ class LearnedRenderer:
         with torch.cuda.stream(self.stream):
             rgba = self._buf("rgba", (1, lp.height, lp.width, 4), torch.float32)
             aux = self._buf("aux", (1, lp.height, lp.width, 2), torch.float32)
-            if self.segments and vol.placement == PLACE_DEVICE and params.classification == CLASSIFY_TF:
-                _check(lib().vrc_render_aux_segments(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), _p(rgba),
-                                                     OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux_segments")
-            else:
-                _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None,
-                                            _p(rgba), OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
+            _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None,
+                                        _p(rgba), OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
             out = self._buf("out", (1, H, W, 4), torch.float32)
             self.err.zero_()
             x0 = self._buf("x0", (1, lp.height, lp.width, 16), torch.bfloat16)
@@ -612,6 +604,50 @@ class LearnedRenderer:
                 self._render_plain(vol, tf, params, frame)
         return frame, {"probe_psnr": probe_psnr, "frame_psnr_estimate": frame_psnr, "probe_max_abs": mx,
                        "fallback": fallback, "probe": (x, y, w, h)}
+
+    def stage_times(self, vol, tf, params, steps: int = 20):
+        """Device milliseconds per frame of each stage of render(), each timed
+        alone on the context stream with CUDA events over `steps` repetitions
+        (after one untimed run): the half-resolution half-rate march, the
+        input packing, the network, the probe tile, and the plain full frame
+        a fallback adds. Call after render() has run at this size,
+        so that the network is captured."""
+        import torch
+        from . import OUT_RGBA32F, _check, lib
+        lp = low_params(params, 2)
+        H, W = params.height, params.width
+        rgba = self._buf("rgba", (1, lp.height, lp.width, 4), torch.float32)
+        aux = self._buf("aux", (1, lp.height, lp.width, 2), torch.float32)
+        x0 = self._buf("x0", (1, lp.height, lp.width, 16), torch.bfloat16)
+        out = self._buf("out", (1, H, W, 4), torch.float32)
+        ref = self._buf("probe", (H, W, 4), torch.float32)
+        full = self._buf("fallback", (H, W, 4), torch.float32)
+        x, y, w, h, _ = self.probe_window(W, H)
+
+        def march():
+            _check(lib().vrc_render_aux(self.ctx.handle, vol.handle, tf.handle, C.byref(lp), None, None, _p(rgba),
+                                        OUT_RGBA32F, _p(aux), None), self.ctx, "vrc_render_aux")
+
+        stages = {
+            "march_half": march,
+            "pack_input": lambda: _call("vrc_nn_pack_input", _p(rgba), _p(aux), lp.height * lp.width, _p(x0),
+                                        _stream()),
+            "network": lambda: self._network(x0, rgba, out, lp),
+            "probe_tile": lambda: self._render_plain(vol, tf, params, ref, region=(x, y, w, h)),
+            "plain_frame": lambda: self._render_plain(vol, tf, params, full),
+        }
+        res = {}
+        with torch.cuda.stream(self.stream):
+            for name, fn in stages.items():
+                fn()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(self.stream)
+                for _ in range(steps):
+                    fn()
+                b.record(self.stream)
+                b.synchronize()
+                res[name] = a.elapsed_time(b) / steps
+        return res
 
 
 # ---- training on pairs the plain raycaster renders ---------------------------
