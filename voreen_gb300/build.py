@@ -71,9 +71,7 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compile and link libvrc.so. Environment tuning knobs for the march
     kernel: VRC_MARCH_MIN_BLOCKS (minimum resident CTAs per SM, bounds the
-    registers), VRC_MARCH_ROUND (loop iterations per lane between refills)
-    and VRC_MARCH_DEFER (0: shade inline instead of through the per-warp
-    shading queue)."""
+    registers)."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
@@ -84,7 +82,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         path = os.path.join(CSRC, src)
         obj = os.path.join(BUILD, src.replace(".", "_") + ".o")
         objs.append(obj)
-        tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS", "VRC_MARCH_ROUND", "VRC_MARCH_DEFER")
+        tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS",)
                 if src.startswith("march") and os.environ.get(k)]
         extra = extra + tune
         # an object is rebuilt when its tuning flags differ from the last build's

@@ -49,21 +49,34 @@ __device__ __forceinline__ float a_(float a, float b) { return __fadd_rn(a, b); 
 __device__ __forceinline__ float s_(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); }
 
+// Exact voxel normalisation v / 255 and v / 65535 (VolumeRAM's
+// getVoxelNormalized: float division, correctly rounded), without a
+// division or an integer-to-float conversion instruction.
+// For D = 2^k - 1, 1/D = 2^-k (1 + 2^-k + 2^-2k + ...), so
+//   v / D = v (2^-k + 2^-2k) + v (2^-3k [+ 2^-4k + 2^-5k for k = 8]) + tail,
+// tail >= 0 and smaller than the spacing of the fused sum's grid (2^-48 for
+// k = 16, 2^-40 for k = 8). The fused sum lies on that grid, as do all
+// rounding midpoints of the result, and it is never a midpoint itself (v
+// would need a factor 2^(e + 3k) for a result in [2^e, 2^(e+1))), so the tail
+// cannot change the rounding: fma(v, A, v * B) = RN(v / D) for every v in
+// [0, D]. (Checked exhaustively by the test suite.) v as a float: the bits
+// 0x4B000000 | v are the float 2^23 + v.
+__device__ __forceinline__ float small_uint_to_float(unsigned v) {
+    return __fsub_rn(__int_as_float(0x4B000000u | v), 8388608.f);
+}
 template <int DT> struct Vox;
 template <> struct Vox<VRC_U8> {
     using T = uint8_t;
     static __device__ __forceinline__ float norm(T v) {
-        const float x = (float)v, r = 1.f / 255.f;
-        const float q0 = __fmul_rn(x, r);
-        return __fmaf_rn(__fmaf_rn(-q0, 255.f, x), r, q0);
+        const float x = small_uint_to_float(v);
+        return __fmaf_rn(x, 0x1.01p-8f, __fmul_rn(x, 0x1.0101p-24f));
     }
 };
 template <> struct Vox<VRC_U16> {
     using T = uint16_t;
     static __device__ __forceinline__ float norm(T v) {
-        const float x = (float)v, r = 1.f / 65535.f;
-        const float q0 = __fmul_rn(x, r);
-        return __fmaf_rn(__fmaf_rn(-q0, 65535.f, x), r, q0);
+        const float x = small_uint_to_float(v);
+        return __fmaf_rn(x, 0x1.0001p-16f, __fmul_rn(x, 0x1p-48f));
     }
 };
 template <> struct Vox<VRC_F32> {
@@ -644,8 +657,11 @@ __device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_t
         bool skip_after = false;  // pre-integration: skip the samples after this one in its empty cell
         float skip_lim = 0.f;
         if (P.occupancy) {
-            // Two skip levels: a whole empty brick-sized cell first, else an
-            // empty fine cell (8^3 by default); both words are loaded at once.
+            // Two skip levels. The fine cell (8^3 by default) decides whether
+            // the sample is skipped at all: a coarse (brick-sized) cell holds
+            // its fine cells' value ranges, so it can be empty only where the
+            // fine cell is, and its word is read only then, to jump the whole
+            // coarse cell at once.
             float tsafe = 0.f;
             bool empty = false;
             // cell and brick indices fit 32 bits (checked when the volume is uploaded)
@@ -655,19 +671,22 @@ __device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_t
             constexpr bool MIPS = COMP == VRC_MIP;
             const bool mip_skip = MIPS && P.mip_skip;
             const float fine_max = mip_skip ? __ldg(P.cell_max + fc) : 0.f;
-            if (P.occ_coarse) {
-                const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
-                const unsigned c = ((unsigned)cz * (unsigned)P.ncc[1] + (unsigned)cy) * (unsigned)P.ncc[0] + (unsigned)cx;
-                const uint32_t coarse_word = __ldg(P.occ_coarse + (c >> 5));
-                const float coarse_max = mip_skip ? __ldg(P.brick_max + c) : 0.f;
-                if (((coarse_word >> (c & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, coarse_max, max_int))) {
-                    tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift_coarse, P.ncc);
-                    empty = true;
-                }
-            }
-            if (!empty && (((fine_word >> (fc & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, fine_max, max_int)))) {
-                tsafe = cell_exit_t(P, f, dx, dy, dz, fcx, fcy, fcz, P.cshift, P.nc);
+            if (((fine_word >> (fc & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, fine_max, max_int))) {
                 empty = true;
+                bool coarse_empty = false;
+                if (P.occ_coarse) {
+                    const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
+                    const unsigned c =
+                        ((unsigned)cz * (unsigned)P.ncc[1] + (unsigned)cy) * (unsigned)P.ncc[0] + (unsigned)cx;
+                    const uint32_t coarse_word = __ldg(P.occ_coarse + (c >> 5));
+                    const float coarse_max = mip_skip ? __ldg(P.brick_max + c) : 0.f;
+                    if (((coarse_word >> (c & 31)) & 1u) == 0u ||
+                        (mip_skip && mip_cell_below(P, coarse_max, max_int))) {
+                        tsafe = cell_exit_t(P, f, dx, dy, dz, cx, cy, cz, P.cshift_coarse, P.ncc);
+                        coarse_empty = true;
+                    }
+                }
+                if (!coarse_empty) tsafe = cell_exit_t(P, f, dx, dy, dz, fcx, fcy, fcz, P.cshift, P.nc);
             }
             if (PI && empty && P.pi_chain && prev_empty) {
                 // This sample and the previous one lie in empty cells that
