@@ -103,3 +103,31 @@ def test_network_beats_bilinear_on_held_out_volumes(ctx, net):
     assert np.mean(gain) > 0.2, gain
     for vol, _, _ in vols:
         vol.close()
+
+
+def test_probe_beyond_the_noalloc_scratch_renders_on_the_context_stream(ctx, net):
+    """The probe tile renders on a side stream through vrc_render_noalloc,
+    whose fixed scratch holds at most NOALLOC_MAX_CELLS empty-space cells.
+    A volume with more cells (here 4^3 cells of a 520^3 volume: 2,197,000)
+    makes vrc_render_noalloc return VRC_ERR_SCRATCH_LIMIT; the renderer then
+    renders the tile on the context stream, and the fallback frame is still
+    the plain render."""
+    torch = pytest.importorskip("torch")
+    from voreen_gb300 import learned
+    w = synth.config2(seed=5, size=(520, 520, 520), image=(320, 192))
+    vol = v.Volume(ctx, w.voxels, w.spacing)
+    tf = v.TransferFunction(ctx, v.TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
+    p = w.params(skip_cell_size=4, entry_exit_mode=v.EE_ANALYTIC)
+    assert (520 // 4) ** 3 > v.NOALLOC_MAX_CELLS
+    ref = torch.zeros((w.height, w.width, 4), dtype=torch.float32, device="cuda")
+    with pytest.raises(v.VrcError, match="SCRATCH_LIMIT"):
+        v.render_noalloc(vol, tf, p, None, None, ref)
+    r = learned.LearnedRenderer(ctx, net, psnr_bound=math.inf)
+    frame, info = r.render(vol, tf, p)
+    torch.cuda.synchronize()
+    assert info["fallback"]
+    assert r._no_side.get(vol.handle.value)
+    plain, _ = learned.plain_frame(ctx, vol, tf, p)
+    assert torch.equal(frame, plain)
+    tf.close()
+    vol.close()

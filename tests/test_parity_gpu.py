@@ -103,10 +103,11 @@ def test_odd_shapes_and_brick_sizes(ctx, dims, brick):
 
 
 @pytest.mark.parametrize("cell,brick,shading", [(8, 32, v.SHADE_NONE), (16, 32, v.SHADE_PHONG), (32, 32, v.SHADE_NONE),
-                                                (8, 16, v.SHADE_PHONG), (64, 64, v.SHADE_NONE)])
+                                                (8, 16, v.SHADE_PHONG), (64, 64, v.SHADE_NONE),
+                                                (4, 32, v.SHADE_PHONG), (4, 16, v.SHADE_NONE)])
 def test_empty_space_skipping_is_exact(ctx, cell, brick, shading):
-    """Skipping empty cells (8^3, 16^3 or whole bricks) leaves every pixel
-    and the sample count unchanged."""
+    """Skipping empty cells (4^3, 8^3, 16^3 or whole bricks) leaves every
+    pixel and the sample count unchanged."""
     w = synth.config2(size=(130, 128, 127), image=(256, 192))
     p = w.params(shading=shading, skip_cell_size=cell)
     tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)

@@ -334,9 +334,9 @@ vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* des
     if ((e = vrc::launch_brick_build(lin, desc->dtype, L, v->d_bricks, ctx->stream)) != cudaSuccess ||
         (e = vrc::launch_brick_minmax(v->d_bricks, desc->dtype, L, v->d_bmin, v->d_bmax, ctx->stream)) != cudaSuccess)
         return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: kernel: ") + cudaGetErrorString(e));
-    // finer empty-space cells (8^3, 16^3) below the brick size
-    for (int li = 0; li < 2; ++li) {
-        const int C = li == 0 ? 8 : 16;
+    // finer empty-space cells (4^3, 8^3, 16^3) below the brick size
+    for (int li = 0; li < 3; ++li) {
+        const int C = 4 << li;
         if (C >= brick_size) continue;
         vrc_cell_level& lv = v->levels[li];
         lv.C = C;
@@ -811,9 +811,9 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
     if (p->tile_width != 0 && p->tile_width != 1 && p->tile_width != 2 && p->tile_width != 4 && p->tile_width != 8 &&
         p->tile_width != 16 && p->tile_width != 32)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: tile_width must be 0, 1, 2, 4, 8, 16 or 32");
-    if (p->skip_cell_size != 0 && p->skip_cell_size != 8 && p->skip_cell_size != 16 && p->skip_cell_size != 32 &&
-        p->skip_cell_size != 64)
-        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 8, 16, 32 or 64");
+    if (p->skip_cell_size != 0 && p->skip_cell_size != 4 && p->skip_cell_size != 8 && p->skip_cell_size != 16 &&
+        p->skip_cell_size != 32 && p->skip_cell_size != 64)
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 4, 8, 16, 32 or 64");
     return VRC_OK;
 }
 

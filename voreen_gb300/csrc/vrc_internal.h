@@ -258,7 +258,7 @@ struct vrc_volume {
     bool lod_on = false;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
-    vrc_cell_level levels[2];  // skip cells of edge 8 and 16 (when smaller than the brick)
+    vrc_cell_level levels[3];  // skip cells of edge 4, 8 and 16 (when smaller than the brick)
     size_t bytes = 0;
     float vmin = 0.f, vmax = 0.f;
 };

@@ -459,6 +459,7 @@ class LearnedRenderer:
         self._bufs = {}
         self._scores = None   # per probe-tile mean alpha of the previous frame (host)
         self._side = None     # stream of the probe tile
+        self._no_side = {}    # volume handle -> the probe tile renders on the context stream
         self._graphs = {}     # (h, w, tensor cores, weights step) -> captured network
         self.use_graphs = True
 
@@ -500,11 +501,12 @@ class LearnedRenderer:
         only the volume, the TF and the window, known before the frame).
         vrc_render_noalloc takes the stream explicitly and renders the same
         pixels as vrc_render; pre-integrated classification, which it does not
-        take, renders the tile on the context stream instead. Returns the
-        event the frame waits for, or None."""
+        take, and volumes with more empty-space cells than its fixed scratch
+        holds (VRC_ERR_SCRATCH_LIMIT) render the tile on the context stream
+        instead. Returns the event the frame waits for, or None."""
         import torch
-        from . import CLASSIFY_TF, EE_ANALYTIC, OUT_RGBA32F, render_noalloc
-        if params.classification != CLASSIFY_TF:
+        from . import CLASSIFY_TF, EE_ANALYTIC, OUT_RGBA32F, VrcError, render_noalloc
+        if params.classification != CLASSIFY_TF or self._no_side.get(vol.handle.value):
             return None
         q = low_params(params, 1)
         q.entry_exit_mode = EE_ANALYTIC
@@ -514,7 +516,13 @@ class LearnedRenderer:
         # the side stream must not start before the work already queued on
         # the context stream that produced the volume and TF
         self._side.wait_stream(self.stream)
-        render_noalloc(vol, tf, q, None, None, ref, OUT_RGBA32F, self._side.cuda_stream)
+        try:
+            render_noalloc(vol, tf, q, None, None, ref, OUT_RGBA32F, self._side.cuda_stream)
+        except VrcError as e:
+            if _abi.STATUS_NAMES.get(e.status) != "VRC_ERR_SCRATCH_LIMIT":
+                raise
+            self._no_side[vol.handle.value] = True
+            return None
         ev = torch.cuda.Event()
         ev.record(self._side)
         return ev
@@ -663,6 +671,19 @@ def random_view(rng, vox, spacing, seed, width=1920, height=1080):
     return w
 
 
+def random_view_tubes(rng, meta, spacing, seed, width=1920, height=1080):
+    """A random orbit camera (closer than the CT family's: tubes are thin) and
+    a random 2-peak TF on the tube intensities of a sparse tube volume;
+    meta = {"dims": (X, Y, Z), "minmax": (lo, hi)} of the uploaded volume.
+    Rate 1.5, Phong, light at the camera, as the large tube workload."""
+    from . import synth
+    keys, domain = synth.tubes_tf(seed, 2, meta["minmax"])
+    pos, focus, near, far = synth.orbit_camera(meta["dims"], spacing, rng.uniform(0, 360), rng.uniform(-60, 60),
+                                               rng.uniform(0.9, 1.5))
+    return synth.Workload("train tubes", None, spacing, keys, 4096, domain, width, height, 1.5, compositing=0,
+                          shading=1, camera_pos=pos, camera_focus=focus, near=near, far=far, light_pos=(*pos, 1.0))
+
+
 def make_pair(ctx, vol, tf, params):
     """(x0 BF16 (1,h,w,16), low rgba (1,h,w,4), target (1,H,W,4)) for one view."""
     lp = low_params(params, 2)
@@ -692,9 +713,10 @@ def crops(x0, base, target, n, size, rng, min_alpha: float = 0.02, tries: int = 
 
 
 def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, crop: int = 96, lr: float = 2e-4,
-          refresh_every: int = 2, log=None, width=1920, height=1080, warmup: int = 200):
+          refresh_every: int = 2, log=None, width=1920, height=1080, warmup: int = 200, view_fn=None):
     """Adam on L1 + SSIM over random crops of pairs rendered on the fly from
-    `volumes` [(Volume, voxels, spacing)] with random cameras and TFs."""
+    `volumes` [(Volume, voxels or meta, spacing)] with random cameras and TFs
+    (view_fn: random_view, the CT family, or random_view_tubes)."""
     import random
     import time
 
@@ -709,7 +731,7 @@ def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, cr
     for it in range(steps):
         if pair is None or it % refresh_every == 0:
             vol, vox, sp = volumes[int(rng.integers(0, len(volumes)))]
-            w = random_view(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
+            w = (view_fn or random_view)(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
             tf = TransferFunction(ctx, TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
             pair = make_pair(ctx, vol, tf, w.params())
             tf.close()
@@ -728,7 +750,7 @@ def train(ctx, net: UNet, volumes, steps: int, seed: int = 0, batch: int = 8, cr
     return hist
 
 
-def evaluate(ctx, net, volumes, views: int, seed: int, width=1920, height=1080):
+def evaluate(ctx, net, volumes, views: int, seed: int, width=1920, height=1080, view_fn=None):
     """PSNR of the learned frame and of the bilinear upsample of the same
     half-resolution march (the method without the network) against the plain
     full render, on `views` random views of `volumes`."""
@@ -742,7 +764,7 @@ def evaluate(ctx, net, volumes, views: int, seed: int, width=1920, height=1080):
     out = []
     for _ in range(views):
         vol, vox, sp = volumes[int(rng.integers(0, len(volumes)))]
-        w = random_view(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
+        w = (view_fn or random_view)(prng, vox, sp, int(rng.integers(0, 1 << 30)), width, height)
         tf = TransferFunction(ctx, TransferFunction.bake(w.tf_keys, w.tf_width), w.domain)
         x0, base, target = make_pair(ctx, vol, tf, w.params())
         y = net.forward(x0, base)
@@ -760,8 +782,11 @@ def _main():
 
     import torch
 
-    from . import Context, Volume, build, synth, synth_volume
+    from . import Context, Volume, build, synth, synth_tubes_device, synth_volume
     ap = argparse.ArgumentParser(description="train / evaluate the learned upsampler")
+    ap.add_argument("--family", default="ct", choices=["ct", "tubes"],
+                    help="ct: 512^3 u16 nested shells (spacing 0.7/0.7/1); tubes: 1024x1024x512 u16 with 125 "
+                         "sparse tubes (the large tube workload's density at an eighth of its voxels)")
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--size", type=int, default=512)
     ap.add_argument("--train-volumes", type=int, default=4)
@@ -783,9 +808,17 @@ def _main():
     def vols(seeds):
         res = []
         for s in seeds:
-            vox = synth_volume(synth.SHELLS, 1, d, 4000 + s)
-            res.append((Volume(ctx, vox, (0.7, 0.7, 1.0)), vox, (0.7, 0.7, 1.0)))
+            if args.family == "tubes":
+                dims = (1024, 1024, 512)
+                vox = synth_tubes_device(dims, 125, 6000 + s)
+                vol = Volume(ctx, vox, (1.0, 1.0, 1.0))
+                res.append((vol, {"dims": dims, "minmax": vol.minmax()}, (1.0, 1.0, 1.0)))
+            else:
+                vox = synth_volume(synth.SHELLS, 1, d, 4000 + s)
+                res.append((Volume(ctx, vox, (0.7, 0.7, 1.0)), vox, (0.7, 0.7, 1.0)))
         return res
+
+    view_fn = random_view_tubes if args.family == "tubes" else random_view
 
     t0 = time.time()
     train_vols = vols(range(args.train_volumes))
@@ -796,10 +829,11 @@ def _main():
     print(json.dumps({"volumes_ready_s": time.time() - t0}), flush=True)
     hist = train(ctx, net, train_vols, args.steps, seed=1, batch=args.batch, crop=args.crop, lr=args.lr,
                  log=lambda r: print(json.dumps(r), flush=True), width=args.width, height=args.height,
-                 warmup=args.warmup)
+                 warmup=args.warmup, view_fn=view_fn)
     torch.cuda.synchronize()
     net.save(args.out)
-    ev = evaluate(ctx, net, held_out, args.eval_views, seed=777, width=args.width, height=args.height)
+    ev = evaluate(ctx, net, held_out, args.eval_views, seed=777, width=args.width, height=args.height,
+                  view_fn=view_fn)
     print(json.dumps({"eval": ev, "mean_psnr_net": sum(e["psnr_net"] for e in ev) / len(ev),
                       "mean_psnr_bilinear": sum(e["psnr_bilinear"] for e in ev) / len(ev),
                       "train_seconds": hist[-1]["seconds"] if hist else 0}), flush=True)
