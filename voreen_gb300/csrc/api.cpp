@@ -236,6 +236,8 @@ vrc_status vrc_context_destroy(vrc_context* c) {
     cudaFree(c->d_out);
     cudaFree(c->d_occ);
     cudaFree(c->d_occ_coarse);
+    cudaFree(c->d_dist);
+    cudaFree(c->d_dist_tmp);
     cudaFree(c->d_prefix);
     cudaFree(c->d_counters);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1173,8 +1175,9 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     }
     int occ_launches = 0;
     if (p->empty_space_skipping) {
-        // skip cells: the requested edge if the volume holds that level, else the brick
-        const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
+        // skip cells: the requested edge if the volume holds that level, else
+        // the brick; by default 4^3, whose runs the distance field keeps long
+        const int want = p->skip_cell_size == 0 ? 4 : p->skip_cell_size;
         const float* cmin = vol->d_bmin;
         const float* cmax = vol->d_bmax;
         int C = vol->L.B;
@@ -1192,15 +1195,28 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         uint32_t lo_bits, hi_bits;
         std::memcpy(&lo_bits, &tf->lo, 4);
         std::memcpy(&hi_bits, &tf->hi, 4);
-        const uint64_t key[6] = {vol->uid, occ_source, (uint64_t)occ_width, lo_bits, hi_bits, (uint64_t)C};
+        // the distance field replaces the coarse level except for MIP's
+        // max-based skipping and pre-integration (whose skips need adjacent
+        // samples: two empty cells apart can hold values between them that a
+        // table entry reaches)
+        const bool mip_skip = p->compositing == VRC_MIP && vol->desc.rwm_scale >= 0.f;
+        const bool use_dist = !mip_skip && p->classification == VRC_CLASSIFY_TF;
+        const uint64_t key[6] = {vol->uid, occ_source, (uint64_t)occ_width, lo_bits, hi_bits,
+                                 (uint64_t)C | (use_dist ? 1ull << 32 : 0ull)};
         const uint32_t* occ_before = ctx->d_occ;
         const uint32_t* coarse_before = ctx->d_occ_coarse;
+        const uint8_t* dist_before = ctx->d_dist;
         VRC_CUDA(ctx, ensure((void**)&ctx->d_occ, &ctx->occ_bytes, vrc::occupancy_bytes(n)));
-        if (C < vol->L.B)
+        if (use_dist) {
+            VRC_CUDA(ctx, ensure((void**)&ctx->d_dist, &ctx->dist_bytes, (size_t)n));
+            VRC_CUDA(ctx, ensure((void**)&ctx->d_dist_tmp, &ctx->dist_tmp_bytes, (size_t)n));
+        }
+        if (C < vol->L.B && !use_dist)
             VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes,
                                  vrc::occupancy_bytes(vol->L.nbricks())));
         const bool cached = std::memcmp(key, ctx->occ_key, sizeof(key)) == 0 && ctx->d_occ == occ_before &&
-                            (C >= vol->L.B || ctx->d_occ_coarse == coarse_before);
+                            (C >= vol->L.B || use_dist || ctx->d_occ_coarse == coarse_before) &&
+                            (!use_dist || ctx->d_dist == dist_before);
         if (!cached) {
             std::memset(ctx->occ_key, 0, sizeof(ctx->occ_key));
             VRC_CUDA(ctx, vrc::launch_occupancy(cmin, cmax, n, occ_prefix, occ_width, vol->desc.rwm_scale,
@@ -1210,7 +1226,7 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         P.occupancy = ctx->d_occ;
         // MIP: cells that cannot raise a ray's maximum are skipped too; that
         // needs a monotone real-world mapping
-        if (p->compositing == VRC_MIP && vol->desc.rwm_scale >= 0.f) {
+        if (mip_skip) {
             P.mip_skip = 1;
             P.cell_max = cmax;
             P.brick_max = vol->d_bmax;
@@ -1219,8 +1235,14 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         for (int i = 0; i < 3; ++i) P.nc[i] = nc[i];
         const int maxdim = std::max(vol->desc.dims[0], std::max(vol->desc.dims[1], vol->desc.dims[2]));
         P.skip_margin = 0.01f + 2e-5f * float(maxdim);
-        if (C < vol->L.B) {
-            // coarse level: whole bricks, tested first
+        if (use_dist) {
+            if (!cached) {
+                VRC_CUDA(ctx, vrc::launch_occ_distance(ctx->d_occ, nc, ctx->d_dist, ctx->d_dist_tmp, s));
+                occ_launches += 3;
+            }
+            P.occ_dist = ctx->d_dist;
+        } else if (C < vol->L.B) {
+            // coarse level: whole bricks, tested where the fine cell is empty
             const long long nb = vol->L.nbricks();
             if (!cached) {
                 VRC_CUDA(ctx, vrc::launch_occupancy(vol->d_bmin, vol->d_bmax, nb, occ_prefix, occ_width,

@@ -439,6 +439,27 @@ __device__ __forceinline__ float cell_exit_t(const MarchParams& P, float4 f, flo
     return tmax;
 }
 
+// The same for a box of cells [c - r, c + r] on each axis (clipped to the
+// grid: a face on the grid's border is never left, samples beyond it clamp
+// to the border cells).
+__device__ __forceinline__ float box_exit_t(const MarchParams& P, float4 f, float dx, float dy, float dz, int cx,
+                                            int cy, int cz, int r, int shift, const int* nc) {
+    const int C = 1 << shift;
+    const float fo[3] = {f.x, f.y, f.z}, di[3] = {dx, dy, dz};
+    const int ci[3] = {cx, cy, cz};
+    float tmax = INFINITY;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const float a = P.dimf[i] * fo[i] - 0.5f, b = P.dimf[i] * di[i];
+        if (b > 0.f && ci[i] + r < nc[i] - 1) {
+            tmax = fminf(tmax, __fdividef((float)((ci[i] + r + 1) * C) - P.skip_margin - a, b));
+        } else if (b < 0.f && ci[i] - r > 0) {
+            tmax = fminf(tmax, __fdividef((float)((ci[i] - r) * C) + P.skip_margin - a, b));
+        }
+    }
+    return tmax;
+}
+
 // Advances (t, loop) over the samples of an empty run in closed form: every
 // sample with t <= lim is processed (and changes nothing). The FP32 sum
 // t + step, for t on the grid of its binade [2^(e-1), 2^e) with spacing u,
@@ -674,7 +695,13 @@ __device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_t
             if (((fine_word >> (fc & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, fine_max, max_int))) {
                 empty = true;
                 bool coarse_empty = false;
-                if (P.occ_coarse) {
+                if (P.occ_dist) {
+                    // jump the empty box around the cell that the distance to
+                    // the nearest occupied cell guarantees
+                    const int r = (int)__ldg(P.occ_dist + fc) - 1;
+                    tsafe = box_exit_t(P, f, dx, dy, dz, fcx, fcy, fcz, r, P.cshift, P.nc);
+                    coarse_empty = true;
+                } else if (P.occ_coarse) {
                     const int cx = ix >> P.cshift_coarse, cy = iy >> P.cshift_coarse, cz = iz >> P.cshift_coarse;
                     const unsigned c =
                         ((unsigned)cz * (unsigned)P.ncc[1] + (unsigned)cy) * (unsigned)P.ncc[0] + (unsigned)cx;

@@ -96,7 +96,9 @@ vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_ren
     vrc_status st = vrc::fill_params(nullptr, vol, p, P);
     if (st != VRC_OK) return st;
 
-    // empty-space cells: the requested level, else the brick grid (as vrc_render)
+    // empty-space cells: the requested level, else the brick grid (as
+    // vrc_render); by default 8^3 (one level and no distance field here:
+    // finer cells would only make more, shorter runs)
     const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
     const float* cmin = vol->d_bmin;
     const float* cmax = vol->d_bmax;

@@ -177,6 +177,51 @@ __global__ void occupancy_kernel(const float* bmin, const float* bmax, long long
     }
 }
 
+// Chebyshev distance to the nearest occupied cell, capped at OCC_DIST_CAP:
+// d(c) = min over occupied o of max(|cx-ox|, |cy-oy|, |cz-oz|). The max of
+// the axis offsets composes per axis, so three passes give it exactly:
+// along x the distance to the nearest occupied cell of the row, then along
+// y and along z the min over offsets k of max(|k|, previous pass at c + k).
+// Offsets beyond the cap only give values above it, so each pass looks at
+// |k| < OCC_DIST_CAP. One thread per cell; consecutive threads take
+// consecutive x, so every pass reads coalesced.
+__global__ void occ_dist_x_kernel(const uint32_t* __restrict__ occ, int nx, int ny, int nz, uint8_t* __restrict__ out) {
+    const long long n = (long long)nx * ny * nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const int x = (int)(c % nx);
+        const long long row = c - x;
+        int d = OCC_DIST_CAP;
+        for (int k = 0; k < OCC_DIST_CAP && k < d; ++k) {
+            const int xa = x - k, xb = x + k;
+            if (xa >= 0) {
+                const long long i = row + xa;
+                if ((__ldg(occ + (i >> 5)) >> (i & 31)) & 1u) d = k;
+            }
+            if (xb < nx && d > k) {
+                const long long i = row + xb;
+                if ((__ldg(occ + (i >> 5)) >> (i & 31)) & 1u) d = k;
+            }
+        }
+        out[c] = (uint8_t)d;
+    }
+}
+
+__global__ void occ_dist_axis_kernel(const uint8_t* __restrict__ in, int nx, int ny, int nz, int axis,
+                                     uint8_t* __restrict__ out) {
+    const long long n = (long long)nx * ny * nz;
+    const long long stride = axis == 1 ? nx : (long long)nx * ny;
+    const int len = axis == 1 ? ny : nz;
+    for (long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x) {
+        const int pos = axis == 1 ? (int)((c / nx) % ny) : (int)(c / ((long long)nx * ny));
+        int d = __ldg(in + c);
+        for (int k = 1; k < d; ++k) {
+            if (pos - k >= 0) d = min(d, max(k, (int)__ldg(in + c - k * stride)));
+            if (pos + k < len) d = min(d, max(k, (int)__ldg(in + c + k * stride)));
+        }
+        out[c] = (uint8_t)d;
+    }
+}
+
 int grid_for(long long n, int block) {
     long long g = (n + block - 1) / block;
     if (g > 152LL * 64) g = 152LL * 64;
@@ -297,6 +342,15 @@ cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long nce
                              uint32_t* occ, cudaStream_t s) {
     occupancy_kernel<<<grid_for((ncells + 31) / 32, 128), 128, 0, s>>>(bmin, bmax, ncells, alpha_prefix, tf_width,
                                                                        rwm_scale, rwm_offset, tf_lo, tf_hi, occ);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_occ_distance(const uint32_t* occ, const int nc[3], uint8_t* dist, uint8_t* tmp, cudaStream_t s) {
+    const long long n = (long long)nc[0] * nc[1] * nc[2];
+    const int g = grid_for(n, 256);
+    occ_dist_x_kernel<<<g, 256, 0, s>>>(occ, nc[0], nc[1], nc[2], dist);
+    occ_dist_axis_kernel<<<g, 256, 0, s>>>(dist, nc[0], nc[1], nc[2], 1, tmp);
+    occ_dist_axis_kernel<<<g, 256, 0, s>>>(tmp, nc[0], nc[1], nc[2], 2, dist);
     return cudaGetLastError();
 }
 

@@ -47,6 +47,11 @@ struct MarchParams {
     const uint32_t* occ_coarse; // optional coarser skip level (one bit per brick); nullptr = single level
     int cshift_coarse;
     int ncc[3];
+    // optional, per skip cell: Chebyshev distance in cells to the nearest
+    // occupied cell, capped at OCC_DIST_CAP (an empty cell at distance d is
+    // the centre of an empty box of (2d - 1)^3 cells); used instead of the
+    // coarse level when set, nullptr = off
+    const uint8_t* occ_dist;
     // TF classification: the RGBA8 entries (the CPU path's texel bytes) and,
     // per alpha byte, the alpha the march composites -- 1-(1-a/255)^(step*200)
     // for DVR / MIDA, a/255 otherwise (computed on the host with the same powf
@@ -101,6 +106,8 @@ struct MarchParams {
     uint32_t* brick_used;        // one bit per brick touched by a sample or tap, nullptr = not tracked
     float mida_gamma;            // "gammaValue" of MIDA compositing
 };
+
+constexpr int OCC_DIST_CAP = 16;
 
 // Internal compositing code of the march kernels: DVR with pre-integrated
 // classification (no opacity correction, classify(previous, current)).
@@ -172,6 +179,9 @@ cudaError_t launch_cell_minmax(const void* linear, int dtype, const int dims[3],
 cudaError_t launch_occupancy(const float* bmin, const float* bmax, long long ncells, const int* alpha_prefix,
                              int tf_width, float rwm_scale, float rwm_offset, float tf_lo, float tf_hi,
                              uint32_t* occ, cudaStream_t s);
+// occ_dist from the occupancy bits of an nc[0] x nc[1] x nc[2] cell grid
+// (three separable passes; tmp holds as many bytes as dist).
+cudaError_t launch_occ_distance(const uint32_t* occ, const int nc[3], uint8_t* dist, uint8_t* tmp, cudaStream_t s);
 inline size_t occupancy_bytes(long long ncells) { return (size_t)((ncells + 31) / 32) * 4; }
 
 // Process-unique id of a volume, TF or pre-integration table: identifies
@@ -199,6 +209,9 @@ struct vrc_context {
     size_t occ_bytes = 0;
     uint32_t* d_occ_coarse = nullptr;
     size_t occ_coarse_bytes = 0;
+    uint8_t* d_dist = nullptr;       // occ_dist of the skip cells, and the passes' scratch
+    uint8_t* d_dist_tmp = nullptr;
+    size_t dist_bytes = 0, dist_tmp_bytes = 0;
     int* d_prefix = nullptr;
     size_t prefix_bytes = 0;
     unsigned long long* d_counters = nullptr;  // 4 counters + status + tile counter
