@@ -322,8 +322,8 @@ typedef struct {
     int entry_exit_mode;        /* vrc_entry_exit_mode */
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
-    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (4 for vrc_render, 8 for the
-                                   no-alloc and batched paths), else 4, 8, 16 or the brick size */
+    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (4; 8 for vrc_render_noalloc),
+                                   else 4, 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
     int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
     int classification;         /* vrc_classification, default VRC_CLASSIFY_TF */

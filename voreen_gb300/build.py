@@ -71,7 +71,8 @@ def _stale(target: str, deps: list[str]) -> bool:
 def build(verbose: bool = False, force: bool = False) -> str:
     """Compile and link libvrc.so. Environment tuning knobs for the march
     kernel: VRC_MARCH_MIN_BLOCKS (minimum resident CTAs per SM, bounds the
-    registers)."""
+    registers) and VRC_OCC_DIST_CAP (largest empty-space distance stored per
+    cell, at most 255)."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
@@ -84,6 +85,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         objs.append(obj)
         tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS",)
                 if src.startswith("march") and os.environ.get(k)]
+        tune += [f"-DVRC_OCC_DIST_CAP={int(os.environ['VRC_OCC_DIST_CAP'])}"] if os.environ.get("VRC_OCC_DIST_CAP") else []
         extra = extra + tune
         # an object is rebuilt when its tuning flags differ from the last build's
         stamp = obj + ".flags"

@@ -20,7 +20,8 @@ struct vrc_batch {
     vrc::BatchReq* d_reqs = nullptr;
     unsigned* d_prefix = nullptr;
     unsigned long long* d_state = nullptr;  // [tile counter, start ns, samples, end ns per launch position]
-    std::vector<uint32_t*> occ;             // per request: fine and coarse bitmaps
+    std::vector<uint32_t*> occ;             // per request: the cell bitmap
+    std::vector<uint8_t*> dist;             // per request: the cells' distance field; one shared scratch last
     unsigned total_tiles = 0;
     int kernels = 0;
     cudaGraph_t graph = nullptr;
@@ -42,6 +43,7 @@ void release(vrc_batch* b) {
     cudaFree(b->d_prefix);
     cudaFree(b->d_state);
     for (auto* p : b->occ) cudaFree(p);
+    for (auto* p : b->dist) cudaFree(p);
     delete b;
 }
 
@@ -125,8 +127,11 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         uint32_t* map;
         const vrc_tf* tf;
         const vrc_volume* vol;
+        uint8_t* dist;
+        int nc[3];
     };
     std::vector<Occ> occ_jobs;
+    long long max_cells = 0;
     for (int i = 0; i < n; ++i) {
         const vrc_batch_item& it = items[i];
         vrc::BatchReq& R = reqs[i];
@@ -151,37 +156,30 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         R.P.out = it.out;
         R.P.out_format = it.out_format;
         if (it.params.empty_space_skipping) {
+            // as vrc_render: 4^3 cells by default, and the cells' distance
+            // field, so an empty run jumps the whole empty box around its cell
             const float *mn, *mx;
             int C, nc[3];
-            pick_level(it.volume, it.params.skip_cell_size == 0 ? 8 : it.params.skip_cell_size, &mn, &mx, &C, nc);
+            pick_level(it.volume, it.params.skip_cell_size == 0 ? 4 : it.params.skip_cell_size, &mn, &mx, &C, nc);
             const long long cells = (long long)nc[0] * nc[1] * nc[2];
             uint32_t* map = nullptr;
-            if ((e = cudaMalloc((void**)&map, vrc::occupancy_bytes(cells))) != cudaSuccess) {
+            uint8_t* dist = nullptr;
+            if ((e = cudaMalloc((void**)&map, vrc::occupancy_bytes(cells))) == cudaSuccess) b->occ.push_back(map);
+            if (e == cudaSuccess && (e = cudaMalloc((void**)&dist, (size_t)cells)) == cudaSuccess) b->dist.push_back(dist);
+            if (e != cudaSuccess) {
                 release(b);
                 return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: occupancy allocation");
             }
-            b->occ.push_back(map);
-            occ_jobs.push_back({mn, mx, cells, map, it.tf, it.volume});
+            occ_jobs.push_back({mn, mx, cells, map, it.tf, it.volume, dist, {nc[0], nc[1], nc[2]}});
+            max_cells = std::max(max_cells, cells);
             R.P.occupancy = map;
+            R.P.occ_dist = dist;
             int sh = 0;
             while ((1 << sh) < C) ++sh;
             R.P.cshift = sh;
             for (int k = 0; k < 3; ++k) R.P.nc[k] = nc[k];
             const int maxdim = std::max(it.volume->desc.dims[0], std::max(it.volume->desc.dims[1], it.volume->desc.dims[2]));
             R.P.skip_margin = 0.01f + 2e-5f * float(maxdim);
-            if (C < it.volume->L.B) {
-                const long long nb = it.volume->L.nbricks();
-                uint32_t* cm = nullptr;
-                if ((e = cudaMalloc((void**)&cm, vrc::occupancy_bytes(nb))) != cudaSuccess) {
-                    release(b);
-                    return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: occupancy allocation");
-                }
-                b->occ.push_back(cm);
-                occ_jobs.push_back({it.volume->d_bmin, it.volume->d_bmax, nb, cm, it.tf, it.volume});
-                R.P.occ_coarse = cm;
-                R.P.cshift_coarse = it.volume->L.shift;
-                for (int k = 0; k < 3; ++k) R.P.ncc[k] = it.volume->L.nb[k];
-            }
         }
         const int maxdim = std::max(it.volume->desc.dims[0], std::max(it.volume->desc.dims[1], it.volume->desc.dims[2]));
         cost[i] = double(it.params.width) * it.params.height * maxdim * it.params.sampling_rate;
@@ -214,6 +212,15 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
     }
+    // scratch of the distance passes, shared by the requests (the graph runs them in order)
+    uint8_t* dist_tmp = nullptr;
+    if (max_cells > 0) {
+        if ((e = cudaMalloc((void**)&dist_tmp, (size_t)max_cells)) != cudaSuccess) {
+            release(b);
+            return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: distance scratch allocation");
+        }
+        b->dist.push_back(dist_tmp);
+    }
     // capture: state reset + start stamp, empty-space maps, one persistent march
     cudaStream_t s = ctx->stream;
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
@@ -221,10 +228,12 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture: ") + cudaGetErrorString(e));
     }
     cudaError_t ce = vrc::launch_batch_begin(b->d_state, n, s);
-    for (const Occ& j : occ_jobs)
+    for (const Occ& j : occ_jobs) {
         if (ce == cudaSuccess)
             ce = vrc::launch_occupancy(j.mn, j.mx, j.cells, j.tf->d_prefix, j.tf->width, j.vol->desc.rwm_scale,
                                        j.vol->desc.rwm_offset, j.tf->lo, j.tf->hi, j.map, s);
+        if (ce == cudaSuccess) ce = vrc::launch_occ_distance(j.map, j.nc, j.dist, dist_tmp, s);
+    }
     if (ce == cudaSuccess)
         ce = vrc::launch_march_batch(b->d_reqs, n, b->d_prefix, b->total_tiles, b->d_state, b->compositing,
                                      b->shading, ctx->num_sms, s);
@@ -234,7 +243,7 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture failed: ") +
                                             cudaGetErrorString(ce != cudaSuccess ? ce : e));
     }
-    b->kernels = 2 + (int)occ_jobs.size();
+    b->kernels = 2 + 4 * (int)occ_jobs.size();
     if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) {
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: instantiate: ") + cudaGetErrorString(e));

@@ -107,7 +107,10 @@ struct MarchParams {
     float mida_gamma;            // "gammaValue" of MIDA compositing
 };
 
-constexpr int OCC_DIST_CAP = 16;
+#ifndef VRC_OCC_DIST_CAP
+#define VRC_OCC_DIST_CAP 16
+#endif
+constexpr int OCC_DIST_CAP = VRC_OCC_DIST_CAP;
 
 // Internal compositing code of the march kernels: DVR with pre-integrated
 // classification (no opacity correction, classify(previous, current)).
