@@ -1195,14 +1195,18 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
         uint32_t lo_bits, hi_bits;
         std::memcpy(&lo_bits, &tf->lo, 4);
         std::memcpy(&hi_bits, &tf->hi, 4);
-        // the distance field replaces the coarse level except for MIP's
-        // max-based skipping and pre-integration (whose skips need adjacent
-        // samples: two empty cells apart can hold values between them that a
-        // table entry reaches)
+        // The distance field serves TF-empty cells, and replaces the coarse
+        // (brick) level unless MIP's max-based skipping needs the bricks' max.
+        // Pre-integration takes it only when a step moves less than a voxel
+        // per axis: consecutive samples in an all-empty box then lie in the
+        // same or adjacent empty cells, whose value ranges overlap, so every
+        // table entry between them has alpha 0 (with longer steps two empty
+        // cells apart can hold values between them that an entry reaches).
         const bool mip_skip = p->compositing == VRC_MIP && vol->desc.rwm_scale >= 0.f;
-        const bool use_dist = !mip_skip && p->classification == VRC_CLASSIFY_TF;
+        const bool use_dist = p->classification == VRC_CLASSIFY_TF || P.pi_chain;
+        const bool use_coarse = C < vol->L.B && (!use_dist || mip_skip);
         const uint64_t key[6] = {vol->uid, occ_source, (uint64_t)occ_width, lo_bits, hi_bits,
-                                 (uint64_t)C | (use_dist ? 1ull << 32 : 0ull)};
+                                 (uint64_t)C | (use_dist ? 1ull << 32 : 0ull) | (use_coarse ? 1ull << 33 : 0ull)};
         const uint32_t* occ_before = ctx->d_occ;
         const uint32_t* coarse_before = ctx->d_occ_coarse;
         const uint8_t* dist_before = ctx->d_dist;
@@ -1211,11 +1215,11 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
             VRC_CUDA(ctx, ensure((void**)&ctx->d_dist, &ctx->dist_bytes, (size_t)n));
             VRC_CUDA(ctx, ensure((void**)&ctx->d_dist_tmp, &ctx->dist_tmp_bytes, (size_t)n));
         }
-        if (C < vol->L.B && !use_dist)
+        if (use_coarse)
             VRC_CUDA(ctx, ensure((void**)&ctx->d_occ_coarse, &ctx->occ_coarse_bytes,
                                  vrc::occupancy_bytes(vol->L.nbricks())));
         const bool cached = std::memcmp(key, ctx->occ_key, sizeof(key)) == 0 && ctx->d_occ == occ_before &&
-                            (C >= vol->L.B || use_dist || ctx->d_occ_coarse == coarse_before) &&
+                            (!use_coarse || ctx->d_occ_coarse == coarse_before) &&
                             (!use_dist || ctx->d_dist == dist_before);
         if (!cached) {
             std::memset(ctx->occ_key, 0, sizeof(ctx->occ_key));
@@ -1241,7 +1245,8 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
                 occ_launches += 3;
             }
             P.occ_dist = ctx->d_dist;
-        } else if (C < vol->L.B) {
+        }
+        if (use_coarse) {
             // coarse level: whole bricks, tested where the fine cell is empty
             const long long nb = vol->L.nbricks();
             if (!cached) {

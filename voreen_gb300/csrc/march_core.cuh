@@ -692,10 +692,11 @@ __device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_t
             constexpr bool MIPS = COMP == VRC_MIP;
             const bool mip_skip = MIPS && P.mip_skip;
             const float fine_max = mip_skip ? __ldg(P.cell_max + fc) : 0.f;
-            if (((fine_word >> (fc & 31)) & 1u) == 0u || (mip_skip && mip_cell_below(P, fine_max, max_int))) {
+            const bool fine_bit_empty = ((fine_word >> (fc & 31)) & 1u) == 0u;
+            if (fine_bit_empty || (mip_skip && mip_cell_below(P, fine_max, max_int))) {
                 empty = true;
                 bool coarse_empty = false;
-                if (P.occ_dist) {
+                if (P.occ_dist && fine_bit_empty) {
                     // jump the empty box around the cell that the distance to
                     // the nearest occupied cell guarantees
                     const int r = (int)__ldg(P.occ_dist + fc) - 1;
