@@ -322,8 +322,8 @@ typedef struct {
     int entry_exit_mode;        /* vrc_entry_exit_mode */
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
-    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (4; 8 for vrc_render_noalloc),
-                                   else 4, 8, 16 or the brick size */
+    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (4; in vrc_render_noalloc
+                                   8 when the 4^3 cells exceed its scratch), else 4, 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
     int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
     int classification;         /* vrc_classification, default VRC_CLASSIFY_TF */
@@ -428,15 +428,15 @@ vrc_status vrc_batch_destroy(vrc_batch* b);
  * synchronise the device and stall the frame), or hosts whose device memory
  * belongs to their own fixed-budget pool or to another runtime. It renders
  * like vrc_render but keeps its scratch (sample and tile counters, the
- * per-render alpha table, the empty-space cell map) in one fixed-size array in
- * device global memory that every GPU loading the library holds until exit,
- * and it allocates nothing.
+ * per-render alpha table, the empty-space cell map and its distance field)
+ * in one fixed-size array (4.5 MB) in device global memory that every GPU
+ * loading the library holds until exit, and it allocates nothing.
  * Limits: at most VRC_NOALLOC_MAX_CELLS empty-space cells when skipping is on
- * (a 1024^3 volume at the default 8^3 cells) and TF width <= 4096; larger
- * requests return VRC_ERR_SCRATCH_LIMIT and render nothing. TF
- * classification only (VRC_ERR_UNSUPPORTED otherwise). Frames equal
- * vrc_render's, but empty space is skipped at the requested cell level only
- * (no brick-level pass, no MIP cell skipping), and a host-placed brick pool
+ * (skip_cell_size 0 takes 4^3 cells up to 512^3 voxels and 8^3 cells, up to
+ * a 1024^3 volume, above) and TF width <= 4096; larger requests return
+ * VRC_ERR_SCRATCH_LIMIT and render nothing. TF classification only
+ * (VRC_ERR_UNSUPPORTED otherwise). Frames equal vrc_render's, but MIP's
+ * max-based cell skipping is not taken, and a host-placed brick pool
  * is read in place (no device brick cache, no level of detail), so some
  * frames take longer than vrc_render's.
  * The caller passes the inputs (an uploaded volume, a TF of the same

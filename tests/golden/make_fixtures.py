@@ -8,7 +8,9 @@ Run where the Voreen source tree is available:
 Copied unchanged (data files, not code):
   resource/voreenve/volumes/nucleon.{vvd,raw}   41^3 uint8
   resource/voreenve/volumes/walnut.{vvd,raw}    128x96x114 uint16
+  resource/voreenve/volumes/vessel-tree-noisy.{vvd,raw}   101^3 uint8 (path list, RealWorldMapping 255)
   resource/voreencore/transferfuncs/{nucleon,walnut}.tfi
+  resource/voreencore/transferfuncs/presets/1dkeys/101_Hot Metal.tfi -> hot_metal.tfi
 Extracted from modules/base/test/render/cpuraycaster.vws (the reference's
 CPURaycaster regression workspace) into cpuraycaster_vws.json: the canvas
 size, the MeshEntryExitPoints camera, the proxy mode and, per CPURaycaster
@@ -86,10 +88,12 @@ def main(reference_root=None):
     if not os.path.isdir(vols):
         raise SystemExit(f"Voreen tree not found at {root}")
     os.makedirs(OUT, exist_ok=True)
-    for name in ("nucleon.vvd", "nucleon.raw", "walnut.vvd", "walnut.raw"):
+    for name in ("nucleon.vvd", "nucleon.raw", "walnut.vvd", "walnut.raw", "vessel-tree-noisy.vvd",
+                 "vessel-tree-noisy.raw"):
         shutil.copyfile(os.path.join(vols, name), os.path.join(OUT, name))
     for name in ("nucleon.tfi", "walnut.tfi"):
         shutil.copyfile(os.path.join(tfs, name), os.path.join(OUT, name))
+    shutil.copyfile(os.path.join(tfs, "presets", "1dkeys", "101_Hot Metal.tfi"), os.path.join(OUT, "hot_metal.tfi"))
     case = workspace_case(os.path.join(root, "modules", "base", "test", "render", "cpuraycaster.vws"))
     with open(os.path.join(OUT, "cpuraycaster_vws.json"), "w") as f:
         json.dump(case, f, indent=1)

@@ -1,7 +1,8 @@
 """The reference's own fixed-input cases, rendered on the GPU against the CPU
-oracle: Voreen's sample volumes nucleon (41^3 uint8) and walnut
-(128x96x114 uint16) loaded through vrc_volume_load_vvd with their sample
-transfer functions read by vrc_tf_read_tfi, and the CPURaycaster regression
+oracle: Voreen's sample volumes nucleon (41^3 uint8), walnut
+(128x96x114 uint16) and vessel-tree-noisy (101^3 uint8) loaded through
+vrc_volume_load_vvd with their sample transfer functions (a key preset for
+the vessel tree) read by vrc_tf_read_tfi, and the CPURaycaster regression
 workspace modules/base/test/render/cpuraycaster.vws (nucleon, its 12-key TF,
 camera and canvas; TF and pre-integrated classification). The files are
 copies made by tests/golden/make_fixtures.py.
@@ -110,6 +111,31 @@ def test_sample_volume_with_its_tfi(ctx, name, shading):
     p.shading = shading
     _check(ctx, vol, tf, table, t["domain"], vox, spacing, offset, rwm, p,
            f"{name} + {name}.tfi, 256x224, {'Phong' if shading else 'unshaded'}")
+    tf.close()
+    vol.close()
+
+
+@pytest.mark.parametrize("shading", [v.SHADE_NONE, v.SHADE_PHONG])
+def test_vessel_tree_with_a_preset(ctx, shading):
+    """vessel-tree-noisy (101^3 uint8, a .vvd whose raw file is found through
+    its path list, an explicit RealWorldMapping of 255) with the "Hot Metal"
+    key preset, its domain fitted to the volume's real-world range as
+    TransFunc1DKeysProperty::applyDomainFromData does."""
+    vol, vox, spacing, offset, rwm = _load(ctx, "vessel-tree-noisy")
+    assert vox.shape == (101, 101, 101)
+    t = v.read_tfi(os.path.join(FIX, "hot_metal.tfi"))
+    domain = (float(vox.min()) * rwm[0] / 255.0, float(vox.max()) * rwm[0] / 255.0)
+    width = 256
+    table = _apply_alpha_mode(v.TransferFunction.bake(t["keys"], width, t["gamma"], t["threshold"]), t["alpha_mode"])
+    np.testing.assert_array_equal(table, _apply_alpha_mode(
+        oracle.bake_tf(t["keys"], width, t["gamma"], t["threshold"]), t["alpha_mode"]))
+    tf = v.TransferFunction(ctx, table, domain)
+    p = v.default_params(240, 200)
+    p.camera = _orbit(vol.dims, spacing, offset, -40.0, 30.0)
+    p.light_position[:] = [*p.camera.position, 1.0]
+    p.shading = shading
+    _check(ctx, vol, tf, table, domain, vox, spacing, offset, rwm, p,
+           f"vessel-tree-noisy + Hot Metal preset, 240x200, {'Phong' if shading else 'unshaded'}")
     tf.close()
     vol.close()
 

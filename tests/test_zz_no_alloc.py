@@ -37,7 +37,7 @@ def _frame_pair(ctx, torch, w, p, out_format=v.OUT_RGBA32F):
 
 def test_noalloc_matches_render_on_consecutive_calls(ctx):
     torch = pytest.importorskip("torch")
-    # call 1: shaded DVR with a 4096-entry TF and 8^3 skip cells
+    # call 1: shaded DVR with a 4096-entry TF and the default skip cells (4^3 with the distance field)
     w1 = synth.config2(size=(96, 88, 80), image=(200, 150))
     p1 = w1.params()
     ref1, got1, keep1 = _frame_pair(ctx, torch, w1, p1)
@@ -54,7 +54,7 @@ def test_noalloc_matches_render_on_consecutive_calls(ctx):
 
 def test_noalloc_refuses_requests_beyond_its_scratch(ctx):
     torch = pytest.importorskip("torch")
-    # 1040^3 voxels at 8^3 cells = 130^3 cells > VRC_NOALLOC_MAX_CELLS
+    # 1040^3 voxels: the default takes 8^3 cells (4^3 would be 260^3), and 130^3 cells > VRC_NOALLOC_MAX_CELLS
     vox = np.zeros((1040, 1040, 1040), np.uint8)
     vox[500:540, 500:540, 500:540] = 200
     vol = v.Volume(ctx, vox)

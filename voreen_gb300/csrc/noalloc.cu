@@ -5,8 +5,9 @@
 // host application whose device memory is handed out by its own
 // fixed-budget pool or by another runtime. vrc_render grows scratch buffers
 // on demand; this variant keeps the same scratch -- the sample counters and
-// tile counter, the per-render float4 TF table and the empty-space cell map
-// -- in one fixed-size array in device global memory.
+// tile counter, the per-render alpha table, the empty-space cell map and its
+// distance field (with the passes' scratch) -- in one fixed-size array in
+// device global memory.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads the
 // library holds NOALLOC_SCRATCH_BYTES of it until the process exits. Host
@@ -37,7 +38,8 @@ constexpr size_t COUNTER_BYTES = 256;                        // 16 x u64 counter
 constexpr int MAX_TF = 4096;
 constexpr size_t ALPHA_BYTES = 256 * sizeof(float);           // alpha per alpha byte of the TF
 constexpr size_t OCC_OFFSET = COUNTER_BYTES + ALPHA_BYTES;
-constexpr size_t SCRATCH_BYTES = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS / 8;  // one bit per cell
+constexpr size_t DIST_OFFSET = OCC_OFFSET + (size_t)VRC_NOALLOC_MAX_CELLS / 8;     // one bit per cell
+constexpr size_t SCRATCH_BYTES = DIST_OFFSET + 2 * (size_t)VRC_NOALLOC_MAX_CELLS;   // distance byte + pass scratch
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
@@ -97,9 +99,14 @@ vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_ren
     if (st != VRC_OK) return st;
 
     // empty-space cells: the requested level, else the brick grid (as
-    // vrc_render); by default 8^3 (one level and no distance field here:
-    // finer cells would only make more, shorter runs)
-    const int want = p->skip_cell_size == 0 ? 8 : p->skip_cell_size;
+    // vrc_render); by default the finest of 4^3 and 8^3 whose cells fit the
+    // scratch (4^3 up to 512^3 voxels)
+    int want = p->skip_cell_size;
+    if (want == 0) {
+        want = 8;
+        for (const auto& lv : vol->levels)
+            if (lv.C == 4 && lv.d_min && lv.count() <= (long long)VRC_NOALLOC_MAX_CELLS) want = 4;
+    }
     const float* cmin = vol->d_bmin;
     const float* cmax = vol->d_bmax;
     int C = vol->L.B;
@@ -140,6 +147,12 @@ vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_ren
                                        vol->desc.rwm_offset, tf->lo, tf->hi, occ, s)) != cudaSuccess)
             return cuda_status(e);
         P.occupancy = occ;
+        // the cells' distance field: an empty run jumps the whole empty box
+        // around its cell (MIP's max-based skipping is not taken here)
+        uint8_t* dist = scratch + DIST_OFFSET;
+        if ((e = vrc::launch_occ_distance(occ, nc, dist, dist + VRC_NOALLOC_MAX_CELLS, s)) != cudaSuccess)
+            return cuda_status(e);
+        P.occ_dist = dist;
         int shift = 0;
         while ((1 << shift) < C) ++shift;
         P.cshift = shift;
