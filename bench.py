@@ -619,7 +619,7 @@ def run_large(args, warmup, ws, rank, local):
         vol.set_cache_limit(int(args.cache_gb * 1e9))
     if placement == v.PLACE_HOST and args.lod:
         t0 = time.time()
-        vol.set_lod(True)
+        vol.set_lod(args.lod_level)
         lod_build_s = time.time() - t0
     lo, hi = vol.minmax()
     keys, domain = synth.tubes_tf(5002, 2, (lo, hi))
@@ -673,11 +673,12 @@ def run_large(args, warmup, ws, rank, local):
         _, su = v.render(ctx, vol, tf, p, None, None, v.OUT_RGBA32F, out)
         vol.set_cache_limit(int(args.cache_gb * 1e9) if args.cache_gb is not None else 2**62)
         if lod_on:
-            vol.set_lod(True)
+            vol.set_lod(args.lod_level)
         nb = int(np.prod(vol.brick_minmax()[2]))
         cache = {"bricks_cached": cached, "bricks_reachable": reach, "bricks_total": nb,
                  "cache_bytes": cached * (vol.host_bytes // nb), "first_frame_ms_with_fill": first_ms,
                  "uncached_kernel_ms": su.kernel_ms, "cache_limit_gb": args.cache_gb, "lod": bool(args.lod),
+                 "lod_level": args.lod_level if args.lod else 0,
                  "frames_after_first": settle, "missed_in_last_timed_frame": missed_timed}
         if args.lod:
             cache["lod_build_s"] = lod_build_s
@@ -761,7 +762,9 @@ def main():
     ap.add_argument("--cache-gb", type=float, default=None,
                     help="large workload, host placement: device brick cache budget (default: free memory)")
     ap.add_argument("--lod", action="store_true",
-                    help="large workload, host placement: sample uncached bricks from a half-resolution level")
+                    help="large workload, host placement: sample uncached bricks from a coarser level")
+    ap.add_argument("--lod-level", type=int, default=1,
+                    help="with --lod: the level sampled for uncached bricks (k: 2^-k resolution, 1..6)")
     ap.add_argument("--placement", default="device", choices=["device", "host"],
                     help="large workload: brick pool in HBM or in pinned host memory read over NVLink-C2C")
     ap.add_argument("--skip-cell", type=int, default=0, help="empty-space cell edge (0 = library default)")
