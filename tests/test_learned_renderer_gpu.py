@@ -1,7 +1,7 @@
 """The learned render path end to end (LearnedRenderer): the probe's fallback
 decision, the fallback frame, and what the trained network gains over the
 method without it (bilinear upsampling of the same half-resolution march),
-judged against the plain full-rate render on held-out volumes."""
+compared with the plain full-rate render on held-out volumes."""
 import math
 import os
 
