@@ -500,8 +500,12 @@ int vrc_nn_conv3x3_tc(const void* in0, int C0, const void* in1, int C1, int N, i
     p.Cout = Cout;
     p.act = act;
     p.out_mode = out_mode;
-    // R output rows per tile: two sets of R accumulators in at most 256 columns
-    int R = 128 / n_tile;
+    // R output rows per tile: two sets of R accumulators in the 512 columns of
+    // tensor memory (one CTA per SM). More rows per tile give each staged
+    // input row more MMAs (up to three output rows read it), which covers the
+    // TMA round trip of the next stage when the weights leave room for few
+    // stages (64 -> 128: 147 KB of weights, 3 stages)
+    int R = 256 / n_tile;
     if (R > MAX_ROWS) R = MAX_ROWS;
     if (R < 1) R = 1;
     p.rows = R;
