@@ -46,7 +46,7 @@ constexpr int THREADS = (2 + EPI_WARPS) * 32;
 constexpr unsigned long long WAIT_NS = 200ull * 1000ull * 1000ull;
 constexpr float LEAK = 0.05f;
 constexpr int NBARS = 2 * MAX_STAGES + 2 + 2 + 2;  // full, empty, tmem full, tmem empty, weights, mma done
-constexpr size_t SMEM_BUDGET = 200 * 1024;
+constexpr size_t SMEM_BUDGET = 224 * 1024;  // of the 227 KB a CTA may hold
 
 struct TcParams {
     int N, H, W;
