@@ -233,10 +233,14 @@ __device__ __noinline__ float lod_tap(const MarchParams& P, float sx, float sy, 
     return RAW ? tri_raw<DT>(b, o, L.S, L.S * L.S, fx, fy, fz) : tri_at<DT>(b, o, L.S, L.S * L.S, fx, fy, fz);
 }
 
-// The same from a full-resolution voxel position (gradient and previous-sample taps).
+// The same from a full-resolution voxel position (gradient and previous-sample
+// taps of a brick without a cache slot). These taps read the coarser level
+// and so approximate the full-resolution values whatever the rounding of
+// their texture-space position; a fast division serves.
 template <int DT, bool RAW>
 __device__ __forceinline__ float lod_tap_voxel(const MarchParams& P, float vx, float vy, float vz) {
-    return lod_tap<DT, RAW>(P, d_(a_(vx, 0.5f), P.dimf[0]), d_(a_(vy, 0.5f), P.dimf[1]), d_(a_(vz, 0.5f), P.dimf[2]));
+    return lod_tap<DT, RAW>(P, __fdividef(vx + 0.5f, P.dimf[0]), __fdividef(vy + 0.5f, P.dimf[1]),
+                            __fdividef(vz + 0.5f, P.dimf[2]));
 }
 
 template <int DT, bool POOL>
