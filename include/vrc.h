@@ -322,8 +322,10 @@ typedef struct {
     int entry_exit_mode;        /* vrc_entry_exit_mode */
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
-    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (4; in vrc_render_noalloc
-                                   8 when the 4^3 cells exceed its scratch), else 4, 8, 16 or the brick size */
+    int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (vrc_render: 2 where the volume
+                                   holds the 2^3 level -- up to 2^26 cells -- else 4; batches: 4;
+                                   vrc_render_noalloc: the finest of 2, 4, 8 that fits its scratch), else 2,
+                                   4, 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
     int region[4];              /* x, y, w, h of the pixel window to render; w or h 0 = the whole image */
     int classification;         /* vrc_classification, default VRC_CLASSIFY_TF */
@@ -432,8 +434,9 @@ vrc_status vrc_batch_destroy(vrc_batch* b);
  * in one fixed-size array (4.5 MB) in device global memory that every GPU
  * loading the library holds until exit, and it allocates nothing.
  * Limits: at most VRC_NOALLOC_MAX_CELLS empty-space cells when skipping is on
- * (skip_cell_size 0 takes 4^3 cells up to 512^3 voxels and 8^3 cells, up to
- * a 1024^3 volume, above) and TF width <= 4096; larger requests return
+ * (skip_cell_size 0 takes 2^3 cells up to 256^3 voxels, 4^3 up to 512^3
+ * and 8^3, up to a 1024^3 volume, above) and TF width <= 4096; larger
+ * requests return
  * VRC_ERR_SCRATCH_LIMIT and render nothing. TF classification only
  * (VRC_ERR_UNSUPPORTED otherwise). Frames equal vrc_render's, but MIP's
  * max-based cell skipping is not taken, and a host-placed brick pool

@@ -68,7 +68,7 @@ def test_random_case_matches_oracle(ctx, seed):
     p.mida_gamma = float(rng.uniform(-1.0, 1.0))
     brick = [8, 16, 32][int(rng.integers(0, 3))]
     p.empty_space_skipping = int(rng.uniform() < 0.8)
-    p.skip_cell_size = [0, 4, 8, 16, brick][int(rng.integers(0, 5))]
+    p.skip_cell_size = [0, 2, 4, 8, 16, brick][int(rng.integers(0, 6))]
     spacing = tuple(float(s) for s in rng.uniform(0.5, 2.0, 3))
     ext = np.array(dims, np.float64) * np.array(spacing)
     centre = ext / 2 - 0.5 * np.array(spacing)

@@ -102,7 +102,7 @@ def test_odd_shapes_and_brick_sizes(ctx, dims, brick):
     np.testing.assert_array_equal(_bits(img), _bits(o32))
 
 
-@pytest.mark.parametrize("cell,compositing", [(4, v.DVR), (8, v.DVR), (32, v.DVR), (4, v.MIP), (4, v.ISO)])
+@pytest.mark.parametrize("cell,compositing", [(2, v.DVR), (4, v.DVR), (8, v.DVR), (32, v.DVR), (4, v.MIP), (2, v.ISO)])
 def test_sparse_volume_skipping_is_exact(ctx, cell, compositing):
     """Sparse tubes (most skip cells empty, occupied ones in thin strands):
     jumping the empty box around a cell that the distance to the nearest
@@ -131,9 +131,10 @@ def test_sparse_volume_skipping_is_exact(ctx, cell, compositing):
 
 @pytest.mark.parametrize("cell,brick,shading", [(8, 32, v.SHADE_NONE), (16, 32, v.SHADE_PHONG), (32, 32, v.SHADE_NONE),
                                                 (8, 16, v.SHADE_PHONG), (64, 64, v.SHADE_NONE),
-                                                (4, 32, v.SHADE_PHONG), (4, 16, v.SHADE_NONE)])
+                                                (4, 32, v.SHADE_PHONG), (4, 16, v.SHADE_NONE),
+                                                (2, 32, v.SHADE_PHONG), (2, 16, v.SHADE_NONE)])
 def test_empty_space_skipping_is_exact(ctx, cell, brick, shading):
-    """Skipping empty cells (4^3, 8^3, 16^3 or whole bricks) leaves every
+    """Skipping empty cells (2^3, 4^3, 8^3, 16^3 or whole bricks) leaves every
     pixel and the sample count unchanged."""
     w = synth.config2(size=(130, 128, 127), image=(256, 192))
     p = w.params(shading=shading, skip_cell_size=cell)

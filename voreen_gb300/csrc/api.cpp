@@ -336,15 +336,17 @@ vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* des
     if ((e = vrc::launch_brick_build(lin, desc->dtype, L, v->d_bricks, ctx->stream)) != cudaSuccess ||
         (e = vrc::launch_brick_minmax(v->d_bricks, desc->dtype, L, v->d_bmin, v->d_bmax, ctx->stream)) != cudaSuccess)
         return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: kernel: ") + cudaGetErrorString(e));
-    // finer empty-space cells (4^3, 8^3, 16^3) below the brick size
-    for (int li = 0; li < 3; ++li) {
-        const int C = 4 << li;
+    // finer empty-space cells (2^3, 4^3, 8^3, 16^3) below the brick size;
+    // 2^3 cells (8 bytes of tables per 8 voxels) only up to 2^26 of them
+    // (a 512^3 volume, 512 MB of tables)
+    for (int li = 0; li < 4; ++li) {
+        const int C = 2 << li;
         if (C >= brick_size) continue;
         vrc_cell_level& lv = v->levels[li];
         lv.C = C;
         for (int i = 0; i < 3; ++i) lv.nc[i] = (desc->dims[i] + C - 1) / C;
-        if (lv.count() >= (1LL << 32)) {  // beyond the march's 32-bit cell index: skip by bricks
-            lv.C = 0;
+        if (lv.count() >= (1LL << 32) || (C == 2 && lv.count() > (1LL << 26))) {
+            lv.C = 0;  // beyond the march's 32-bit cell index, or the 2^3 table budget
             continue;
         }
         if ((e = cudaMalloc((void**)&lv.d_min, lv.count() * sizeof(float))) != cudaSuccess ||
@@ -813,9 +815,9 @@ vrc_status check_params(vrc_context* ctx, const vrc_render_params* p) {
     if (p->tile_width != 0 && p->tile_width != 1 && p->tile_width != 2 && p->tile_width != 4 && p->tile_width != 8 &&
         p->tile_width != 16 && p->tile_width != 32)
         return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: tile_width must be 0, 1, 2, 4, 8, 16 or 32");
-    if (p->skip_cell_size != 0 && p->skip_cell_size != 4 && p->skip_cell_size != 8 && p->skip_cell_size != 16 &&
-        p->skip_cell_size != 32 && p->skip_cell_size != 64)
-        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 4, 8, 16, 32 or 64");
+    if (p->skip_cell_size != 0 && p->skip_cell_size != 2 && p->skip_cell_size != 4 && p->skip_cell_size != 8 &&
+        p->skip_cell_size != 16 && p->skip_cell_size != 32 && p->skip_cell_size != 64)
+        return ::fail(ctx, VRC_ERR_INVALID_ARG, "vrc_render: skip_cell_size must be 0, 2, 4, 8, 16, 32 or 64");
     return VRC_OK;
 }
 
@@ -1176,8 +1178,9 @@ vrc_status render_impl(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf
     int occ_launches = 0;
     if (p->empty_space_skipping) {
         // skip cells: the requested edge if the volume holds that level, else
-        // the brick; by default 4^3, whose runs the distance field keeps long
-        const int want = p->skip_cell_size == 0 ? 4 : p->skip_cell_size;
+        // the brick; by default the finest level held of 2^3 and 4^3, whose
+        // runs the distance field keeps long
+        const int want = p->skip_cell_size == 0 ? vrc::default_skip_cell(vol) : p->skip_cell_size;
         const float* cmin = vol->d_bmin;
         const float* cmax = vol->d_bmax;
         int C = vol->L.B;

@@ -156,8 +156,10 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         R.P.out = it.out;
         R.P.out_format = it.out_format;
         if (it.params.empty_space_skipping) {
-            // as vrc_render: 4^3 cells by default, and the cells' distance
-            // field, so an empty run jumps the whole empty box around its cell
+            // 4^3 cells by default (the graph rebuilds every request's cell map
+            // and distance field on each launch, so 2^3 cells cost more there
+            // than they save), and the cells' distance field, so an empty run
+            // jumps the whole empty box around its cell
             const float *mn, *mx;
             int C, nc[3];
             pick_level(it.volume, it.params.skip_cell_size == 0 ? 4 : it.params.skip_cell_size, &mn, &mx, &C, nc);

@@ -99,13 +99,13 @@ vrc_status render_noalloc(const vrc_volume* vol, const vrc_tf* tf, const vrc_ren
     if (st != VRC_OK) return st;
 
     // empty-space cells: the requested level, else the brick grid (as
-    // vrc_render); by default the finest of 4^3 and 8^3 whose cells fit the
-    // scratch (4^3 up to 512^3 voxels)
+    // vrc_render); by default the finest of 2^3, 4^3 and 8^3 whose cells fit
+    // the scratch (2^3 up to 256^3 voxels, 4^3 up to 512^3)
     int want = p->skip_cell_size;
     if (want == 0) {
         want = 8;
         for (const auto& lv : vol->levels)
-            if (lv.C == 4 && lv.d_min && lv.count() <= (long long)VRC_NOALLOC_MAX_CELLS) want = 4;
+            if (lv.C < want && lv.C >= 2 && lv.d_min && lv.count() <= (long long)VRC_NOALLOC_MAX_CELLS) want = lv.C;
     }
     const float* cmin = vol->d_bmin;
     const float* cmax = vol->d_bmax;

@@ -235,6 +235,7 @@ struct vrc_volume {
     vrc_context* ctx = nullptr;
     uint64_t uid = vrc::next_uid();
     vrc_volume_desc desc{};
+
     vrc::BrickLayout L{};
     void* d_bricks = nullptr;     // device address of the brick pool
     void* h_bricks = nullptr;     // the pool's pinned host allocation (VRC_PLACE_HOST), else null
@@ -274,10 +275,20 @@ struct vrc_volume {
     bool lod_on = false;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
-    vrc_cell_level levels[3];  // skip cells of edge 4, 8 and 16 (when smaller than the brick)
+    vrc_cell_level levels[4];  // skip cells of edge 2, 4, 8 and 16 (when smaller than the brick; 2 up to 2^26 cells)
     size_t bytes = 0;
     float vmin = 0.f, vmax = 0.f;
 };
+
+namespace vrc {
+// The default skip-cell edge of a volume: 2 where it holds the 2^3 level,
+// else 4.
+inline int default_skip_cell(const vrc_volume* v) {
+    for (const auto& lv : v->levels)
+        if (lv.C == 2 && lv.d_min) return 2;
+    return 4;
+}
+}  // namespace vrc
 
 struct vrc_tf {
     vrc_context* ctx = nullptr;
