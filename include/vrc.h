@@ -323,7 +323,7 @@ typedef struct {
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
     int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (vrc_render: 2 where the volume
-                                   holds the 2^3 level -- up to 2^26 cells -- else 4; batches: 4;
+                                   holds the 2^3 level -- up to 2^30 cells -- else 4; batches: 4;
                                    vrc_render_noalloc: the finest of 2, 4, 8 that fits its scratch), else 2,
                                    4, 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */

@@ -86,6 +86,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         tune = [f"-D{k}={int(os.environ[k])}" for k in ("VRC_MARCH_MIN_BLOCKS",)
                 if src.startswith("march") and os.environ.get(k)]
         tune += [f"-DVRC_OCC_DIST_CAP={int(os.environ['VRC_OCC_DIST_CAP'])}"] if os.environ.get("VRC_OCC_DIST_CAP") else []
+        tune += [f"-DVRC_CELL2_LOG2_MAX={int(os.environ['VRC_CELL2_LOG2_MAX'])}"] if os.environ.get("VRC_CELL2_LOG2_MAX") else []
         extra = extra + tune
         # an object is rebuilt when its tuning flags differ from the last build's
         stamp = obj + ".flags"

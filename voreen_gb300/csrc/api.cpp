@@ -337,15 +337,15 @@ vrc_status vrc_volume_upload_placed(vrc_context* ctx, const vrc_volume_desc* des
         (e = vrc::launch_brick_minmax(v->d_bricks, desc->dtype, L, v->d_bmin, v->d_bmax, ctx->stream)) != cudaSuccess)
         return cleanup(VRC_ERR_CUDA, std::string("vrc_volume_upload: kernel: ") + cudaGetErrorString(e));
     // finer empty-space cells (2^3, 4^3, 8^3, 16^3) below the brick size;
-    // 2^3 cells (8 bytes of tables per 8 voxels) only up to 2^26 of them
-    // (a 512^3 volume, 512 MB of tables)
+    // 2^3 cells (8 bytes of tables per 8 voxels) only up to
+    // 2^VRC_CELL2_LOG2_MAX of them
     for (int li = 0; li < 4; ++li) {
         const int C = 2 << li;
         if (C >= brick_size) continue;
         vrc_cell_level& lv = v->levels[li];
         lv.C = C;
         for (int i = 0; i < 3; ++i) lv.nc[i] = (desc->dims[i] + C - 1) / C;
-        if (lv.count() >= (1LL << 32) || (C == 2 && lv.count() > (1LL << 26))) {
+        if (lv.count() >= (1LL << 32) || (C == 2 && lv.count() > (1LL << VRC_CELL2_LOG2_MAX))) {
             lv.C = 0;  // beyond the march's 32-bit cell index, or the 2^3 table budget
             continue;
         }

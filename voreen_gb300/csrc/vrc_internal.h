@@ -275,10 +275,16 @@ struct vrc_volume {
     bool lod_on = false;
     float* d_bmin = nullptr;
     float* d_bmax = nullptr;
-    vrc_cell_level levels[4];  // skip cells of edge 2, 4, 8 and 16 (when smaller than the brick; 2 up to 2^26 cells)
+    vrc_cell_level levels[4];  // skip cells of edge 2, 4, 8 and 16 (when smaller than the brick; 2 up to 2^30 cells)
     size_t bytes = 0;
     float vmin = 0.f, vmax = 0.f;
 };
+
+// The 2^3 cell level is built up to 2^VRC_CELL2_LOG2_MAX cells (2^30: an
+// 8-Gvoxel volume, 8.6 GB of min/max tables).
+#ifndef VRC_CELL2_LOG2_MAX
+#define VRC_CELL2_LOG2_MAX 30
+#endif
 
 namespace vrc {
 // The default skip-cell edge of a volume: 2 where it holds the 2^3 level,
