@@ -323,7 +323,7 @@ typedef struct {
     int quantize_entry_exit;    /* analytic mode: round coordinates to k/65535 like RGBA16 targets */
     int empty_space_skipping;   /* skip cells whose TF opacity is zero (exact: results unchanged) */
     int skip_cell_size;         /* empty-space cell edge in voxels: 0 = default (vrc_render: 2 where the volume
-                                   holds the 2^3 level -- up to 2^30 cells -- else 4; batches: 4;
+                                   holds the 2^3 level -- up to 2^30 cells -- else 4, also for batches;
                                    vrc_render_noalloc: the finest of 2, 4, 8 that fits its scratch), else 2,
                                    4, 8, 16 or the brick size */
     int tile_width;             /* ray tile per warp: tile_width x (32 / tile_width) pixels; 0 = default (8) */
@@ -378,9 +378,11 @@ vrc_status vrc_image_rescale(vrc_context* ctx, const void* d_src, int w, int h, 
 /* ---- batched persistent render ----------------------------------------------
  * No counterpart in the reference (it renders one request per processor
  * call). Many requests -- uneven volumes, dtypes and image sizes -- march in
- * ONE persistent kernel launch; the whole per-launch sequence (state reset,
- * every request's empty-space maps, the march) is captured once as a CUDA
- * graph on the context's stream and replayed by vrc_batch_launch. All items
+ * ONE persistent kernel launch; every request's empty-space maps are built
+ * once, when the batch is created (volumes and TFs do not change after
+ * creation), and the per-launch sequence (state reset, the march) is
+ * captured as a CUDA graph on the context's stream and replayed by
+ * vrc_batch_launch. All items
  * share compositing and shading and use analytic entry/exit (the camera in
  * their params); each writes its own device image. */
 typedef struct {

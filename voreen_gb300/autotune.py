@@ -19,7 +19,7 @@ from . import EE_ANALYTIC, OUT_RGBA8, TransferFunction, Volume, render
 
 TILE_WIDTHS = (4, 8, 16)
 BRICKS = (16, 32)
-SKIP_CELLS = (4, 8, 16)
+SKIP_CELLS = (2, 4, 8, 16)
 
 
 def class_key(dtype: int, dims, width: int, height: int) -> str:

@@ -156,13 +156,13 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         R.P.out = it.out;
         R.P.out_format = it.out_format;
         if (it.params.empty_space_skipping) {
-            // 4^3 cells by default (the graph rebuilds every request's cell map
-            // and distance field on each launch, so 2^3 cells cost more there
-            // than they save), and the cells' distance field, so an empty run
-            // jumps the whole empty box around its cell
+            // as vrc_render: the finest of 2^3 and 4^3 cells by default, and
+            // the cells' distance field, so an empty run jumps the whole empty
+            // box around its cell
             const float *mn, *mx;
             int C, nc[3];
-            pick_level(it.volume, it.params.skip_cell_size == 0 ? 4 : it.params.skip_cell_size, &mn, &mx, &C, nc);
+            pick_level(it.volume, it.params.skip_cell_size == 0 ? vrc::default_skip_cell(it.volume) : it.params.skip_cell_size,
+                       &mn, &mx, &C, nc);
             const long long cells = (long long)nc[0] * nc[1] * nc[2];
             uint32_t* map = nullptr;
             uint8_t* dist = nullptr;
@@ -214,28 +214,36 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, cudaGetErrorString(e));
     }
-    // scratch of the distance passes, shared by the requests (the graph runs them in order)
-    uint8_t* dist_tmp = nullptr;
-    if (max_cells > 0) {
+    // Empty-space maps, built once: a request's cell map and distance field
+    // depend only on its volume, TF and cell edge, none of which changes
+    // after creation, so launches replay the march alone.
+    cudaStream_t s = ctx->stream;
+    if (!occ_jobs.empty()) {
+        uint8_t* dist_tmp = nullptr;  // scratch of the distance passes, shared by the requests in turn
         if ((e = cudaMalloc((void**)&dist_tmp, (size_t)max_cells)) != cudaSuccess) {
             release(b);
             return bfail(ctx, VRC_ERR_OUT_OF_MEMORY, "vrc_batch_create: distance scratch allocation");
         }
-        b->dist.push_back(dist_tmp);
+        cudaError_t me = cudaSuccess;
+        for (const Occ& j : occ_jobs) {
+            if (me == cudaSuccess)
+                me = vrc::launch_occupancy(j.mn, j.mx, j.cells, j.tf->d_prefix, j.tf->width, j.vol->desc.rwm_scale,
+                                           j.vol->desc.rwm_offset, j.tf->lo, j.tf->hi, j.map, s);
+            if (me == cudaSuccess) me = vrc::launch_occ_distance(j.map, j.nc, j.dist, dist_tmp, s);
+        }
+        if (me == cudaSuccess) me = cudaStreamSynchronize(s);
+        cudaFree(dist_tmp);
+        if (me != cudaSuccess) {
+            release(b);
+            return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: empty-space maps: ") + cudaGetErrorString(me));
+        }
     }
-    // capture: state reset + start stamp, empty-space maps, one persistent march
-    cudaStream_t s = ctx->stream;
+    // capture: state reset + start stamp, one persistent march
     if ((e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) {
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture: ") + cudaGetErrorString(e));
     }
     cudaError_t ce = vrc::launch_batch_begin(b->d_state, n, s);
-    for (const Occ& j : occ_jobs) {
-        if (ce == cudaSuccess)
-            ce = vrc::launch_occupancy(j.mn, j.mx, j.cells, j.tf->d_prefix, j.tf->width, j.vol->desc.rwm_scale,
-                                       j.vol->desc.rwm_offset, j.tf->lo, j.tf->hi, j.map, s);
-        if (ce == cudaSuccess) ce = vrc::launch_occ_distance(j.map, j.nc, j.dist, dist_tmp, s);
-    }
     if (ce == cudaSuccess)
         ce = vrc::launch_march_batch(b->d_reqs, n, b->d_prefix, b->total_tiles, b->d_state, b->compositing,
                                      b->shading, ctx->num_sms, s);
@@ -245,7 +253,7 @@ vrc_status create_batch(vrc_context* ctx, const vrc_batch_item* all, int n_items
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: capture failed: ") +
                                             cudaGetErrorString(ce != cudaSuccess ? ce : e));
     }
-    b->kernels = 2 + 4 * (int)occ_jobs.size();
+    b->kernels = 2;
     if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) {
         release(b);
         return bfail(ctx, VRC_ERR_CUDA, std::string("vrc_batch_create: instantiate: ") + cudaGetErrorString(e));
