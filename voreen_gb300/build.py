@@ -69,10 +69,12 @@ def _stale(target: str, deps: list[str]) -> bool:
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
-    """Compile and link libvrc.so. Environment tuning knobs for the march
-    kernel: VRC_MARCH_MIN_BLOCKS (minimum resident CTAs per SM, bounds the
-    registers) and VRC_OCC_DIST_CAP (largest empty-space distance stored per
-    cell, at most 255)."""
+    """Compile and link libvrc.so. Environment tuning knobs:
+    VRC_MARCH_MIN_BLOCKS (march kernels: minimum resident CTAs per SM, bounds
+    the registers; default 3), VRC_OCC_DIST_CAP (largest empty-space distance
+    stored per cell, at most 255; default 16) and VRC_CELL2_LOG2_MAX (the 2^3
+    cell level is built for volumes of at most 2^this cells; default 30).
+    Objects are rebuilt when their knobs differ from the last build's."""
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hdrs = _headers()
