@@ -56,10 +56,10 @@ __device__ __forceinline__ float d_(float a, float b) { return __fdiv_rn(a, b); 
 //   v / D = v (2^-k + 2^-2k) + v (2^-3k [+ 2^-4k + 2^-5k for k = 8]) + tail,
 // tail >= 0 and smaller than the spacing of the fused sum's grid (2^-48 for
 // k = 16, 2^-40 for k = 8). The fused sum lies on that grid, as do all
-// rounding midpoints of the result, and it is never a midpoint itself (v
-// would need a factor 2^(e + 3k) for a result in [2^e, 2^(e+1))), so the tail
-// cannot change the rounding: fma(v, A, v * B) = RN(v / D) for every v in
-// [0, D]. (Checked exhaustively by the test suite.) v as a float: the bits
+// rounding midpoints of the result, and it is never a midpoint itself: for a
+// result in [2^e, 2^(e+1)), v would need a factor 2^(e + 24) (k = 16) or
+// 2^(e + 16) (k = 8), more than v < 2^(e + k + 1) holds. So the tail cannot
+// change the rounding: fma(v, A, v * B) = RN(v / D) for every v in [0, D]. (Checked exhaustively by the test suite.) v as a float: the bits
 // 0x4B000000 | v are the float 2^23 + v.
 __device__ __forceinline__ float small_uint_to_float(unsigned v) {
     return __fsub_rn(__int_as_float(0x4B000000u | v), 8388608.f);
@@ -682,11 +682,13 @@ __device__ float4 march_ray(const MarchParams& P, const uchar4* __restrict__ s_t
         bool skip_after = false;  // pre-integration: skip the samples after this one in its empty cell
         float skip_lim = 0.f;
         if (P.occupancy) {
-            // Two skip levels. The fine cell (8^3 by default) decides whether
-            // the sample is skipped at all: a coarse (brick-sized) cell holds
-            // its fine cells' value ranges, so it can be empty only where the
-            // fine cell is, and its word is read only then, to jump the whole
-            // coarse cell at once.
+            // The fine cell (2^3 or 4^3 by default) decides whether the sample
+            // is skipped at all. A TF-empty cell with the cells' distance field
+            // given jumps the whole empty box around it; otherwise (MIP's
+            // max-based skipping, pre-integration with steps of a voxel or
+            // more) a coarse (brick-sized) cell, which holds its fine cells'
+            // value ranges and so can be empty only where the fine cell is,
+            // is read to jump the whole brick at once.
             float tsafe = 0.f;
             bool empty = false;
             // cell and brick indices fit 32 bits (checked when the volume is uploaded)
