@@ -124,8 +124,10 @@ typedef struct {
 } vrc_volume_desc;
 
 /* Upload a linear x-fastest volume into the bricked device layout and build
- * the per-brick min/max table. `voxels_on_device` != 0 means `voxels` is a
- * device pointer. brick_size: 0 = default (32); otherwise 8, 16, 32 or 64. */
+ * the per-brick min/max table and the empty-space cell tables (2^3 cells up
+ * to 2^30 of them -- 1 byte of tables per voxel --, 4^3, 8^3, 16^3 below the
+ * brick size). `voxels_on_device` != 0 means `voxels` is a device pointer.
+ * brick_size: 0 = default (32); otherwise 8, 16, 32 or 64. */
 vrc_status vrc_volume_upload(vrc_context* ctx, const vrc_volume_desc* desc, const void* voxels,
                              int voxels_on_device, int brick_size, vrc_volume** out);
 /* Brick-pool placement: device memory (HBM), or pinned host memory that
