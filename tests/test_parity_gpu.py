@@ -102,6 +102,23 @@ def test_odd_shapes_and_brick_sizes(ctx, dims, brick):
     np.testing.assert_array_equal(_bits(img), _bits(o32))
 
 
+def test_default_skip_cell_is_the_finest_level(ctx):
+    """skip_cell_size 0 takes the 2^3 cells where the volume holds them: the
+    same fetched samples and pixels as an explicit 2, fewer fetches than 4^3
+    cells, and every frame equal to the render without skipping."""
+    w = synth.config2(size=(96, 88, 80), image=(200, 150))
+    tf = v.TransferFunction.bake(w.tf_keys, w.tf_width)
+    c = Case(ctx, w.voxels, tf, w.domain, w.params(), w.spacing)
+    a, sa = c.gpu(skip_cell_size=0)
+    b, sb = c.gpu(skip_cell_size=2)
+    d, sd = c.gpu(skip_cell_size=4)
+    e, se = c.gpu(empty_space_skipping=0, skip_cell_size=0)
+    for img in (b, d, e):
+        np.testing.assert_array_equal(_bits(a), _bits(img))
+    assert sa.samples_fetched == sb.samples_fetched < sd.samples_fetched < se.samples_fetched
+    assert sa.samples == sb.samples == sd.samples == se.samples
+
+
 @pytest.mark.parametrize("cell,compositing", [(2, v.DVR), (4, v.DVR), (8, v.DVR), (32, v.DVR), (4, v.MIP), (2, v.ISO)])
 def test_sparse_volume_skipping_is_exact(ctx, cell, compositing):
     """Sparse tubes (most skip cells empty, occupied ones in thin strands):
