@@ -100,7 +100,7 @@ def test_network_beats_bilinear_on_held_out_volumes(ctx, net):
     ev = learned.evaluate(ctx, net, vols, views=3, seed=777)
     gain = [e["psnr_net"] - e["psnr_bilinear"] for e in ev]
     assert min(gain) > 0.0, gain
-    assert np.mean(gain) > 0.2, gain
+    assert np.mean(gain) > 1.0, gain
     for vol, _, _ in vols:
         vol.close()
 
