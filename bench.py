@@ -735,7 +735,7 @@ def run_large(args, warmup, ws, rank, local):
             "parity_band": {"rows": [r0, r0 + 2], "max_abs": float(band.max()), "oracle_samples":
                             int(s32[r0:r0 + 2].sum()), "cpu_seconds": cpu_s},
             "learned": {"at_bound": learned_res[40.0], "without_fallback": learned_res[0.0],
-                        "weights": "upsampler_tubes.npz (held-out tube views: 33.8 dB learned, 32.7 dB bilinear)"},
+                        "weights": "upsampler_tubes.npz (held-out tube views: 34.0 dB learned, 32.7 dB bilinear)"},
             "gpu_launches": steps * launches_per_frame, "clocks": clocks}
     if rank == 0:
         print(json.dumps(line))
