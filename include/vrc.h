@@ -370,6 +370,13 @@ vrc_status vrc_render(vrc_context* ctx, const vrc_volume* vol, const vrc_tf* tf,
  * march's gathers are compared with beside the HBM copy peak. */
 vrc_status vrc_measure_l2_read(vrc_context* ctx, size_t bytes, int reps, float* gbs);
 
+/* Diagnostics: the empty-space distance field the march skips by, computed
+ * from a device bitmap of nx x ny x nz cells (bit i of word i / 32 set =
+ * occupied, cells x-fastest): d_out[i] = the Chebyshev distance in cells
+ * from cell i to the nearest occupied cell, capped at 16 in the default
+ * build (0 for occupied cells). Device pointers; runs on the context stream and returns when done. */
+vrc_status vrc_occupancy_distance(vrc_context* ctx, const uint32_t* d_bits, int nx, int ny, int nz, uint8_t* d_out);
+
 /* Bilinear rescale of a device RGBA image (w x h) to W x H on the context
  * stream: VolumeRaycaster::rescaleRendering (GL_LINEAR, clamp to edge) as
  * SingleVolumeRaycaster applies it after an interaction-coarseness render.

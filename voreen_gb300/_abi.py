@@ -101,6 +101,7 @@ SIGNATURES = {
     "vrc_volume_cache_info": (C.c_int, [VP, P(C.c_longlong), P(C.c_longlong), P(C.c_longlong)]),
     "vrc_volume_set_lod": (C.c_int, [VP, C.c_int]),
     "vrc_measure_l2_read": (C.c_int, [VP, C.c_size_t, C.c_int, P(C.c_float)]),
+    "vrc_occupancy_distance": (C.c_int, [VP, VP, C.c_int, C.c_int, C.c_int, VP]),
     "vrc_tf_read_tfi": (C.c_int, [C.c_char_p, P(TfiInfo), P(TFKey), C.c_int]),
     "vrc_volume_set_cache_upload_budget": (C.c_int, [VP, C.c_size_t]),
     "vrc_volume_minmax": (C.c_int, [VP, P(C.c_float), P(C.c_float)]),

@@ -24,6 +24,25 @@ __global__ void l2_read_kernel(const uint4* __restrict__ buf, long long n, int r
 
 }  // namespace
 
+extern "C" vrc_status vrc_occupancy_distance(vrc_context* ctx, const uint32_t* d_bits, int nx, int ny, int nz,
+                                             uint8_t* d_out) {
+    if (!ctx || !d_bits || !d_out || nx < 1 || ny < 1 || nz < 1) return VRC_ERR_INVALID_ARG;
+    const long long n = (long long)nx * ny * nz;
+    if (n >= (1LL << 32)) return VRC_ERR_INVALID_ARG;
+    const int nc[3] = {nx, ny, nz};
+    uint8_t* tmp = nullptr;
+    cudaError_t e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaMalloc(&tmp, (size_t)n);
+    if (e == cudaSuccess) e = vrc::launch_occ_distance(d_bits, nc, d_out, tmp, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    cudaFree(tmp);
+    if (e != cudaSuccess) {
+        ctx->last_error = std::string("vrc_occupancy_distance: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? VRC_ERR_OUT_OF_MEMORY : VRC_ERR_CUDA;
+    }
+    return VRC_OK;
+}
+
 extern "C" vrc_status vrc_measure_l2_read(vrc_context* ctx, size_t bytes, int reps, float* gbs) {
     if (!ctx || !gbs || bytes < (1u << 20) || reps < 1) return VRC_ERR_INVALID_ARG;
     *gbs = 0.f;
